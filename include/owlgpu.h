@@ -1,0 +1,709 @@
+/*
+ * owlgpu.h -- C ABI of libowlgpu, a GB300 (sm_103a) implementation of Owl's
+ * dense-ndarray convolution and pooling stubs.
+ *
+ * Two families of entry points replace the C stubs that Owl binds from
+ * src/owl/core/owl_ndarray_conv.ml and src/owl/core/owl_ndarray_pool.ml:
+ *
+ *  1. Host drop-in, `owl_<kind>_ndarray_<op>`: the OCaml `external` name of
+ *     the stub it replaces, the same argument order, meaning and units, with
+ *     Bigarray values replaced by their data pointers (host memory) and OCaml
+ *     ints by `long`.  The call copies the inputs to the GPU, runs, copies the
+ *     outputs back and returns when the outputs are in host memory, exactly
+ *     like the synchronous CPU stub.  Outputs are fully overwritten (the CPU
+ *     stubs memset them first), so `_ ~out` callers see the same behaviour.
+ *
+ *  2. Device resident, `owlgpu_<kind>_ndarray_<op>`: the same arguments with
+ *     device pointers, followed by `precision` (float32 only; ignored for
+ *     float64) and a `cudaStream_t` passed as `void *` (NULL = the legacy
+ *     default stream).  The call is asynchronous on that stream.
+ *
+ * Every entry point returns OWLGPU_OK (0) or a negative status; the reason is
+ * available from owlgpu_last_error() on the calling thread.  Nothing aborts
+ * the process.  The Owl stubs return unit and exit(1) on allocation failure
+ * (owl_ndarray_conv_impl.h:300); the OCaml binding turns a negative status
+ * into an exception instead.
+ *
+ * Layouts are Owl's row-major ones: input [batch][cols][rows]([dpts])[ch],
+ * kernel [kcols][krows]([kdpts])[in_ch][out_ch].  "row_stride"/"col_stride"
+ * follow the stub parameter names (col = dim 1, row = dim 2).
+ */
+#ifndef OWLGPU_H
+#define OWLGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+/* ---- status, precision, housekeeping ---------------------------------- */
+
+#define OWLGPU_OK              0
+#define OWLGPU_ERR_INVALID    -1 /* bad shape / argument                  */
+#define OWLGPU_ERR_CUDA       -2 /* CUDA runtime error                    */
+#define OWLGPU_ERR_NOMEM      -3 /* device or pinned allocation failed    */
+#define OWLGPU_ERR_UNSUPPORTED -4
+#define OWLGPU_ERR_TIMEOUT    -5 /* a bounded device-side wait gave up    */
+
+/* Arithmetic used by float32 convolutions.  FP32 is the plain SIMT kernel
+ * (results within 1e-4 relative of Owl's S.conv2d); TF32 and BF16 run on the
+ * tcgen05 tensor cores with FP32 accumulation; BF16X3 splits each operand
+ * into bf16 hi + lo parts and sums hi*hi + hi*lo + lo*hi on the tensor cores
+ * (close to FP32 accuracy).  Float64 always runs FP64 SIMT kernels. */
+#define OWLGPU_PREC_FP32   0
+#define OWLGPU_PREC_TF32   1
+#define OWLGPU_PREC_BF16   2
+#define OWLGPU_PREC_BF16X3 3
+
+/* Last error message of the calling thread ("" if none). */
+const char *owlgpu_last_error(void);
+/* Library version string. */
+const char *owlgpu_version(void);
+/* Process-wide precision used by the host drop-in float32 convolutions.
+ * The initial value comes from the environment variable OWLGPU_PRECISION
+ * (fp32 | tf32 | bf16 | bf16x3), default fp32. Returns the previous value. */
+int owlgpu_set_precision(int precision);
+int owlgpu_get_precision(void);
+/* Number of kernel launches issued by this library since the process began
+ * (all threads).  Lets a caller count GPU work inside a timed region. */
+uint64_t owlgpu_launch_count(void);
+/* Device ordinal used by the host drop-in entry points (default 0). */
+int owlgpu_set_device(int device);
+/* Release cached device/pinned staging memory held by the host drop-in. */
+int owlgpu_trim(void);
+
+/* ======================================================================
+ * Convolution.  Owl kernel families: GEBP `spatial*` for 2-D
+ * (owl_ndarray_conv.ml:257-282), `cuboid_*_im2col` for 3-D
+ * (owl_ndarray_conv.ml:826-851), `dilated_*_im2col` (owl_ndarray_conv.ml:
+ * 2540-2596).  All of them map onto the same GPU implementation.
+ * ====================================================================== */
+
+/* replaces stub_float32_ndarray_conv_spatial_native
+ * (owl_ndarray_conv.ml:13, owl_ndarray_conv_impl.h:246-253).
+ * padding: 0 = SAME, 1 = VALID. row/col_in_stride are ignored as in Owl. */
+int owl_float32_ndarray_conv_spatial(
+    const float *input, const float *kernel, float *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride);
+/* replaces stub_float64_ndarray_conv_spatial_native (owl_ndarray_conv.ml:34) */
+int owl_float64_ndarray_conv_spatial(
+    const double *input, const double *kernel, double *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride);
+
+/* replaces stub_float32_ndarray_conv_spatial_backward_input_native
+ * (owl_ndarray_conv.ml:97, owl_ndarray_conv_impl.h:465-472).
+ * First argument is dX (written); `output` is dY.  The padding is re-derived
+ * from the shapes as in owl_ndarray_conv_impl.h:502-505. */
+int owl_float32_ndarray_conv_spatial_backward_input(
+    float *input_grad, const float *kernel, const float *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+/* replaces stub_float64_ndarray_conv_spatial_backward_input_native (:117) */
+int owl_float64_ndarray_conv_spatial_backward_input(
+    double *input_grad, const double *kernel, const double *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+
+/* replaces stub_float32_ndarray_conv_spatial_backward_kernel_native
+ * (owl_ndarray_conv.ml:177, owl_ndarray_conv_impl.h:675-682).
+ * Second argument is dW (written). */
+int owl_float32_ndarray_conv_spatial_backward_kernel(
+    const float *input, float *kernel_grad, const float *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+/* replaces stub_float64_ndarray_conv_spatial_backward_kernel_native (:197) */
+int owl_float64_ndarray_conv_spatial_backward_kernel(
+    const double *input, double *kernel_grad, const double *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+
+/* replace the im2col spelling of the same three 2-D stubs
+ * (owl_ndarray_conv.ml:287, :308, :328 and float64 :415, :436, :456).
+ * Identical semantics to the GEBP entry points above. */
+int owl_float32_ndarray_conv_spatial_im2col(
+    const float *input, const float *kernel, float *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride);
+int owl_float64_ndarray_conv_spatial_im2col(
+    const double *input, const double *kernel, double *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride);
+int owl_float32_ndarray_conv_spatial_backward_input_im2col(
+    float *input_grad, const float *kernel, const float *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_float64_ndarray_conv_spatial_backward_input_im2col(
+    double *input_grad, const double *kernel, const double *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_float32_ndarray_conv_spatial_backward_kernel_im2col(
+    const float *input, float *kernel_grad, const float *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_float64_ndarray_conv_spatial_backward_kernel_im2col(
+    const double *input, double *kernel_grad, const double *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+
+/* replaces stub_{float32,float64}_ndarray_conv_cuboid_im2col_native
+ * (owl_ndarray_conv.ml:348/:476, owl_ndarray_conv_impl.h:1211-1219). */
+int owl_float32_ndarray_conv_cuboid_im2col(
+    const float *input, const float *kernel, float *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long padding);
+int owl_float64_ndarray_conv_cuboid_im2col(
+    const double *input, const double *kernel, double *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long padding);
+/* replaces stub_*_ndarray_conv_cuboid_backward_input_im2col_native
+ * (owl_ndarray_conv.ml:393/:521, owl_ndarray_conv_impl.h:1456-1463). */
+int owl_float32_ndarray_conv_cuboid_backward_input_im2col(
+    float *input_grad, const float *kernel, const float *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride);
+int owl_float64_ndarray_conv_cuboid_backward_input_im2col(
+    double *input_grad, const double *kernel, const double *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride);
+/* replaces stub_*_ndarray_conv_cuboid_backward_kernel_im2col_native
+ * (owl_ndarray_conv.ml:371/:499, owl_ndarray_conv_impl.h:1331-1338). */
+int owl_float32_ndarray_conv_cuboid_backward_kernel_im2col(
+    const float *input, float *kernel_grad, const float *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride);
+int owl_float64_ndarray_conv_cuboid_backward_kernel_im2col(
+    const double *input, double *kernel_grad, const double *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride);
+
+/* replaces stub_*_ndarray_conv_dilated_spatial_im2col_native
+ * (owl_ndarray_conv.ml:1992, owl_ndarray_conv_impl.h:3097-3103):
+ * row/col_in_stride are the dilation rates. */
+int owl_float32_ndarray_conv_dilated_spatial_im2col(
+    const float *input, const float *kernel, float *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride);
+int owl_float64_ndarray_conv_dilated_spatial_im2col(
+    const double *input, const double *kernel, double *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride);
+/* replaces stub_*_ndarray_conv_dilated_spatial_backward_input_im2col_native
+ * (owl_ndarray_conv.ml:2033, owl_ndarray_conv_impl.h:3317-3323). */
+int owl_float32_ndarray_conv_dilated_spatial_backward_input_im2col(
+    float *input_grad, const float *kernel, const float *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_float64_ndarray_conv_dilated_spatial_backward_input_im2col(
+    double *input_grad, const double *kernel, const double *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+/* replaces stub_*_ndarray_conv_dilated_spatial_backward_kernel_im2col_native
+ * (owl_ndarray_conv.ml:2013, owl_ndarray_conv_impl.h:3203-3209). */
+int owl_float32_ndarray_conv_dilated_spatial_backward_kernel_im2col(
+    const float *input, float *kernel_grad, const float *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_float64_ndarray_conv_dilated_spatial_backward_kernel_im2col(
+    const double *input, double *kernel_grad, const double *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+
+/* replaces stub_*_ndarray_conv_dilated_cuboid_im2col_native
+ * (owl_ndarray_conv.ml:2053, owl_ndarray_conv_impl.h:3417-3426). */
+int owl_float32_ndarray_conv_dilated_cuboid_im2col(
+    const float *input, const float *kernel, float *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long dpt_in_stride, long row_in_stride,
+    long col_in_stride, long padding);
+int owl_float64_ndarray_conv_dilated_cuboid_im2col(
+    const double *input, const double *kernel, double *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long dpt_in_stride, long row_in_stride,
+    long col_in_stride, long padding);
+/* replaces stub_*_ndarray_conv_dilated_cuboid_backward_input_im2col_native
+ * (owl_ndarray_conv.ml:2104, owl_ndarray_conv_impl.h:3678-3686). */
+int owl_float32_ndarray_conv_dilated_cuboid_backward_input_im2col(
+    float *input_grad, const float *kernel, const float *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride, long dpt_in_stride,
+    long row_in_stride, long col_in_stride);
+int owl_float64_ndarray_conv_dilated_cuboid_backward_input_im2col(
+    double *input_grad, const double *kernel, const double *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride, long dpt_in_stride,
+    long row_in_stride, long col_in_stride);
+/* replaces stub_*_ndarray_conv_dilated_cuboid_backward_kernel_im2col_native
+ * (owl_ndarray_conv.ml:2079, owl_ndarray_conv_impl.h:3545-3553). */
+int owl_float32_ndarray_conv_dilated_cuboid_backward_kernel_im2col(
+    const float *input, float *kernel_grad, const float *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride, long dpt_in_stride,
+    long row_in_stride, long col_in_stride);
+int owl_float64_ndarray_conv_dilated_cuboid_backward_kernel_im2col(
+    const double *input, double *kernel_grad, const double *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride, long dpt_in_stride,
+    long row_in_stride, long col_in_stride);
+
+/* ======================================================================
+ * Pooling (owl_ndarray_pool.ml:1042-1115 dispatch; owl_ndarray_pool_impl.h).
+ * Max pooling keeps Owl's tie rule (first maximum in scan order wins, NaN is
+ * never selected); average pooling divides by the in-range element count.
+ * ====================================================================== */
+
+/* replaces stub_*_ndarray_{max,avg}pool_spatial_native
+ * (owl_ndarray_pool.ml:9/:28, owl_ndarray_pool_impl.h:9-15) */
+int owl_float32_ndarray_maxpool_spatial(
+    const float *input, float *output, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride);
+int owl_float64_ndarray_maxpool_spatial(
+    const double *input, double *output, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride);
+int owl_float32_ndarray_avgpool_spatial(
+    const float *input, float *output, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride);
+int owl_float64_ndarray_avgpool_spatial(
+    const double *input, double *output, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride);
+
+/* replaces stub_*_ndarray_{max,avg}pool_spatial_backward_native
+ * (owl_ndarray_pool.ml:47/:66, owl_ndarray_pool_impl.h:102-108).
+ * (input, output_grad, input_grad written); pads are explicit, negatives
+ * clipped to 0.  Average pooling ignores `input` (Owl passes a dummy). */
+int owl_float32_ndarray_maxpool_spatial_backward(
+    const float *input, const float *output_grad, float *input_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long row_stride, long col_stride, long pad_rows, long pad_cols);
+int owl_float64_ndarray_maxpool_spatial_backward(
+    const double *input, const double *output_grad, double *input_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long row_stride, long col_stride, long pad_rows, long pad_cols);
+int owl_float32_ndarray_avgpool_spatial_backward(
+    const float *input, const float *output_grad, float *input_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long row_stride, long col_stride, long pad_rows, long pad_cols);
+int owl_float64_ndarray_avgpool_spatial_backward(
+    const double *input, const double *output_grad, double *input_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long row_stride, long col_stride, long pad_rows, long pad_cols);
+
+/* replaces stub_*_ndarray_maxpool_spatial_arg_native
+ * (owl_ndarray_pool.ml:121 `maxpool_argmax_spatial`,
+ *  owl_ndarray_pool_impl.h:459-465): max value and int64 flat index into the
+ * whole input (batch offset included), -1 for a window with no maximum. */
+int owl_float32_ndarray_maxpool_argmax_spatial(
+    const float *input, float *output, int64_t *argmax, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long row_stride,
+    long col_stride, long pad_rows, long pad_cols);
+int owl_float64_ndarray_maxpool_argmax_spatial(
+    const double *input, double *output, int64_t *argmax, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long row_stride,
+    long col_stride, long pad_rows, long pad_cols);
+
+/* replaces stub_*_ndarray_{max,avg}pool_cuboid_native
+ * (owl_ndarray_pool.ml:140/:161, owl_ndarray_pool_impl.h:212-219) */
+int owl_float32_ndarray_maxpool_cuboid(
+    const float *input, float *output, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long dpt_stride, long row_stride, long col_stride,
+    long padding);
+int owl_float64_ndarray_maxpool_cuboid(
+    const double *input, double *output, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long dpt_stride, long row_stride, long col_stride,
+    long padding);
+int owl_float32_ndarray_avgpool_cuboid(
+    const float *input, float *output, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long dpt_stride, long row_stride, long col_stride,
+    long padding);
+int owl_float64_ndarray_avgpool_cuboid(
+    const double *input, double *output, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long dpt_stride, long row_stride, long col_stride,
+    long padding);
+
+/* replaces stub_*_ndarray_{max,avg}pool_cuboid_backward_native
+ * (owl_ndarray_pool.ml:182, owl_ndarray_pool_impl.h:324-331).  Note the
+ * stride order col, row, dpt -- reversed relative to the forward. */
+int owl_float32_ndarray_maxpool_cuboid_backward(
+    const float *input, const float *output_grad, float *input_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long col_stride,
+    long row_stride, long dpt_stride, long padding);
+int owl_float64_ndarray_maxpool_cuboid_backward(
+    const double *input, const double *output_grad, double *input_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long col_stride,
+    long row_stride, long dpt_stride, long padding);
+int owl_float32_ndarray_avgpool_cuboid_backward(
+    const float *input, const float *output_grad, float *input_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long col_stride,
+    long row_stride, long dpt_stride, long padding);
+int owl_float64_ndarray_avgpool_cuboid_backward(
+    const double *input, const double *output_grad, double *input_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long col_stride,
+    long row_stride, long dpt_stride, long padding);
+
+/* ======================================================================
+ * Device-resident entry points.  For every host drop-in `owl_<kind>_ndarray_
+ * <op>(args...)` above (except the 2-D `_im2col` spellings, which are plain
+ * aliases) there is an `owlgpu_<kind>_ndarray_<op>(args..., int precision,
+ * void *stream)` taking device pointers, asynchronous on `stream`.
+ * ====================================================================== */
+
+#define OWLGPU_DEVICE_ARGS , int precision, void *stream
+
+int owlgpu_float32_ndarray_conv_spatial(
+    const float *input, const float *kernel, float *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_ndarray_conv_spatial(
+    const double *input, const double *kernel, double *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_float32_ndarray_conv_spatial_backward_input(
+    float *input_grad, const float *kernel, const float *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_ndarray_conv_spatial_backward_input(
+    double *input_grad, const double *kernel, const double *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_float32_ndarray_conv_spatial_backward_kernel(
+    const float *input, float *kernel_grad, const float *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_ndarray_conv_spatial_backward_kernel(
+    const double *input, double *kernel_grad, const double *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_float32_ndarray_conv_cuboid_im2col(
+    const float *input, const float *kernel, float *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long padding OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_ndarray_conv_cuboid_im2col(
+    const double *input, const double *kernel, double *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long padding OWLGPU_DEVICE_ARGS);
+int owlgpu_float32_ndarray_conv_cuboid_backward_input_im2col(
+    float *input_grad, const float *kernel, const float *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_ndarray_conv_cuboid_backward_input_im2col(
+    double *input_grad, const double *kernel, const double *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_float32_ndarray_conv_cuboid_backward_kernel_im2col(
+    const float *input, float *kernel_grad, const float *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_ndarray_conv_cuboid_backward_kernel_im2col(
+    const double *input, double *kernel_grad, const double *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_float32_ndarray_conv_dilated_spatial_im2col(
+    const float *input, const float *kernel, float *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_ndarray_conv_dilated_spatial_im2col(
+    const double *input, const double *kernel, double *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_float32_ndarray_conv_dilated_spatial_backward_input_im2col(
+    float *input_grad, const float *kernel, const float *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_ndarray_conv_dilated_spatial_backward_input_im2col(
+    double *input_grad, const double *kernel, const double *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_float32_ndarray_conv_dilated_spatial_backward_kernel_im2col(
+    const float *input, float *kernel_grad, const float *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_ndarray_conv_dilated_spatial_backward_kernel_im2col(
+    const double *input, double *kernel_grad, const double *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_float32_ndarray_conv_dilated_cuboid_im2col(
+    const float *input, const float *kernel, float *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long dpt_in_stride, long row_in_stride,
+    long col_in_stride, long padding OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_ndarray_conv_dilated_cuboid_im2col(
+    const double *input, const double *kernel, double *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long dpt_in_stride, long row_in_stride,
+    long col_in_stride, long padding OWLGPU_DEVICE_ARGS);
+int owlgpu_float32_ndarray_conv_dilated_cuboid_backward_input_im2col(
+    float *input_grad, const float *kernel, const float *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride, long dpt_in_stride,
+    long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_ndarray_conv_dilated_cuboid_backward_input_im2col(
+    double *input_grad, const double *kernel, const double *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride, long dpt_in_stride,
+    long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_float32_ndarray_conv_dilated_cuboid_backward_kernel_im2col(
+    const float *input, float *kernel_grad, const float *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride, long dpt_in_stride,
+    long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_ndarray_conv_dilated_cuboid_backward_kernel_im2col(
+    const double *input, double *kernel_grad, const double *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride, long dpt_in_stride,
+    long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
+
+int owlgpu_float32_ndarray_maxpool_spatial(
+    const float *input, float *output, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_ndarray_maxpool_spatial(
+    const double *input, double *output, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_float32_ndarray_avgpool_spatial(
+    const float *input, float *output, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_ndarray_avgpool_spatial(
+    const double *input, double *output, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_float32_ndarray_maxpool_spatial_backward(
+    const float *input, const float *output_grad, float *input_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long row_stride, long col_stride, long pad_rows,
+    long pad_cols OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_ndarray_maxpool_spatial_backward(
+    const double *input, const double *output_grad, double *input_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long row_stride, long col_stride, long pad_rows,
+    long pad_cols OWLGPU_DEVICE_ARGS);
+int owlgpu_float32_ndarray_avgpool_spatial_backward(
+    const float *input, const float *output_grad, float *input_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long row_stride, long col_stride, long pad_rows,
+    long pad_cols OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_ndarray_avgpool_spatial_backward(
+    const double *input, const double *output_grad, double *input_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long row_stride, long col_stride, long pad_rows,
+    long pad_cols OWLGPU_DEVICE_ARGS);
+int owlgpu_float32_ndarray_maxpool_argmax_spatial(
+    const float *input, float *output, int64_t *argmax, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long row_stride,
+    long col_stride, long pad_rows, long pad_cols OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_ndarray_maxpool_argmax_spatial(
+    const double *input, double *output, int64_t *argmax, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long row_stride,
+    long col_stride, long pad_rows, long pad_cols OWLGPU_DEVICE_ARGS);
+int owlgpu_float32_ndarray_maxpool_cuboid(
+    const float *input, float *output, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long dpt_stride, long row_stride, long col_stride,
+    long padding OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_ndarray_maxpool_cuboid(
+    const double *input, double *output, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long dpt_stride, long row_stride, long col_stride,
+    long padding OWLGPU_DEVICE_ARGS);
+int owlgpu_float32_ndarray_avgpool_cuboid(
+    const float *input, float *output, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long dpt_stride, long row_stride, long col_stride,
+    long padding OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_ndarray_avgpool_cuboid(
+    const double *input, double *output, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long dpt_stride, long row_stride, long col_stride,
+    long padding OWLGPU_DEVICE_ARGS);
+int owlgpu_float32_ndarray_maxpool_cuboid_backward(
+    const float *input, const float *output_grad, float *input_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long col_stride,
+    long row_stride, long dpt_stride, long padding OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_ndarray_maxpool_cuboid_backward(
+    const double *input, const double *output_grad, double *input_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long col_stride,
+    long row_stride, long dpt_stride, long padding OWLGPU_DEVICE_ARGS);
+int owlgpu_float32_ndarray_avgpool_cuboid_backward(
+    const float *input, const float *output_grad, float *input_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long col_stride,
+    long row_stride, long dpt_stride, long padding OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_ndarray_avgpool_cuboid_backward(
+    const double *input, const double *output_grad, double *input_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long col_stride,
+    long row_stride, long dpt_stride, long padding OWLGPU_DEVICE_ARGS);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OWLGPU_H */

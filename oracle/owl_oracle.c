@@ -1,0 +1,341 @@
+/*
+ * owl_oracle.c -- CPU oracle for Owl's dense-ndarray conv / pool path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the CUDA library and the timed
+ * CPU arm of the benchmark.  The shipped library never links or calls it.
+ *
+ * Exported entry points keep the names and the argument order of Owl's C
+ * stubs (src/owl/core/owl_ndarray_conv_stub.c, owl_ndarray_pool_stub.c), with
+ * the OCaml `value` wrappers replaced by plain pointers and longs and the
+ * prefix `oracle_` in place of `stub_`.  The algorithms are restated in
+ * oracle_impl.h; this file holds the argument plumbing and the padding rules:
+ *   forward     : pad = max(0, (stride*(out-1) + k_eff - in) / 2) unless
+ *                 padding == 1 (VALID)  -- owl_ndarray_conv_impl.h:288-294,
+ *                 :1262-1270, :3145-3150;
+ *   backward    : the same expression, always applied (the stubs re-derive
+ *                 the padding from the shapes) -- :502-505, :713-716;
+ *   non-dilated backward stubs ignore row/col_in_stride -- :491-492.
+ *
+ * GEMMs go to a BLAS registered at run time (oracle_set_blas), matching Owl's
+ * use of cblas_?gemm; without one a plain triple loop is used.
+ */
+
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+typedef struct {
+  long B, IC, IR, ID, Ci, KC, KR, KD, OC, OR, OD, Co;
+  long sc, sr, sd;  /* strides (cols, rows, depths) */
+  long dc, dr, dd;  /* dilation rates ("in strides") */
+  long pc, pr, pd;  /* leading padding */
+} geom_t;
+
+typedef struct {
+  long B, IC, IR, ID, Ch, KC, KR, KD, OC, OR, OD;
+  long sc, sr, sd, pc, pr, pd;
+} pgeom_t;
+
+/* ---- BLAS registration ------------------------------------------------- */
+
+typedef void (*sgemm32_t)(int, int, int, int, int, int, float, const float *, int,
+                          const float *, int, float, float *, int);
+typedef void (*dgemm32_t)(int, int, int, int, int, int, double, const double *, int,
+                          const double *, int, double, double *, int);
+typedef void (*sgemm64_t)(int, int, int, int64_t, int64_t, int64_t, float, const float *,
+                          int64_t, const float *, int64_t, float, float *, int64_t);
+typedef void (*dgemm64_t)(int, int, int, int64_t, int64_t, int64_t, double, const double *,
+                          int64_t, const double *, int64_t, double, double *, int64_t);
+
+static void *g_sgemm = 0, *g_dgemm = 0;
+static int g_ilp64 = 0;
+
+/* Register cblas_sgemm / cblas_dgemm (LP64 when ilp64 == 0, else 64-bit
+ * integer interface).  Passing nulls reverts to the built-in loops. */
+void oracle_set_blas(void *sgemm, void *dgemm, int ilp64) {
+  g_sgemm = sgemm;
+  g_dgemm = dgemm;
+  g_ilp64 = ilp64;
+}
+
+int oracle_has_blas(void) { return g_sgemm != 0 && g_dgemm != 0; }
+
+enum { RowMajor = 101, NoTrans = 111, Trans = 112 };
+
+#define LOOP_GEMM(T)                                                              \
+  do {                                                                            \
+    for (long i = 0; i < m; ++i)                                                  \
+      for (long j = 0; j < n; ++j) {                                              \
+        T s = 0;                                                                  \
+        for (long p = 0; p < k; ++p) {                                            \
+          T av = transA ? A[p * lda + i] : A[i * lda + p];                        \
+          T bv = transB ? B[j * ldb + p] : B[p * ldb + j];                        \
+          s += av * bv;                                                           \
+        }                                                                         \
+        C[i * ldc + j] = beta == 0 ? s : beta * C[i * ldc + j] + s;               \
+      }                                                                           \
+  } while (0)
+
+static void gemm_f32(int transA, int transB, long m, long n, long k, const float *A, long lda,
+                     const float *B, long ldb, float beta, float *C, long ldc) {
+  if (g_sgemm) {
+    if (g_ilp64)
+      ((sgemm64_t)g_sgemm)(RowMajor, transA ? Trans : NoTrans, transB ? Trans : NoTrans, m, n, k,
+                           1.0f, A, lda, B, ldb, beta, C, ldc);
+    else
+      ((sgemm32_t)g_sgemm)(RowMajor, transA ? Trans : NoTrans, transB ? Trans : NoTrans, (int)m,
+                           (int)n, (int)k, 1.0f, A, (int)lda, B, (int)ldb, beta, C, (int)ldc);
+    return;
+  }
+  LOOP_GEMM(float);
+}
+
+static void gemm_f64(int transA, int transB, long m, long n, long k, const double *A, long lda,
+                     const double *B, long ldb, double beta, double *C, long ldc) {
+  if (g_dgemm) {
+    if (g_ilp64)
+      ((dgemm64_t)g_dgemm)(RowMajor, transA ? Trans : NoTrans, transB ? Trans : NoTrans, m, n, k,
+                           1.0, A, lda, B, ldb, beta, C, ldc);
+    else
+      ((dgemm32_t)g_dgemm)(RowMajor, transA ? Trans : NoTrans, transB ? Trans : NoTrans, (int)m,
+                           (int)n, (int)k, 1.0, A, (int)lda, B, (int)ldb, beta, C, (int)ldc);
+    return;
+  }
+  LOOP_GEMM(double);
+}
+
+/* ---- instantiate the algorithms for float and double ------------------- */
+
+#define T float
+#define SFX f32
+#include "oracle_impl.h"
+#undef T
+#undef SFX
+
+#define T double
+#define SFX f64
+#include "oracle_impl.h"
+#undef T
+#undef SFX
+
+/* ---- padding rules ----------------------------------------------------- */
+
+static long fwd_pad(long padding, long stride, long out, long keff, long in) {
+  if (padding == 1) return 0;
+  long p = (stride * (out - 1) + keff - in) / 2; /* C division, as the stubs */
+  return p < 0 ? 0 : p;
+}
+
+static long bwd_pad(long stride, long out, long keff, long in) {
+  long p = (stride * (out - 1) + keff - in) / 2;
+  return p < 0 ? 0 : p;
+}
+
+static long keff(long k, long rate) { return k + (k - 1) * (rate - 1); }
+
+static geom_t geom3(long B, long IC, long IR, long ID, long Ci, long KC, long KR, long KD, long OC,
+                    long OR, long OD, long Co, long sc, long sr, long sd, long dc, long dr,
+                    long dd) {
+  geom_t g = {B, IC, IR, ID, Ci, KC, KR, KD, OC, OR, OD, Co, sc, sr, sd, dc, dr, dd, 0, 0, 0};
+  return g;
+}
+
+/* ---- conv entry points (Owl stub argument order) ----------------------- */
+
+#define DEF_CONV_ALL(TY, NAME, SFX2)                                                            \
+  /* owl_ndarray_conv_impl.h:246-253 (spatial fwd), dilation fixed at 1 */                      \
+  int oracle_##NAME##_ndarray_conv_spatial(                                                     \
+      TY *x, TY *w, TY *y, long B, long IC, long IR, long Ci, long KC, long KR, long OC,        \
+      long OR, long Co, long sr, long sc, long padding, long rin, long cin) {                   \
+    (void)rin; (void)cin;                                                                        \
+    geom_t g = geom3(B, IC, IR, 1, Ci, KC, KR, 1, OC, OR, 1, Co, sc, sr, 1, 1, 1, 1);            \
+    g.pc = fwd_pad(padding, sc, OC, KC, IC);                                                     \
+    g.pr = fwd_pad(padding, sr, OR, KR, IR);                                                     \
+    return conv_fwd_##SFX2(&g, x, w, y);                                                         \
+  }                                                                                              \
+  /* owl_ndarray_conv_impl.h:465-472: first argument is dX (written) */                          \
+  int oracle_##NAME##_ndarray_conv_spatial_backward_input(                                      \
+      TY *dx, TY *w, TY *dy, long B, long IC, long IR, long Ci, long KC, long KR, long OC,       \
+      long OR, long Co, long sr, long sc, long rin, long cin) {                                  \
+    (void)rin; (void)cin;                                                                        \
+    geom_t g = geom3(B, IC, IR, 1, Ci, KC, KR, 1, OC, OR, 1, Co, sc, sr, 1, 1, 1, 1);            \
+    g.pc = bwd_pad(sc, OC, KC, IC);                                                              \
+    g.pr = bwd_pad(sr, OR, KR, IR);                                                              \
+    return conv_bwd_input_##SFX2(&g, dx, w, dy);                                                 \
+  }                                                                                              \
+  /* owl_ndarray_conv_impl.h:675-682: second argument is dW (written) */                         \
+  int oracle_##NAME##_ndarray_conv_spatial_backward_kernel(                                     \
+      TY *x, TY *dw, TY *dy, long B, long IC, long IR, long Ci, long KC, long KR, long OC,       \
+      long OR, long Co, long sr, long sc, long rin, long cin) {                                  \
+    (void)rin; (void)cin;                                                                        \
+    geom_t g = geom3(B, IC, IR, 1, Ci, KC, KR, 1, OC, OR, 1, Co, sc, sr, 1, 1, 1, 1);            \
+    g.pc = bwd_pad(sc, OC, KC, IC);                                                              \
+    g.pr = bwd_pad(sr, OR, KR, IR);                                                              \
+    return conv_bwd_kernel_##SFX2(&g, x, dw, dy);                                                \
+  }                                                                                              \
+  /* owl_ndarray_conv_impl.h:3097-3150 */                                                        \
+  int oracle_##NAME##_ndarray_conv_dilated_spatial_im2col(                                      \
+      TY *x, TY *w, TY *y, long B, long IC, long IR, long Ci, long KC, long KR, long OC,        \
+      long OR, long Co, long sr, long sc, long padding, long rin, long cin) {                   \
+    geom_t g = geom3(B, IC, IR, 1, Ci, KC, KR, 1, OC, OR, 1, Co, sc, sr, 1, cin, rin, 1);        \
+    g.pc = fwd_pad(padding, sc, OC, keff(KC, cin), IC);                                          \
+    g.pr = fwd_pad(padding, sr, OR, keff(KR, rin), IR);                                          \
+    return conv_fwd_##SFX2(&g, x, w, y);                                                         \
+  }                                                                                              \
+  /* owl_ndarray_conv_impl.h:3317-3350 */                                                        \
+  int oracle_##NAME##_ndarray_conv_dilated_spatial_backward_input_im2col(                       \
+      TY *dx, TY *w, TY *dy, long B, long IC, long IR, long Ci, long KC, long KR, long OC,       \
+      long OR, long Co, long sr, long sc, long rin, long cin) {                                  \
+    geom_t g = geom3(B, IC, IR, 1, Ci, KC, KR, 1, OC, OR, 1, Co, sc, sr, 1, cin, rin, 1);        \
+    g.pc = bwd_pad(sc, OC, keff(KC, cin), IC);                                                   \
+    g.pr = bwd_pad(sr, OR, keff(KR, rin), IR);                                                   \
+    return conv_bwd_input_##SFX2(&g, dx, w, dy);                                                 \
+  }                                                                                              \
+  /* owl_ndarray_conv_impl.h:3203-3240 */                                                        \
+  int oracle_##NAME##_ndarray_conv_dilated_spatial_backward_kernel_im2col(                      \
+      TY *x, TY *dw, TY *dy, long B, long IC, long IR, long Ci, long KC, long KR, long OC,       \
+      long OR, long Co, long sr, long sc, long rin, long cin) {                                  \
+    geom_t g = geom3(B, IC, IR, 1, Ci, KC, KR, 1, OC, OR, 1, Co, sc, sr, 1, cin, rin, 1);        \
+    g.pc = bwd_pad(sc, OC, keff(KC, cin), IC);                                                   \
+    g.pr = bwd_pad(sr, OR, keff(KR, rin), IR);                                                   \
+    return conv_bwd_kernel_##SFX2(&g, x, dw, dy);                                                \
+  }                                                                                              \
+  /* owl_ndarray_conv_impl.h:1211-1219 */                                                        \
+  int oracle_##NAME##_ndarray_conv_cuboid_im2col(                                               \
+      TY *x, TY *w, TY *y, long B, long IC, long IR, long ID, long Ci, long KC, long KR,        \
+      long KD, long OC, long OR, long OD, long Co, long sd, long sr, long sc, long padding) {    \
+    geom_t g = geom3(B, IC, IR, ID, Ci, KC, KR, KD, OC, OR, OD, Co, sc, sr, sd, 1, 1, 1);        \
+    g.pc = fwd_pad(padding, sc, OC, KC, IC);                                                     \
+    g.pr = fwd_pad(padding, sr, OR, KR, IR);                                                     \
+    g.pd = fwd_pad(padding, sd, OD, KD, ID);                                                     \
+    return conv_fwd_##SFX2(&g, x, w, y);                                                         \
+  }                                                                                              \
+  /* owl_ndarray_conv_impl.h:1456-1463 */                                                        \
+  int oracle_##NAME##_ndarray_conv_cuboid_backward_input_im2col(                                \
+      TY *dx, TY *w, TY *dy, long B, long IC, long IR, long ID, long Ci, long KC, long KR,       \
+      long KD, long OC, long OR, long OD, long Co, long sd, long sr, long sc) {                  \
+    geom_t g = geom3(B, IC, IR, ID, Ci, KC, KR, KD, OC, OR, OD, Co, sc, sr, sd, 1, 1, 1);        \
+    g.pc = bwd_pad(sc, OC, KC, IC);                                                              \
+    g.pr = bwd_pad(sr, OR, KR, IR);                                                              \
+    g.pd = bwd_pad(sd, OD, KD, ID);                                                              \
+    return conv_bwd_input_##SFX2(&g, dx, w, dy);                                                 \
+  }                                                                                              \
+  /* owl_ndarray_conv_impl.h:1331-1338 */                                                        \
+  int oracle_##NAME##_ndarray_conv_cuboid_backward_kernel_im2col(                               \
+      TY *x, TY *dw, TY *dy, long B, long IC, long IR, long ID, long Ci, long KC, long KR,       \
+      long KD, long OC, long OR, long OD, long Co, long sd, long sr, long sc) {                  \
+    geom_t g = geom3(B, IC, IR, ID, Ci, KC, KR, KD, OC, OR, OD, Co, sc, sr, sd, 1, 1, 1);        \
+    g.pc = bwd_pad(sc, OC, KC, IC);                                                              \
+    g.pr = bwd_pad(sr, OR, KR, IR);                                                              \
+    g.pd = bwd_pad(sd, OD, KD, ID);                                                              \
+    return conv_bwd_kernel_##SFX2(&g, x, dw, dy);                                                \
+  }                                                                                              \
+  /* owl_ndarray_conv_impl.h:3417-3426 */                                                        \
+  int oracle_##NAME##_ndarray_conv_dilated_cuboid_im2col(                                       \
+      TY *x, TY *w, TY *y, long B, long IC, long IR, long ID, long Ci, long KC, long KR,        \
+      long KD, long OC, long OR, long OD, long Co, long sd, long sr, long sc, long din,         \
+      long rin, long cin, long padding) {                                                        \
+    geom_t g = geom3(B, IC, IR, ID, Ci, KC, KR, KD, OC, OR, OD, Co, sc, sr, sd, cin, rin, din);  \
+    g.pc = fwd_pad(padding, sc, OC, keff(KC, cin), IC);                                          \
+    g.pr = fwd_pad(padding, sr, OR, keff(KR, rin), IR);                                          \
+    g.pd = fwd_pad(padding, sd, OD, keff(KD, din), ID);                                          \
+    return conv_fwd_##SFX2(&g, x, w, y);                                                         \
+  }                                                                                              \
+  /* owl_ndarray_conv_impl.h:3678-3686 */                                                        \
+  int oracle_##NAME##_ndarray_conv_dilated_cuboid_backward_input_im2col(                        \
+      TY *dx, TY *w, TY *dy, long B, long IC, long IR, long ID, long Ci, long KC, long KR,       \
+      long KD, long OC, long OR, long OD, long Co, long sd, long sr, long sc, long din,          \
+      long rin, long cin) {                                                                      \
+    geom_t g = geom3(B, IC, IR, ID, Ci, KC, KR, KD, OC, OR, OD, Co, sc, sr, sd, cin, rin, din);  \
+    g.pc = bwd_pad(sc, OC, keff(KC, cin), IC);                                                   \
+    g.pr = bwd_pad(sr, OR, keff(KR, rin), IR);                                                   \
+    g.pd = bwd_pad(sd, OD, keff(KD, din), ID);                                                   \
+    return conv_bwd_input_##SFX2(&g, dx, w, dy);                                                 \
+  }                                                                                              \
+  /* owl_ndarray_conv_impl.h:3545-3553 */                                                        \
+  int oracle_##NAME##_ndarray_conv_dilated_cuboid_backward_kernel_im2col(                       \
+      TY *x, TY *dw, TY *dy, long B, long IC, long IR, long ID, long Ci, long KC, long KR,       \
+      long KD, long OC, long OR, long OD, long Co, long sd, long sr, long sc, long din,          \
+      long rin, long cin) {                                                                      \
+    geom_t g = geom3(B, IC, IR, ID, Ci, KC, KR, KD, OC, OR, OD, Co, sc, sr, sd, cin, rin, din);  \
+    g.pc = bwd_pad(sc, OC, keff(KC, cin), IC);                                                   \
+    g.pr = bwd_pad(sr, OR, keff(KR, rin), IR);                                                   \
+    g.pd = bwd_pad(sd, OD, keff(KD, din), ID);                                                   \
+    return conv_bwd_kernel_##SFX2(&g, x, dw, dy);                                                \
+  }
+
+DEF_CONV_ALL(float, float32, f32)
+DEF_CONV_ALL(double, float64, f64)
+
+/* ---- pool entry points (Owl stub argument order) ----------------------- */
+
+static pgeom_t pgeom(long B, long IC, long IR, long ID, long Ch, long KC, long KR, long KD,
+                     long OC, long OR, long OD, long sc, long sr, long sd) {
+  pgeom_t g = {B, IC, IR, ID, Ch, KC, KR, KD, OC, OR, OD, sc, sr, sd, 0, 0, 0};
+  return g;
+}
+
+#define DEF_POOL_ALL(TY, NAME, SFX2, KIND, MODE)                                                 \
+  /* owl_ndarray_pool_impl.h:9-15 (fwd), padding flag as :43-49 */                              \
+  int oracle_##NAME##_ndarray_##KIND##_spatial(                                                 \
+      TY *x, TY *y, long B, long IC, long IR, long Ch, long KC, long KR, long OC, long OR,      \
+      long sr, long sc, long padding, long rin, long cin) {                                      \
+    (void)rin; (void)cin;                                                                        \
+    pgeom_t g = pgeom(B, IC, IR, 1, Ch, KC, KR, 1, OC, OR, 1, sc, sr, 1);                        \
+    g.pr = fwd_pad(padding, sr, OR, KR, IR);                                                     \
+    g.pc = fwd_pad(padding, sc, OC, KC, IC);                                                     \
+    pool_fwd_##SFX2(&g, x, y, 0, MODE);                                                          \
+    return 0;                                                                                    \
+  }                                                                                              \
+  /* owl_ndarray_pool_impl.h:102-108: explicit pads, negatives clipped (:136-137) */            \
+  int oracle_##NAME##_ndarray_##KIND##_spatial_backward(                                        \
+      TY *x, TY *dy, TY *dx, long B, long IC, long IR, long Ch, long KC, long KR, long OC,      \
+      long OR, long sr, long sc, long pad_rows, long pad_cols) {                                 \
+    pgeom_t g = pgeom(B, IC, IR, 1, Ch, KC, KR, 1, OC, OR, 1, sc, sr, 1);                        \
+    g.pr = pad_rows < 0 ? 0 : pad_rows;                                                          \
+    g.pc = pad_cols < 0 ? 0 : pad_cols;                                                          \
+    pool_bwd_##SFX2(&g, x, dy, dx, MODE);                                                        \
+    return 0;                                                                                    \
+  }                                                                                              \
+  /* owl_ndarray_pool_impl.h:212-219 */                                                          \
+  int oracle_##NAME##_ndarray_##KIND##_cuboid(                                                  \
+      TY *x, TY *y, long B, long IC, long IR, long ID, long Ch, long KC, long KR, long KD,      \
+      long OC, long OR, long OD, long sd, long sr, long sc, long padding) {                      \
+    pgeom_t g = pgeom(B, IC, IR, ID, Ch, KC, KR, KD, OC, OR, OD, sc, sr, sd);                    \
+    g.pc = fwd_pad(padding, sc, OC, KC, IC);                                                     \
+    g.pr = fwd_pad(padding, sr, OR, KR, IR);                                                     \
+    g.pd = fwd_pad(padding, sd, OD, KD, ID);                                                     \
+    pool_fwd_##SFX2(&g, x, y, 0, MODE);                                                          \
+    return 0;                                                                                    \
+  }                                                                                              \
+  /* owl_ndarray_pool_impl.h:324-331: strides arrive col, row, dpt */                           \
+  int oracle_##NAME##_ndarray_##KIND##_cuboid_backward(                                         \
+      TY *x, TY *dy, TY *dx, long B, long IC, long IR, long ID, long Ch, long KC, long KR,      \
+      long KD, long OC, long OR, long OD, long sc, long sr, long sd, long padding) {             \
+    pgeom_t g = pgeom(B, IC, IR, ID, Ch, KC, KR, KD, OC, OR, OD, sc, sr, sd);                    \
+    g.pc = fwd_pad(padding, sc, OC, KC, IC);                                                     \
+    g.pr = fwd_pad(padding, sr, OR, KR, IR);                                                     \
+    g.pd = fwd_pad(padding, sd, OD, KD, ID);                                                     \
+    pool_bwd_##SFX2(&g, x, dy, dx, MODE);                                                        \
+    return 0;                                                                                    \
+  }
+
+DEF_POOL_ALL(float, float32, f32, maxpool, 0)
+DEF_POOL_ALL(float, float32, f32, avgpool, 1)
+DEF_POOL_ALL(double, float64, f64, maxpool, 0)
+DEF_POOL_ALL(double, float64, f64, avgpool, 1)
+
+/* owl_ndarray_pool_impl.h:459-465: max value plus int64 flat argmax */
+#define DEF_ARG(TY, NAME, SFX2)                                                                 \
+  int oracle_##NAME##_ndarray_maxpool_spatial_arg(                                              \
+      TY *x, TY *y, int64_t *arg, long B, long IC, long IR, long Ch, long KC, long KR,          \
+      long OC, long OR, long sr, long sc, long pad_rows, long pad_cols) {                        \
+    pgeom_t g = pgeom(B, IC, IR, 1, Ch, KC, KR, 1, OC, OR, 1, sc, sr, 1);                        \
+    g.pr = pad_rows < 0 ? 0 : pad_rows;                                                          \
+    g.pc = pad_cols < 0 ? 0 : pad_cols;                                                          \
+    pool_fwd_##SFX2(&g, x, y, arg, 0);                                                           \
+    return 0;                                                                                    \
+  }
+DEF_ARG(float, float32, f32)
+DEF_ARG(double, float64, f64)

@@ -1,0 +1,712 @@
+// api.cu -- the C ABI of libowlgpu (declared in include/owlgpu.h).
+//
+// Two families per Owl stub:
+//   owl_<kind>_ndarray_<op>(host pointers, Owl stub arguments)
+//       synchronous drop-in for the C stub of the same OCaml external name;
+//       stages inputs to the GPU, runs, copies outputs back.
+//   owlgpu_<kind>_ndarray_<op>(device pointers, Owl stub arguments,
+//                              precision, stream)
+//       asynchronous, device resident.
+// Both turn the stub arguments into a ConvGeom / PoolGeom with the padding
+// rules of the Owl stubs and call the compute layer.
+#include <cuda_runtime.h>
+
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/owlgpu.h"
+#include "common.cuh"
+
+namespace owlgpu {
+
+std::atomic<uint64_t> g_launches{0};
+
+static thread_local std::string t_error;
+
+void set_error(const std::string &msg) { t_error = msg; }
+const char *get_error() { return t_error.c_str(); }
+
+int cuda_fail(cudaError_t e, const char *where) {
+  set_error(std::string(where) + ": " + cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? kErrNoMem : kErrCuda;
+}
+
+int scratch_alloc(void **p, size_t bytes, cudaStream_t s) {
+  *p = nullptr;
+  if (bytes == 0) return kOk;
+  cudaError_t e = cudaMallocAsync(p, bytes, s);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return cuda_fail(e, "cudaMallocAsync(scratch)");
+  }
+  return kOk;
+}
+
+void scratch_free(void *p, cudaStream_t s) {
+  if (p) cudaFreeAsync(p, s);
+}
+
+// ---- dispatch between SIMT and tensor-core kernels -----------------------
+
+static bool tc_requested(Dtype dt, int prec) { return dt == F32 && prec != OWLGPU_PREC_FP32; }
+
+int conv_fwd(Dtype dt, int prec, const ConvGeom &g, const void *x, const void *w, void *y,
+             cudaStream_t s) {
+  if (tc_requested(dt, prec)) {
+    int rc = tc_conv_fwd(prec, g, (const float *)x, (const float *)w, (float *)y, s);
+    if (rc != kErrUnsupported) return rc;
+  }
+  return simt_conv_fwd(dt, g, x, w, y, s);
+}
+
+int conv_bwd_input(Dtype dt, int prec, const ConvGeom &g, void *dx, const void *w,
+                   const void *dy, cudaStream_t s) {
+  if (tc_requested(dt, prec)) {
+    int rc = tc_conv_bwd_input(prec, g, (float *)dx, (const float *)w, (const float *)dy, s);
+    if (rc != kErrUnsupported) return rc;
+  }
+  return simt_conv_bwd_input(dt, g, dx, w, dy, s);
+}
+
+int conv_bwd_kernel(Dtype dt, int prec, const ConvGeom &g, const void *x, void *dw,
+                    const void *dy, cudaStream_t s) {
+  if (tc_requested(dt, prec)) {
+    int rc = tc_conv_bwd_kernel(prec, g, (const float *)x, (float *)dw, (const float *)dy, s);
+    if (rc != kErrUnsupported) return rc;
+  }
+  return simt_conv_bwd_kernel(dt, g, x, dw, dy, s);
+}
+
+// ---- argument checking and geometry construction -------------------------
+
+static bool bad_dims(std::initializer_list<long> dims) {
+  for (long d : dims)
+    if (d < 0 || d > (1L << 30)) return true;
+  return false;
+}
+static bool bad_pos(std::initializer_list<long> v) {
+  for (long d : v)
+    if (d < 1 || d > (1L << 20)) return true;
+  return false;
+}
+
+static long keff(long k, long rate) { return k + (k - 1) * (rate - 1); }
+static int fwd_pad(long padding, long stride, long out, long ke, long in) {
+  if (padding == 1) return 0;
+  long p = (stride * (out - 1) + ke - in) / 2;
+  return (int)(p < 0 ? 0 : p);
+}
+static int bwd_pad(long stride, long out, long ke, long in) {
+  long p = (stride * (out - 1) + ke - in) / 2;
+  return (int)(p < 0 ? 0 : p);
+}
+
+static int invalid(const char *fn, const char *what) {
+  set_error(std::string(fn) + ": " + what);
+  return kErrInvalid;
+}
+
+// Build a ConvGeom.  `bwd` selects the backward padding rule; `rates` are
+// (cols, rows, dpts) dilation rates, all 1 for the non-dilated stubs.
+static int make_conv(const char *fn, ConvGeom &g, long B, long IC, long IR, long ID, long Ci,
+                     long KC, long KR, long KD, long OC, long OR, long OD, long Co, long sc,
+                     long sr, long sd, long dc, long dr, long dd, bool bwd, long padding) {
+  if (bad_dims({B, IC, IR, ID, Ci, KC, KR, KD, OC, OR, OD, Co}))
+    return invalid(fn, "negative or oversized dimension");
+  if (bad_pos({sc, sr, sd})) return invalid(fn, "stride must be >= 1");
+  if (bad_pos({dc, dr, dd})) return invalid(fn, "dilation rate must be >= 1");
+  if (!bwd && padding != 0 && padding != 1) return invalid(fn, "padding must be 0 (SAME) or 1 (VALID)");
+  g.B = B; g.IC = IC; g.IR = IR; g.ID = ID; g.Ci = Ci;
+  g.KC = KC; g.KR = KR; g.KD = KD;
+  g.OC = OC; g.OR = OR; g.OD = OD; g.Co = Co;
+  g.sc = (int)sc; g.sr = (int)sr; g.sd = (int)sd;
+  g.dc = (int)dc; g.dr = (int)dr; g.dd = (int)dd;
+  if (bwd) {
+    g.pc = bwd_pad(sc, OC, keff(KC, dc), IC);
+    g.pr = bwd_pad(sr, OR, keff(KR, dr), IR);
+    g.pd = bwd_pad(sd, OD, keff(KD, dd), ID);
+  } else {
+    g.pc = fwd_pad(padding, sc, OC, keff(KC, dc), IC);
+    g.pr = fwd_pad(padding, sr, OR, keff(KR, dr), IR);
+    g.pd = fwd_pad(padding, sd, OD, keff(KD, dd), ID);
+  }
+  return kOk;
+}
+
+static int make_pool(const char *fn, PoolGeom &g, long B, long IC, long IR, long ID, long Ch,
+                     long KC, long KR, long KD, long OC, long OR, long OD, long sc, long sr,
+                     long sd) {
+  if (bad_dims({B, IC, IR, ID, Ch, KC, KR, KD, OC, OR, OD}))
+    return invalid(fn, "negative or oversized dimension");
+  if (bad_pos({sc, sr, sd})) return invalid(fn, "stride must be >= 1");
+  g.B = B; g.IC = IC; g.IR = IR; g.ID = ID; g.Ch = Ch;
+  g.KC = KC; g.KR = KR; g.KD = KD;
+  g.OC = OC; g.OR = OR; g.OD = OD;
+  g.sc = (int)sc; g.sr = (int)sr; g.sd = (int)sd;
+  g.pc = g.pr = g.pd = 0;
+  return kOk;
+}
+
+// ---- host drop-in staging --------------------------------------------------
+
+static std::atomic<int> g_precision{-1};
+static std::atomic<int> g_device{0};
+
+static int default_precision() {
+  int p = g_precision.load();
+  if (p >= 0) return p;
+  const char *e = getenv("OWLGPU_PRECISION");
+  p = OWLGPU_PREC_FP32;
+  if (e) {
+    if (!strcmp(e, "tf32")) p = OWLGPU_PREC_TF32;
+    else if (!strcmp(e, "bf16")) p = OWLGPU_PREC_BF16;
+    else if (!strcmp(e, "bf16x3")) p = OWLGPU_PREC_BF16X3;
+  }
+  int expected = -1;
+  g_precision.compare_exchange_strong(expected, p);
+  return g_precision.load();
+}
+
+struct HostStream {
+  cudaStream_t s = nullptr;
+  int device = -1;
+  ~HostStream() {}
+};
+static thread_local HostStream t_stream;
+
+static int host_stream(cudaStream_t *out) {
+  int dev = g_device.load();
+  if (t_stream.s == nullptr || t_stream.device != dev) {
+    OWL_CUDA(cudaSetDevice(dev));
+    // Keep freed staging memory cached in the device's default pool so that
+    // repeated drop-in calls do not return it to the driver at every sync.
+    cudaMemPool_t pool;
+    OWL_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+    uint64_t keep = UINT64_MAX;
+    OWL_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    cudaStream_t s;
+    OWL_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    t_stream.s = s;
+    t_stream.device = dev;
+  } else {
+    OWL_CUDA(cudaSetDevice(dev));
+  }
+  *out = t_stream.s;
+  return kOk;
+}
+
+struct Buf {
+  const void *host;  // source (inputs) or destination (outputs)
+  size_t bytes;
+  bool in, out;
+  void *dev = nullptr;
+};
+
+// Stage `bufs` to the device, run `body(dev pointers, stream)`, copy the
+// outputs back and wait.  Device memory comes from the stream-ordered pool,
+// so repeated calls of the same size reuse it.
+template <typename F>
+static int host_call(std::vector<Buf> bufs, F body) {
+  cudaStream_t s;
+  int rc = host_stream(&s);
+  if (rc) return rc;
+  for (auto &b : bufs) {
+    if (b.bytes == 0) continue;
+    rc = scratch_alloc(&b.dev, b.bytes, s);
+    if (rc) break;
+    if (b.in) {
+      cudaError_t e = cudaMemcpyAsync(b.dev, b.host, b.bytes, cudaMemcpyHostToDevice, s);
+      if (e != cudaSuccess) { rc = cuda_fail(e, "cudaMemcpyAsync(H2D)"); break; }
+    }
+  }
+  if (rc == kOk) {
+    std::vector<void *> ptrs;
+    for (auto &b : bufs) ptrs.push_back(b.dev);
+    rc = body(ptrs, s);
+  }
+  if (rc == kOk) {
+    for (auto &b : bufs) {
+      if (!b.out || b.bytes == 0) continue;
+      cudaError_t e = cudaMemcpyAsync(const_cast<void *>(b.host), b.dev, b.bytes,
+                                      cudaMemcpyDeviceToHost, s);
+      if (e != cudaSuccess) { rc = cuda_fail(e, "cudaMemcpyAsync(D2H)"); break; }
+    }
+  }
+  for (auto &b : bufs) scratch_free(b.dev, s);
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (rc == kOk && e != cudaSuccess) rc = cuda_fail(e, "cudaStreamSynchronize");
+  return rc;
+}
+
+template <typename T>
+static Dtype dtype_of() { return sizeof(T) == 4 ? F32 : F64; }
+
+// Conv op kinds.
+enum ConvOp { OP_FWD, OP_BWDI, OP_BWDK };
+
+template <typename T>
+static int conv_device(ConvOp op, const ConvGeom &g, void *a, void *b, void *c, int prec,
+                       cudaStream_t s) {
+  Dtype dt = dtype_of<T>();
+  if (op == OP_FWD) return conv_fwd(dt, prec, g, a, b, c, s);
+  if (op == OP_BWDI) return conv_bwd_input(dt, prec, g, a, b, c, s);
+  return conv_bwd_kernel(dt, prec, g, a, b, c, s);
+}
+
+// Host drop-in for a conv stub: argument roles follow the Owl stubs.
+//   FWD : (X in, W in, Y out)
+//   BWDI: (dX out, W in, dY in)
+//   BWDK: (X in, dW out, dY in)
+template <typename T>
+static int conv_host(ConvOp op, const ConvGeom &g, const void *a, const void *b, const void *c) {
+  size_t xb = sizeof(T) * g.x_elems(), wb = sizeof(T) * g.w_elems(), yb = sizeof(T) * g.y_elems();
+  std::vector<Buf> bufs;
+  if (op == OP_FWD) bufs = {{a, xb, true, false}, {b, wb, true, false}, {c, yb, false, true}};
+  else if (op == OP_BWDI) bufs = {{a, xb, false, true}, {b, wb, true, false}, {c, yb, true, false}};
+  else bufs = {{a, xb, true, false}, {b, wb, false, true}, {c, yb, true, false}};
+  int prec = default_precision();
+  return host_call(bufs, [&](std::vector<void *> &p, cudaStream_t s) {
+    return conv_device<T>(op, g, p[0], p[1], p[2], prec, s);
+  });
+}
+
+template <typename T>
+static int pool_fwd_host(PoolMode mode, const PoolGeom &g, const void *x, void *y,
+                         int64_t *arg) {
+  std::vector<Buf> bufs = {{x, sizeof(T) * g.x_elems(), true, false},
+                           {y, sizeof(T) * g.y_elems(), false, true}};
+  if (arg) bufs.push_back({arg, sizeof(int64_t) * g.y_elems(), false, true});
+  return host_call(bufs, [&](std::vector<void *> &p, cudaStream_t s) {
+    return pool_fwd(dtype_of<T>(), mode, g, p[0], p[1], arg ? (int64_t *)p[2] : nullptr, s);
+  });
+}
+
+template <typename T>
+static int pool_bwd_host(PoolMode mode, const PoolGeom &g, const void *x, const void *dy,
+                         void *dx) {
+  // Average pooling never reads X (Owl passes a dummy there).
+  std::vector<Buf> bufs = {{x, mode == POOL_MAX ? sizeof(T) * g.x_elems() : 0, true, false},
+                           {dy, sizeof(T) * g.y_elems(), true, false},
+                           {dx, sizeof(T) * g.x_elems(), false, true}};
+  return host_call(bufs, [&](std::vector<void *> &p, cudaStream_t s) {
+    return pool_bwd(dtype_of<T>(), mode, g, p[0], p[1], p[2], s);
+  });
+}
+
+}  // namespace owlgpu
+
+using namespace owlgpu;
+
+// ===========================================================================
+// Exported C ABI
+// ===========================================================================
+
+extern "C" {
+
+const char *owlgpu_last_error(void) { return get_error(); }
+const char *owlgpu_version(void) { return "owlgpu 0.1 (sm_103a)"; }
+
+int owlgpu_set_precision(int p) {
+  if (p < OWLGPU_PREC_FP32 || p > OWLGPU_PREC_BF16X3) {
+    set_error("owlgpu_set_precision: unknown precision");
+    return kErrInvalid;
+  }
+  int prev = default_precision();
+  g_precision.store(p);
+  return prev;
+}
+int owlgpu_get_precision(void) { return default_precision(); }
+uint64_t owlgpu_launch_count(void) { return g_launches.load(); }
+int owlgpu_set_device(int d) {
+  int n = 0;
+  OWL_CUDA(cudaGetDeviceCount(&n));
+  if (d < 0 || d >= n) { set_error("owlgpu_set_device: no such device"); return kErrInvalid; }
+  g_device.store(d);
+  return kOk;
+}
+int owlgpu_trim(void) {
+  int dev = g_device.load();
+  cudaMemPool_t pool;
+  OWL_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+  OWL_CUDA(cudaDeviceSynchronize());
+  OWL_CUDA(cudaMemPoolTrimTo(pool, 0));
+  return kOk;
+}
+
+// ---- 2-D conv (GEBP spatial family and its im2col / dilated spellings) ----
+
+#define CONV2D_FWD(KIND, T, NAME, DIL)                                                        \
+  int owl_##KIND##_ndarray_##NAME(const T *input, const T *kernel, T *output, long batches,  \
+                                  long input_cols, long input_rows, long in_channel,          \
+                                  long kernel_cols, long kernel_rows, long output_cols,       \
+                                  long output_rows, long out_channel, long row_stride,        \
+                                  long col_stride, long padding, long row_in_stride,          \
+                                  long col_in_stride) {                                       \
+    ConvGeom g;                                                                               \
+    int rc = make_conv(#NAME, g, batches, input_cols, input_rows, 1, in_channel, kernel_cols, \
+                       kernel_rows, 1, output_cols, output_rows, 1, out_channel, col_stride,  \
+                       row_stride, 1, DIL ? col_in_stride : 1, DIL ? row_in_stride : 1, 1,    \
+                       false, padding);                                                       \
+    if (rc) return rc;                                                                        \
+    return conv_host<T>(OP_FWD, g, input, kernel, output);                                    \
+  }                                                                                           \
+  int owlgpu_##KIND##_ndarray_##NAME(const T *input, const T *kernel, T *output,            \
+                                     long batches, long input_cols, long input_rows,          \
+                                     long in_channel, long kernel_cols, long kernel_rows,     \
+                                     long output_cols, long output_rows, long out_channel,    \
+                                     long row_stride, long col_stride, long padding,          \
+                                     long row_in_stride, long col_in_stride, int precision,   \
+                                     void *stream) {                                          \
+    ConvGeom g;                                                                               \
+    int rc = make_conv(#NAME, g, batches, input_cols, input_rows, 1, in_channel, kernel_cols, \
+                       kernel_rows, 1, output_cols, output_rows, 1, out_channel, col_stride,  \
+                       row_stride, 1, DIL ? col_in_stride : 1, DIL ? row_in_stride : 1, 1,    \
+                       false, padding);                                                       \
+    if (rc) return rc;                                                                        \
+    return conv_device<T>(OP_FWD, g, (void *)input, (void *)kernel, output, precision,        \
+                          (cudaStream_t)stream);                                              \
+  }
+
+#define CONV2D_BWD(KIND, T, NAME, OP, DIL, A_T, B_T, C_T, A_N, B_N, C_N)                       \
+  int owl_##KIND##_ndarray_##NAME(A_T A_N, B_T B_N, C_T C_N, long batches, long input_cols,   \
+                                  long input_rows, long in_channel, long kernel_cols,         \
+                                  long kernel_rows, long output_cols, long output_rows,       \
+                                  long out_channel, long row_stride, long col_stride,         \
+                                  long row_in_stride, long col_in_stride) {                   \
+    ConvGeom g;                                                                               \
+    int rc = make_conv(#NAME, g, batches, input_cols, input_rows, 1, in_channel, kernel_cols, \
+                       kernel_rows, 1, output_cols, output_rows, 1, out_channel, col_stride,  \
+                       row_stride, 1, DIL ? col_in_stride : 1, DIL ? row_in_stride : 1, 1,    \
+                       true, 0);                                                              \
+    if (rc) return rc;                                                                        \
+    return conv_host<T>(OP, g, A_N, B_N, C_N);                                                \
+  }                                                                                           \
+  int owlgpu_##KIND##_ndarray_##NAME(A_T A_N, B_T B_N, C_T C_N, long batches,               \
+                                     long input_cols, long input_rows, long in_channel,       \
+                                     long kernel_cols, long kernel_rows, long output_cols,    \
+                                     long output_rows, long out_channel, long row_stride,     \
+                                     long col_stride, long row_in_stride, long col_in_stride, \
+                                     int precision, void *stream) {                           \
+    ConvGeom g;                                                                               \
+    int rc = make_conv(#NAME, g, batches, input_cols, input_rows, 1, in_channel, kernel_cols, \
+                       kernel_rows, 1, output_cols, output_rows, 1, out_channel, col_stride,  \
+                       row_stride, 1, DIL ? col_in_stride : 1, DIL ? row_in_stride : 1, 1,    \
+                       true, 0);                                                              \
+    if (rc) return rc;                                                                        \
+    return conv_device<T>(OP, g, (void *)A_N, (void *)B_N, (void *)C_N, precision,            \
+                          (cudaStream_t)stream);                                              \
+  }
+
+#define CONV2D_ALL(KIND, T)                                                                    \
+  CONV2D_FWD(KIND, T, conv_spatial, 0)                                                        \
+  CONV2D_FWD(KIND, T, conv_spatial_im2col, 0)                                                 \
+  CONV2D_FWD(KIND, T, conv_dilated_spatial_im2col, 1)                                         \
+  CONV2D_BWD(KIND, T, conv_spatial_backward_input, OP_BWDI, 0, T *, const T *, const T *,     \
+             input_grad, kernel, output_grad)                                                 \
+  CONV2D_BWD(KIND, T, conv_spatial_backward_input_im2col, OP_BWDI, 0, T *, const T *,         \
+             const T *, input_grad, kernel, output_grad)                                      \
+  CONV2D_BWD(KIND, T, conv_dilated_spatial_backward_input_im2col, OP_BWDI, 1, T *, const T *, \
+             const T *, input_grad, kernel, output_grad)                                      \
+  CONV2D_BWD(KIND, T, conv_spatial_backward_kernel, OP_BWDK, 0, const T *, T *, const T *,    \
+             input, kernel_grad, output_grad)                                                 \
+  CONV2D_BWD(KIND, T, conv_spatial_backward_kernel_im2col, OP_BWDK, 0, const T *, T *,        \
+             const T *, input, kernel_grad, output_grad)                                      \
+  CONV2D_BWD(KIND, T, conv_dilated_spatial_backward_kernel_im2col, OP_BWDK, 1, const T *,     \
+             T *, const T *, input, kernel_grad, output_grad)
+
+CONV2D_ALL(float32, float)
+CONV2D_ALL(float64, double)
+
+// ---- 3-D conv (cuboid im2col family and dilated cuboid) ---------------------
+
+#define CONV3D_FWD(KIND, T)                                                                    \
+  int owl_##KIND##_ndarray_conv_cuboid_im2col(                                                \
+      const T *input, const T *kernel, T *output, long batches, long input_cols,              \
+      long input_rows, long input_dpts, long in_channel, long kernel_cols, long kernel_rows,   \
+      long kernel_dpts, long output_cols, long output_rows, long output_dpts,                  \
+      long out_channel, long dpt_stride, long row_stride, long col_stride, long padding) {     \
+    ConvGeom g;                                                                               \
+    int rc = make_conv("conv_cuboid_im2col", g, batches, input_cols, input_rows, input_dpts,  \
+                       in_channel, kernel_cols, kernel_rows, kernel_dpts, output_cols,        \
+                       output_rows, output_dpts, out_channel, col_stride, row_stride,         \
+                       dpt_stride, 1, 1, 1, false, padding);                                  \
+    if (rc) return rc;                                                                        \
+    return conv_host<T>(OP_FWD, g, input, kernel, output);                                    \
+  }                                                                                           \
+  int owlgpu_##KIND##_ndarray_conv_cuboid_im2col(                                             \
+      const T *input, const T *kernel, T *output, long batches, long input_cols,              \
+      long input_rows, long input_dpts, long in_channel, long kernel_cols, long kernel_rows,   \
+      long kernel_dpts, long output_cols, long output_rows, long output_dpts,                  \
+      long out_channel, long dpt_stride, long row_stride, long col_stride, long padding,       \
+      int precision, void *stream) {                                                          \
+    ConvGeom g;                                                                               \
+    int rc = make_conv("conv_cuboid_im2col", g, batches, input_cols, input_rows, input_dpts,  \
+                       in_channel, kernel_cols, kernel_rows, kernel_dpts, output_cols,        \
+                       output_rows, output_dpts, out_channel, col_stride, row_stride,         \
+                       dpt_stride, 1, 1, 1, false, padding);                                  \
+    if (rc) return rc;                                                                        \
+    return conv_device<T>(OP_FWD, g, (void *)input, (void *)kernel, output, precision,        \
+                          (cudaStream_t)stream);                                              \
+  }                                                                                           \
+  int owl_##KIND##_ndarray_conv_dilated_cuboid_im2col(                                        \
+      const T *input, const T *kernel, T *output, long batches, long input_cols,              \
+      long input_rows, long input_dpts, long in_channel, long kernel_cols, long kernel_rows,   \
+      long kernel_dpts, long output_cols, long output_rows, long output_dpts,                  \
+      long out_channel, long dpt_stride, long row_stride, long col_stride,                     \
+      long dpt_in_stride, long row_in_stride, long col_in_stride, long padding) {              \
+    ConvGeom g;                                                                               \
+    int rc = make_conv("conv_dilated_cuboid_im2col", g, batches, input_cols, input_rows,      \
+                       input_dpts, in_channel, kernel_cols, kernel_rows, kernel_dpts,         \
+                       output_cols, output_rows, output_dpts, out_channel, col_stride,        \
+                       row_stride, dpt_stride, col_in_stride, row_in_stride, dpt_in_stride,   \
+                       false, padding);                                                       \
+    if (rc) return rc;                                                                        \
+    return conv_host<T>(OP_FWD, g, input, kernel, output);                                    \
+  }                                                                                           \
+  int owlgpu_##KIND##_ndarray_conv_dilated_cuboid_im2col(                                     \
+      const T *input, const T *kernel, T *output, long batches, long input_cols,              \
+      long input_rows, long input_dpts, long in_channel, long kernel_cols, long kernel_rows,   \
+      long kernel_dpts, long output_cols, long output_rows, long output_dpts,                  \
+      long out_channel, long dpt_stride, long row_stride, long col_stride,                     \
+      long dpt_in_stride, long row_in_stride, long col_in_stride, long padding,                \
+      int precision, void *stream) {                                                          \
+    ConvGeom g;                                                                               \
+    int rc = make_conv("conv_dilated_cuboid_im2col", g, batches, input_cols, input_rows,      \
+                       input_dpts, in_channel, kernel_cols, kernel_rows, kernel_dpts,         \
+                       output_cols, output_rows, output_dpts, out_channel, col_stride,        \
+                       row_stride, dpt_stride, col_in_stride, row_in_stride, dpt_in_stride,   \
+                       false, padding);                                                       \
+    if (rc) return rc;                                                                        \
+    return conv_device<T>(OP_FWD, g, (void *)input, (void *)kernel, output, precision,        \
+                          (cudaStream_t)stream);                                              \
+  }
+
+#define CONV3D_BWD(KIND, T, NAME, OP, DIL, A_T, B_T, C_T, A_N, B_N, C_N, DILARGS, DILVALS)      \
+  int owl_##KIND##_ndarray_##NAME(A_T A_N, B_T B_N, C_T C_N, long batches, long input_cols,   \
+                                  long input_rows, long input_dpts, long in_channel,          \
+                                  long kernel_cols, long kernel_rows, long kernel_dpts,       \
+                                  long output_cols, long output_rows, long output_dpts,       \
+                                  long out_channel, long dpt_stride, long row_stride,         \
+                                  long col_stride DILARGS) {                                  \
+    ConvGeom g;                                                                               \
+    int rc = make_conv(#NAME, g, batches, input_cols, input_rows, input_dpts, in_channel,     \
+                       kernel_cols, kernel_rows, kernel_dpts, output_cols, output_rows,       \
+                       output_dpts, out_channel, col_stride, row_stride, dpt_stride, DILVALS, \
+                       true, 0);                                                              \
+    if (rc) return rc;                                                                        \
+    return conv_host<T>(OP, g, A_N, B_N, C_N);                                                \
+  }                                                                                           \
+  int owlgpu_##KIND##_ndarray_##NAME(A_T A_N, B_T B_N, C_T C_N, long batches,               \
+                                     long input_cols, long input_rows, long input_dpts,       \
+                                     long in_channel, long kernel_cols, long kernel_rows,     \
+                                     long kernel_dpts, long output_cols, long output_rows,    \
+                                     long output_dpts, long out_channel, long dpt_stride,     \
+                                     long row_stride, long col_stride DILARGS, int precision, \
+                                     void *stream) {                                          \
+    ConvGeom g;                                                                               \
+    int rc = make_conv(#NAME, g, batches, input_cols, input_rows, input_dpts, in_channel,     \
+                       kernel_cols, kernel_rows, kernel_dpts, output_cols, output_rows,       \
+                       output_dpts, out_channel, col_stride, row_stride, dpt_stride, DILVALS, \
+                       true, 0);                                                              \
+    if (rc) return rc;                                                                        \
+    return conv_device<T>(OP, g, (void *)A_N, (void *)B_N, (void *)C_N, precision,            \
+                          (cudaStream_t)stream);                                              \
+  }
+
+#define NODIL_ARGS
+#define NODIL_VALS 1, 1, 1
+#define DIL_ARGS , long dpt_in_stride, long row_in_stride, long col_in_stride
+#define DIL_VALS col_in_stride, row_in_stride, dpt_in_stride
+
+#define CONV3D_ALL(KIND, T)                                                                     \
+  CONV3D_FWD(KIND, T)                                                                          \
+  CONV3D_BWD(KIND, T, conv_cuboid_backward_input_im2col, OP_BWDI, 0, T *, const T *,           \
+             const T *, input_grad, kernel, output_grad, NODIL_ARGS, NODIL_VALS)               \
+  CONV3D_BWD(KIND, T, conv_cuboid_backward_kernel_im2col, OP_BWDK, 0, const T *, T *,          \
+             const T *, input, kernel_grad, output_grad, NODIL_ARGS, NODIL_VALS)               \
+  CONV3D_BWD(KIND, T, conv_dilated_cuboid_backward_input_im2col, OP_BWDI, 1, T *, const T *,   \
+             const T *, input_grad, kernel, output_grad, DIL_ARGS, DIL_VALS)                   \
+  CONV3D_BWD(KIND, T, conv_dilated_cuboid_backward_kernel_im2col, OP_BWDK, 1, const T *, T *,  \
+             const T *, input, kernel_grad, output_grad, DIL_ARGS, DIL_VALS)
+
+CONV3D_ALL(float32, float)
+CONV3D_ALL(float64, double)
+
+// ---- pooling -----------------------------------------------------------------
+
+#define POOL2D_FWD(KIND, T, WHICH, MODE)                                                        \
+  int owl_##KIND##_ndarray_##WHICH##_spatial(                                                  \
+      const T *input, T *output, long batches, long input_cols, long input_rows,              \
+      long in_channel, long kernel_cols, long kernel_rows, long output_cols, long output_rows, \
+      long row_stride, long col_stride, long padding, long row_in_stride,                      \
+      long col_in_stride) {                                                                    \
+    (void)row_in_stride; (void)col_in_stride;                                                  \
+    PoolGeom g;                                                                               \
+    int rc = make_pool(#WHICH "_spatial", g, batches, input_cols, input_rows, 1, in_channel,  \
+                       kernel_cols, kernel_rows, 1, output_cols, output_rows, 1, col_stride,  \
+                       row_stride, 1);                                                        \
+    if (rc) return rc;                                                                        \
+    g.pr = fwd_pad(padding, row_stride, output_rows, kernel_rows, input_rows);                \
+    g.pc = fwd_pad(padding, col_stride, output_cols, kernel_cols, input_cols);                \
+    return pool_fwd_host<T>(MODE, g, input, output, nullptr);                                 \
+  }                                                                                           \
+  int owlgpu_##KIND##_ndarray_##WHICH##_spatial(                                               \
+      const T *input, T *output, long batches, long input_cols, long input_rows,              \
+      long in_channel, long kernel_cols, long kernel_rows, long output_cols, long output_rows, \
+      long row_stride, long col_stride, long padding, long row_in_stride, long col_in_stride, \
+      int precision, void *stream) {                                                          \
+    (void)row_in_stride; (void)col_in_stride; (void)precision;                                 \
+    PoolGeom g;                                                                               \
+    int rc = make_pool(#WHICH "_spatial", g, batches, input_cols, input_rows, 1, in_channel,  \
+                       kernel_cols, kernel_rows, 1, output_cols, output_rows, 1, col_stride,  \
+                       row_stride, 1);                                                        \
+    if (rc) return rc;                                                                        \
+    g.pr = fwd_pad(padding, row_stride, output_rows, kernel_rows, input_rows);                \
+    g.pc = fwd_pad(padding, col_stride, output_cols, kernel_cols, input_cols);                \
+    return pool_fwd(dtype_of<T>(), MODE, g, input, output, nullptr, (cudaStream_t)stream);    \
+  }
+
+#define POOL2D_BWD(KIND, T, WHICH, MODE)                                                        \
+  int owl_##KIND##_ndarray_##WHICH##_spatial_backward(                                         \
+      const T *input, const T *output_grad, T *input_grad, long batches, long input_cols,     \
+      long input_rows, long in_channel, long kernel_cols, long kernel_rows, long output_cols, \
+      long output_rows, long row_stride, long col_stride, long pad_rows, long pad_cols) {      \
+    PoolGeom g;                                                                               \
+    int rc = make_pool(#WHICH "_spatial_backward", g, batches, input_cols, input_rows, 1,     \
+                       in_channel, kernel_cols, kernel_rows, 1, output_cols, output_rows, 1,  \
+                       col_stride, row_stride, 1);                                            \
+    if (rc) return rc;                                                                        \
+    g.pr = pad_rows < 0 ? 0 : (int)pad_rows;                                                  \
+    g.pc = pad_cols < 0 ? 0 : (int)pad_cols;                                                  \
+    return pool_bwd_host<T>(MODE, g, input, output_grad, input_grad);                         \
+  }                                                                                           \
+  int owlgpu_##KIND##_ndarray_##WHICH##_spatial_backward(                                      \
+      const T *input, const T *output_grad, T *input_grad, long batches, long input_cols,     \
+      long input_rows, long in_channel, long kernel_cols, long kernel_rows, long output_cols, \
+      long output_rows, long row_stride, long col_stride, long pad_rows, long pad_cols,        \
+      int precision, void *stream) {                                                          \
+    (void)precision;                                                                          \
+    PoolGeom g;                                                                               \
+    int rc = make_pool(#WHICH "_spatial_backward", g, batches, input_cols, input_rows, 1,     \
+                       in_channel, kernel_cols, kernel_rows, 1, output_cols, output_rows, 1,  \
+                       col_stride, row_stride, 1);                                            \
+    if (rc) return rc;                                                                        \
+    g.pr = pad_rows < 0 ? 0 : (int)pad_rows;                                                  \
+    g.pc = pad_cols < 0 ? 0 : (int)pad_cols;                                                  \
+    return pool_bwd(dtype_of<T>(), MODE, g, input, output_grad, input_grad,                   \
+                    (cudaStream_t)stream);                                                    \
+  }
+
+#define POOL3D(KIND, T, WHICH, MODE)                                                            \
+  int owl_##KIND##_ndarray_##WHICH##_cuboid(                                                   \
+      const T *input, T *output, long batches, long input_cols, long input_rows,              \
+      long input_dpts, long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts, \
+      long output_cols, long output_rows, long output_dpts, long dpt_stride, long row_stride, \
+      long col_stride, long padding) {                                                        \
+    PoolGeom g;                                                                               \
+    int rc = make_pool(#WHICH "_cuboid", g, batches, input_cols, input_rows, input_dpts,      \
+                       in_channel, kernel_cols, kernel_rows, kernel_dpts, output_cols,        \
+                       output_rows, output_dpts, col_stride, row_stride, dpt_stride);         \
+    if (rc) return rc;                                                                        \
+    g.pc = fwd_pad(padding, col_stride, output_cols, kernel_cols, input_cols);                \
+    g.pr = fwd_pad(padding, row_stride, output_rows, kernel_rows, input_rows);                \
+    g.pd = fwd_pad(padding, dpt_stride, output_dpts, kernel_dpts, input_dpts);                \
+    return pool_fwd_host<T>(MODE, g, input, output, nullptr);                                 \
+  }                                                                                           \
+  int owlgpu_##KIND##_ndarray_##WHICH##_cuboid(                                                \
+      const T *input, T *output, long batches, long input_cols, long input_rows,              \
+      long input_dpts, long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts, \
+      long output_cols, long output_rows, long output_dpts, long dpt_stride, long row_stride, \
+      long col_stride, long padding, int precision, void *stream) {                           \
+    (void)precision;                                                                          \
+    PoolGeom g;                                                                               \
+    int rc = make_pool(#WHICH "_cuboid", g, batches, input_cols, input_rows, input_dpts,      \
+                       in_channel, kernel_cols, kernel_rows, kernel_dpts, output_cols,        \
+                       output_rows, output_dpts, col_stride, row_stride, dpt_stride);         \
+    if (rc) return rc;                                                                        \
+    g.pc = fwd_pad(padding, col_stride, output_cols, kernel_cols, input_cols);                \
+    g.pr = fwd_pad(padding, row_stride, output_rows, kernel_rows, input_rows);                \
+    g.pd = fwd_pad(padding, dpt_stride, output_dpts, kernel_dpts, input_dpts);                \
+    return pool_fwd(dtype_of<T>(), MODE, g, input, output, nullptr, (cudaStream_t)stream);    \
+  }                                                                                           \
+  int owl_##KIND##_ndarray_##WHICH##_cuboid_backward(                                          \
+      const T *input, const T *output_grad, T *input_grad, long batches, long input_cols,     \
+      long input_rows, long input_dpts, long in_channel, long kernel_cols, long kernel_rows,   \
+      long kernel_dpts, long output_cols, long output_rows, long output_dpts, long col_stride, \
+      long row_stride, long dpt_stride, long padding) {                                        \
+    PoolGeom g;                                                                               \
+    int rc = make_pool(#WHICH "_cuboid_backward", g, batches, input_cols, input_rows,         \
+                       input_dpts, in_channel, kernel_cols, kernel_rows, kernel_dpts,         \
+                       output_cols, output_rows, output_dpts, col_stride, row_stride,         \
+                       dpt_stride);                                                           \
+    if (rc) return rc;                                                                        \
+    g.pc = fwd_pad(padding, col_stride, output_cols, kernel_cols, input_cols);                \
+    g.pr = fwd_pad(padding, row_stride, output_rows, kernel_rows, input_rows);                \
+    g.pd = fwd_pad(padding, dpt_stride, output_dpts, kernel_dpts, input_dpts);                \
+    return pool_bwd_host<T>(MODE, g, input, output_grad, input_grad);                         \
+  }                                                                                           \
+  int owlgpu_##KIND##_ndarray_##WHICH##_cuboid_backward(                                       \
+      const T *input, const T *output_grad, T *input_grad, long batches, long input_cols,     \
+      long input_rows, long input_dpts, long in_channel, long kernel_cols, long kernel_rows,   \
+      long kernel_dpts, long output_cols, long output_rows, long output_dpts, long col_stride, \
+      long row_stride, long dpt_stride, long padding, int precision, void *stream) {           \
+    (void)precision;                                                                          \
+    PoolGeom g;                                                                               \
+    int rc = make_pool(#WHICH "_cuboid_backward", g, batches, input_cols, input_rows,         \
+                       input_dpts, in_channel, kernel_cols, kernel_rows, kernel_dpts,         \
+                       output_cols, output_rows, output_dpts, col_stride, row_stride,         \
+                       dpt_stride);                                                           \
+    if (rc) return rc;                                                                        \
+    g.pc = fwd_pad(padding, col_stride, output_cols, kernel_cols, input_cols);                \
+    g.pr = fwd_pad(padding, row_stride, output_rows, kernel_rows, input_rows);                \
+    g.pd = fwd_pad(padding, dpt_stride, output_dpts, kernel_dpts, input_dpts);                \
+    return pool_bwd(dtype_of<T>(), MODE, g, input, output_grad, input_grad,                   \
+                    (cudaStream_t)stream);                                                    \
+  }
+
+#define ARGMAX(KIND, T)                                                                         \
+  int owl_##KIND##_ndarray_maxpool_argmax_spatial(                                             \
+      const T *input, T *output, int64_t *argmax, long batches, long input_cols,              \
+      long input_rows, long in_channel, long kernel_cols, long kernel_rows, long output_cols, \
+      long output_rows, long row_stride, long col_stride, long pad_rows, long pad_cols) {      \
+    PoolGeom g;                                                                               \
+    int rc = make_pool("maxpool_argmax_spatial", g, batches, input_cols, input_rows, 1,       \
+                       in_channel, kernel_cols, kernel_rows, 1, output_cols, output_rows, 1,  \
+                       col_stride, row_stride, 1);                                            \
+    if (rc) return rc;                                                                        \
+    g.pr = pad_rows < 0 ? 0 : (int)pad_rows;                                                  \
+    g.pc = pad_cols < 0 ? 0 : (int)pad_cols;                                                  \
+    return pool_fwd_host<T>(POOL_MAX, g, input, output, argmax);                              \
+  }                                                                                           \
+  int owlgpu_##KIND##_ndarray_maxpool_argmax_spatial(                                          \
+      const T *input, T *output, int64_t *argmax, long batches, long input_cols,              \
+      long input_rows, long in_channel, long kernel_cols, long kernel_rows, long output_cols, \
+      long output_rows, long row_stride, long col_stride, long pad_rows, long pad_cols,        \
+      int precision, void *stream) {                                                          \
+    (void)precision;                                                                          \
+    PoolGeom g;                                                                               \
+    int rc = make_pool("maxpool_argmax_spatial", g, batches, input_cols, input_rows, 1,       \
+                       in_channel, kernel_cols, kernel_rows, 1, output_cols, output_rows, 1,  \
+                       col_stride, row_stride, 1);                                            \
+    if (rc) return rc;                                                                        \
+    g.pr = pad_rows < 0 ? 0 : (int)pad_rows;                                                  \
+    g.pc = pad_cols < 0 ? 0 : (int)pad_cols;                                                  \
+    return pool_fwd(dtype_of<T>(), POOL_MAX, g, input, output, argmax, (cudaStream_t)stream); \
+  }
+
+#define POOL_ALL(KIND, T)            \
+  POOL2D_FWD(KIND, T, maxpool, POOL_MAX) \
+  POOL2D_FWD(KIND, T, avgpool, POOL_AVG) \
+  POOL2D_BWD(KIND, T, maxpool, POOL_MAX) \
+  POOL2D_BWD(KIND, T, avgpool, POOL_AVG) \
+  POOL3D(KIND, T, maxpool, POOL_MAX)     \
+  POOL3D(KIND, T, avgpool, POOL_AVG)     \
+  ARGMAX(KIND, T)
+
+POOL_ALL(float32, float)
+POOL_ALL(float64, double)
+
+}  // extern "C"

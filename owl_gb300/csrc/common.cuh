@@ -1,0 +1,122 @@
+// common.cuh -- shared definitions for libowlgpu (sm_103a).
+//
+// Geometry is always carried as a 3-D problem: a 2-D Owl array
+// [batch][cols][rows][ch] is the 3-D array [batch][cols][rows][1][ch] with a
+// unit depth axis, which keeps the flat element order (and therefore Owl's
+// flat argmax indices and window scan order) unchanged.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <string>
+
+namespace owlgpu {
+
+enum Dtype { F32 = 0, F64 = 1 };
+
+// Convolution geometry.  Leading pads are the values Owl's C stubs derive
+// (owl_ndarray_conv_impl.h:288-294 forward, :502-505 backward); dilation is
+// the "in stride" (owl_ndarray_conv_impl.h:3141-3142).
+struct ConvGeom {
+  int64_t B;
+  int64_t IC, IR, ID, Ci;  // input cols, rows, dpts, channels
+  int64_t KC, KR, KD;      // kernel extent
+  int64_t OC, OR, OD, Co;  // output cols, rows, dpts, channels
+  int sc, sr, sd;          // strides
+  int dc, dr, dd;          // dilation rates
+  int pc, pr, pd;          // leading padding
+  int64_t in_pixels() const { return B * IC * IR * ID; }
+  int64_t out_pixels() const { return B * OC * OR * OD; }
+  int64_t taps() const { return KC * KR * KD; }
+  int64_t x_elems() const { return in_pixels() * Ci; }
+  int64_t y_elems() const { return out_pixels() * Co; }
+  int64_t w_elems() const { return taps() * Ci * Co; }
+};
+
+// Pooling geometry (owl_ndarray_pool_impl.h:9-15, :212-219).
+struct PoolGeom {
+  int64_t B;
+  int64_t IC, IR, ID, Ch;
+  int64_t KC, KR, KD;
+  int64_t OC, OR, OD;
+  int sc, sr, sd;
+  int pc, pr, pd;
+  int64_t in_pixels() const { return B * IC * IR * ID; }
+  int64_t out_pixels() const { return B * OC * OR * OD; }
+  int64_t x_elems() const { return in_pixels() * Ch; }
+  int64_t y_elems() const { return out_pixels() * Ch; }
+};
+
+enum PoolMode { POOL_MAX = 0, POOL_AVG = 1 };
+
+// Status codes (mirrors include/owlgpu.h).
+constexpr int kOk = 0;
+constexpr int kErrInvalid = -1;
+constexpr int kErrCuda = -2;
+constexpr int kErrNoMem = -3;
+constexpr int kErrUnsupported = -4;
+constexpr int kErrTimeout = -5;
+
+// Thread-local error text, read back through owlgpu_last_error().
+void set_error(const std::string &msg);
+const char *get_error();
+int cuda_fail(cudaError_t e, const char *where);
+
+// Launch accounting: every kernel launch in the library goes through
+// note_launch() so that a caller can count the GPU work it triggered.
+extern std::atomic<uint64_t> g_launches;
+inline void note_launch(int n = 1) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
+
+#define OWL_CHECK_LAUNCH(where)                                   \
+  do {                                                            \
+    owlgpu::note_launch();                                        \
+    cudaError_t _e = cudaGetLastError();                          \
+    if (_e != cudaSuccess) return owlgpu::cuda_fail(_e, where);   \
+  } while (0)
+
+#define OWL_CUDA(call)                                            \
+  do {                                                            \
+    cudaError_t _e = (call);                                      \
+    if (_e != cudaSuccess) return owlgpu::cuda_fail(_e, #call);   \
+  } while (0)
+
+// Stream-ordered scratch allocation used by kernels that need workspace.
+int scratch_alloc(void **p, size_t bytes, cudaStream_t s);
+void scratch_free(void *p, cudaStream_t s);
+
+// ---- compute entry points (device pointers, asynchronous) --------------
+int conv_fwd(Dtype dt, int prec, const ConvGeom &g, const void *x, const void *w, void *y,
+             cudaStream_t s);
+int conv_bwd_input(Dtype dt, int prec, const ConvGeom &g, void *dx, const void *w,
+                   const void *dy, cudaStream_t s);
+int conv_bwd_kernel(Dtype dt, int prec, const ConvGeom &g, const void *x, void *dw,
+                    const void *dy, cudaStream_t s);
+
+int pool_fwd(Dtype dt, PoolMode mode, const PoolGeom &g, const void *x, void *y,
+             int64_t *argmax, cudaStream_t s);
+int pool_bwd(Dtype dt, PoolMode mode, const PoolGeom &g, const void *x, const void *dy,
+             void *dx, cudaStream_t s);
+
+// SIMT (CUDA-core) implementations: the plain FP32 path and the FP64 path.
+int simt_conv_fwd(Dtype dt, const ConvGeom &g, const void *x, const void *w, void *y,
+                  cudaStream_t s);
+int simt_conv_bwd_input(Dtype dt, const ConvGeom &g, void *dx, const void *w, const void *dy,
+                        cudaStream_t s);
+int simt_conv_bwd_kernel(Dtype dt, const ConvGeom &g, const void *x, void *dw, const void *dy,
+                         cudaStream_t s);
+
+// Tensor-core (tcgen05) implementations for float32 data.  Return
+// kErrUnsupported when a geometry is outside what the kernels handle, in
+// which case the caller reports the error (there is no silent fallback).
+int tc_conv_fwd(int prec, const ConvGeom &g, const float *x, const float *w, float *y,
+                cudaStream_t s);
+int tc_conv_bwd_input(int prec, const ConvGeom &g, float *dx, const float *w, const float *dy,
+                      cudaStream_t s);
+int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, const float *dy,
+                       cudaStream_t s);
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+}  // namespace owlgpu

@@ -1,0 +1,427 @@
+// conv_simt.cu -- CUDA-core implicit-GEMM convolutions (float32 "plain" and
+// float64), forward / backward-input / backward-kernel, 2-D, 3-D, strided,
+// dilated.  No im2col matrix is ever materialised: every GEMM operand element
+// is gathered from the NHWC-style Owl array while the tile is staged into
+// shared memory.
+//
+// GEMM views (k = ((kc*KR + kr)*KD + kd)*Ci + ci, Owl's im2col column order,
+// owl_ndarray_conv_impl.h:315-325):
+//   forward      Y[m][co]  = sum_k  X[gather(m, k)]           * W[k][co]
+//                m = output pixel (b, oc, or, od)
+//   bwd input    dX[m][ci] = sum_{tap,co} dY[scatter^-1(m,tap)][co] * W[tap][ci][co]
+//                m = input pixel; only taps with (i + p - t*d) % s == 0 hit
+//   bwd kernel   dW[tap*Ci+ci][co] = sum_m X[gather(m, tap)][ci] * dY[m][co]
+//                reduction over output pixels, split across CTAs and summed
+//                by a second kernel in a fixed order (deterministic).
+#include "common.cuh"
+
+namespace owlgpu {
+namespace {
+
+enum Mode { FWD = 0, BWDI = 1, BWDK = 2 };
+
+struct Dev {
+  int64_t B, IC, IR, ID, Ci, KC, KR, KD, OC, OR, OD, Co;
+  int sc, sr, sd, dc, dr, dd, pc, pr, pd;
+  int64_t M, N, K;  // GEMM view sizes
+};
+
+template <typename T, int MODE, int BM, int BN, int BK, int TM, int TN>
+__global__ void __launch_bounds__((BM / TM) * (BN / TN))
+    conv_simt_kernel(Dev g, const T *__restrict__ A0, const T *__restrict__ B0,
+                     T *__restrict__ C, int64_t k_per_split) {
+  constexpr int NT = (BM / TM) * (BN / TN);
+  constexpr int A_PER = BM * BK / NT;
+  constexpr int B_PER = BN * BK / NT;
+  static_assert(BM * BK % NT == 0 && BN * BK % NT == 0, "tile/thread mismatch");
+
+  __shared__ T As[2][BK][BM + 4];
+  __shared__ T Bs[2][BK][BN + 4];
+  // Per-row (FWD/BWDI) or per-k (BWDK) pixel decode cache.
+  constexpr int PIX = (MODE == BWDK) ? BK : BM;
+  __shared__ int64_t s_base[2][PIX];
+  __shared__ int s_c[2][PIX], s_r[2][PIX], s_d[2][PIX];
+
+  const int tid = threadIdx.x;
+  const int64_t m0 = (int64_t)blockIdx.x * BM;
+  const int64_t n0 = (int64_t)blockIdx.y * BN;
+  const int64_t k_begin = (int64_t)blockIdx.z * k_per_split;
+  const int64_t k_end = min(g.K, k_begin + k_per_split);
+
+  // ---- pixel decode helpers ------------------------------------------
+  // FWD: row m is an output pixel; store batch base of X and window origin.
+  // BWDI: row m is an input pixel; store batch base of dY and (i + pad).
+  // BWDK: k index is an output pixel; store batch base of X and origin.
+  auto decode_pixel = [&](int64_t p, int slot, int buf) {
+    if (MODE == BWDI) {
+      if (p < g.M) {
+        int64_t id = p % g.ID, t = p / g.ID;
+        int64_t ir = t % g.IR; t /= g.IR;
+        int64_t ic = t % g.IC, b = t / g.IC;
+        s_base[buf][slot] = b * g.OC * g.OR * g.OD;
+        s_c[buf][slot] = (int)ic + g.pc;
+        s_r[buf][slot] = (int)ir + g.pr;
+        s_d[buf][slot] = (int)id + g.pd;
+      } else {
+        s_base[buf][slot] = -1;
+      }
+    } else {
+      int64_t lim = (MODE == FWD) ? g.M : g.K;
+      if (p < lim) {
+        int64_t od = p % g.OD, t = p / g.OD;
+        int64_t orr = t % g.OR; t /= g.OR;
+        int64_t oc = t % g.OC, b = t / g.OC;
+        s_base[buf][slot] = b * g.IC * g.IR * g.ID;
+        s_c[buf][slot] = (int)(oc * g.sc) - g.pc;
+        s_r[buf][slot] = (int)(orr * g.sr) - g.pr;
+        s_d[buf][slot] = (int)(od * g.sd) - g.pd;
+      } else {
+        s_base[buf][slot] = -1;
+      }
+    }
+  };
+
+  if (MODE != BWDK) {
+    for (int i = tid; i < BM; i += NT) decode_pixel(m0 + i, i, 0);
+    for (int i = tid; i < BM; i += NT) {
+      s_base[1][i] = s_base[0][i];
+      s_c[1][i] = s_c[0][i]; s_r[1][i] = s_r[0][i]; s_d[1][i] = s_d[0][i];
+    }
+  }
+
+  T a_reg[A_PER], b_reg[B_PER];
+
+  // Gather one BK-slab of A and B into registers.
+  auto load_tiles = [&](int64_t k0, int buf) {
+    if (MODE == FWD) {
+      // A[m][k]: thread owns a fixed k column, several rows.
+      const int kk = tid % BK;
+      const int64_t k = k0 + kk;
+      int kc = 0, kr = 0, kd = 0, ci = 0;
+      bool kval = k < k_end;
+      if (kval) {
+        int64_t tap = k / g.Ci;
+        ci = (int)(k - tap * g.Ci);
+        kd = (int)(tap % g.KD); tap /= g.KD;
+        kr = (int)(tap % g.KR); kc = (int)(tap / g.KR);
+      }
+#pragma unroll
+      for (int i = 0; i < A_PER; ++i) {
+        int mm = tid / BK + i * (NT / BK);
+        T v = T(0);
+        int64_t base = s_base[buf][mm];
+        if (kval && base >= 0) {
+          int c = s_c[buf][mm] + kc * g.dc, r = s_r[buf][mm] + kr * g.dr,
+              d = s_d[buf][mm] + kd * g.dd;
+          if (c >= 0 && c < g.IC && r >= 0 && r < g.IR && d >= 0 && d < g.ID)
+            v = A0[((base + ((int64_t)c * g.IR + r) * g.ID + d) * g.Ci) + ci];
+        }
+        a_reg[i] = v;
+      }
+      // B[k][n] = W[k][n], n fastest.
+#pragma unroll
+      for (int i = 0; i < B_PER; ++i) {
+        int e = tid + i * NT;
+        int kk2 = e / BN, nn = e % BN;
+        int64_t kq = k0 + kk2, n = n0 + nn;
+        b_reg[i] = (kq < k_end && n < g.N) ? B0[kq * g.N + n] : T(0);
+      }
+    } else if (MODE == BWDI) {
+      // A[m][k], k = tap*Co + co: thread owns fixed k, several rows.
+      const int kk = tid % BK;
+      const int64_t k = k0 + kk;
+      int kc = 0, kr = 0, kd = 0, co = 0;
+      bool kval = k < k_end;
+      if (kval) {
+        int64_t tap = k / g.Co;
+        co = (int)(k - tap * g.Co);
+        kd = (int)(tap % g.KD); tap /= g.KD;
+        kr = (int)(tap % g.KR); kc = (int)(tap / g.KR);
+      }
+#pragma unroll
+      for (int i = 0; i < A_PER; ++i) {
+        int mm = tid / BK + i * (NT / BK);
+        T v = T(0);
+        int64_t base = s_base[buf][mm];
+        if (kval && base >= 0) {
+          int tc = s_c[buf][mm] - kc * g.dc, tr = s_r[buf][mm] - kr * g.dr,
+              td = s_d[buf][mm] - kd * g.dd;
+          if (tc >= 0 && tr >= 0 && td >= 0 && tc % g.sc == 0 && tr % g.sr == 0 &&
+              td % g.sd == 0) {
+            int oc = tc / g.sc, orr = tr / g.sr, od = td / g.sd;
+            if (oc < g.OC && orr < g.OR && od < g.OD)
+              v = A0[((base + ((int64_t)oc * g.OR + orr) * g.OD + od) * g.Co) + co];
+          }
+        }
+        a_reg[i] = v;
+      }
+      // B[k][n] = W[tap][n=ci][co]: co fastest across threads for coalescing.
+#pragma unroll
+      for (int i = 0; i < B_PER; ++i) {
+        int e = tid + i * NT;
+        int kk2 = e % BK, nn = e / BK;
+        int64_t kq = k0 + kk2, n = n0 + nn;
+        T v = T(0);
+        if (kq < k_end && n < g.N) {
+          int64_t tap = kq / g.Co, co = kq - tap * g.Co;
+          v = B0[(tap * g.Ci + n) * g.Co + co];
+        }
+        b_reg[i] = v;
+      }
+    } else {
+      // BWDK: A[m=(tap,ci)][k=pixel] = X[gather], m fastest across threads.
+#pragma unroll
+      for (int i = 0; i < A_PER; ++i) {
+        int e = tid + i * NT;
+        int mm = e % BM, kk = e / BM;
+        int64_t m = m0 + mm;
+        T v = T(0);
+        int64_t base = s_base[buf][kk];
+        if (m < g.M && base >= 0) {
+          int64_t tap = m / g.Ci;
+          int ci = (int)(m - tap * g.Ci);
+          int kd = (int)(tap % g.KD); tap /= g.KD;
+          int kr = (int)(tap % g.KR), kc = (int)(tap / g.KR);
+          int c = s_c[buf][kk] + kc * g.dc, r = s_r[buf][kk] + kr * g.dr,
+              d = s_d[buf][kk] + kd * g.dd;
+          if (c >= 0 && c < g.IC && r >= 0 && r < g.IR && d >= 0 && d < g.ID)
+            v = A0[((base + ((int64_t)c * g.IR + r) * g.ID + d) * g.Ci) + ci];
+        }
+        a_reg[i] = v;
+      }
+      // B[k=pixel][n=co] = dY[pixel][co].
+#pragma unroll
+      for (int i = 0; i < B_PER; ++i) {
+        int e = tid + i * NT;
+        int kk2 = e / BN, nn = e % BN;
+        int64_t kq = k0 + kk2, n = n0 + nn;
+        b_reg[i] = (kq < k_end && n < g.N) ? B0[kq * g.N + n] : T(0);
+      }
+    }
+  };
+
+  auto store_tiles = [&](int buf) {
+    if (MODE == BWDK) {
+#pragma unroll
+      for (int i = 0; i < A_PER; ++i) {
+        int e = tid + i * NT;
+        As[buf][e / BM][e % BM] = a_reg[i];
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < A_PER; ++i) {
+        int mm = tid / BK + i * (NT / BK);
+        As[buf][tid % BK][mm] = a_reg[i];
+      }
+    }
+    if (MODE == BWDI) {
+#pragma unroll
+      for (int i = 0; i < B_PER; ++i) {
+        int e = tid + i * NT;
+        Bs[buf][e % BK][e / BK] = b_reg[i];
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < B_PER; ++i) {
+        int e = tid + i * NT;
+        Bs[buf][e / BN][e % BN] = b_reg[i];
+      }
+    }
+  };
+
+  T acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) acc[i][j] = T(0);
+
+  const int tx = tid % (BN / TN), ty = tid / (BN / TN);
+
+  if (k_begin < k_end) {
+    int buf = 0;
+    if (MODE == BWDK) {
+      for (int i = tid; i < BK; i += NT) decode_pixel(k_begin + i, i, 0);
+      __syncthreads();
+    }
+    load_tiles(k_begin, 0);
+    store_tiles(0);
+    __syncthreads();
+    for (int64_t k0 = k_begin; k0 < k_end; k0 += BK) {
+      const int64_t kn = k0 + BK;
+      const bool more = kn < k_end;
+      if (more) {
+        if (MODE == BWDK) {
+          for (int i = tid; i < BK; i += NT) decode_pixel(kn + i, i, buf ^ 1);
+          __syncthreads();
+        }
+        load_tiles(kn, buf ^ 1);
+      }
+#pragma unroll
+      for (int kk = 0; kk < BK; ++kk) {
+        T a[TM], b[TN];
+#pragma unroll
+        for (int i = 0; i < TM; ++i) a[i] = As[buf][kk][ty * TM + i];
+#pragma unroll
+        for (int j = 0; j < TN; ++j) b[j] = Bs[buf][kk][tx * TN + j];
+#pragma unroll
+        for (int i = 0; i < TM; ++i)
+#pragma unroll
+          for (int j = 0; j < TN; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+      }
+      if (more) store_tiles(buf ^ 1);
+      __syncthreads();
+      buf ^= 1;
+    }
+  }
+
+  // ---- epilogue --------------------------------------------------------
+  T *Cz = C + (MODE == BWDK ? (int64_t)blockIdx.z * g.M * g.N : 0);
+#pragma unroll
+  for (int i = 0; i < TM; ++i) {
+    int64_t m = m0 + ty * TM + i;
+    if (m >= g.M) continue;
+#pragma unroll
+    for (int j = 0; j < TN; ++j) {
+      int64_t n = n0 + tx * TN + j;
+      if (n < g.N) Cz[m * g.N + n] = acc[i][j];
+    }
+  }
+}
+
+// Fixed-order sum of split-K partials: out[i] = ((p0 + p1) + p2) + ...
+template <typename T>
+__global__ void splitk_reduce_kernel(const T *__restrict__ part, T *__restrict__ out,
+                                     int64_t n, int splits) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (; i < n; i += stride) {
+    T s = part[i];
+    for (int z = 1; z < splits; ++z) s += part[(int64_t)z * n + i];
+    out[i] = s;
+  }
+}
+
+Dev make_dev(const ConvGeom &g, int mode) {
+  Dev d;
+  d.B = g.B; d.IC = g.IC; d.IR = g.IR; d.ID = g.ID; d.Ci = g.Ci;
+  d.KC = g.KC; d.KR = g.KR; d.KD = g.KD;
+  d.OC = g.OC; d.OR = g.OR; d.OD = g.OD; d.Co = g.Co;
+  d.sc = g.sc; d.sr = g.sr; d.sd = g.sd;
+  d.dc = g.dc; d.dr = g.dr; d.dd = g.dd;
+  d.pc = g.pc; d.pr = g.pr; d.pd = g.pd;
+  if (mode == FWD) { d.M = g.out_pixels(); d.N = g.Co; d.K = g.taps() * g.Ci; }
+  else if (mode == BWDI) { d.M = g.in_pixels(); d.N = g.Ci; d.K = g.taps() * g.Co; }
+  else { d.M = g.taps() * g.Ci; d.N = g.Co; d.K = g.out_pixels(); }
+  return d;
+}
+
+template <typename T, int MODE, int BM, int BN, int BK, int TM, int TN>
+int launch_cfg(const Dev &d, const T *A, const T *B, T *C, int splits, int64_t kps,
+               cudaStream_t s) {
+  constexpr int NT = (BM / TM) * (BN / TN);
+  dim3 grid((unsigned)ceil_div(d.M, BM), (unsigned)ceil_div(d.N, BN), (unsigned)splits);
+  conv_simt_kernel<T, MODE, BM, BN, BK, TM, TN><<<grid, NT, 0, s>>>(d, A, B, C, kps);
+  OWL_CHECK_LAUNCH("conv_simt_kernel");
+  return kOk;
+}
+
+// Tile choice by the GEMM's N (output channels for FWD, input channels for
+// BWDI, Co for BWDK).
+template <typename T, int MODE>
+int launch_any(const Dev &d, const T *A, const T *B, T *C, int splits, int64_t kps,
+               cudaStream_t s) {
+  if (sizeof(T) == 4) {
+    if (d.N > 64) return launch_cfg<T, MODE, 128, 128, 8, 8, 8>(d, A, B, C, splits, kps, s);
+    if (d.N > 32) return launch_cfg<T, MODE, 128, 64, 8, 8, 4>(d, A, B, C, splits, kps, s);
+    return launch_cfg<T, MODE, 128, 32, 8, 4, 4>(d, A, B, C, splits, kps, s);
+  } else {
+    if (d.N > 32) return launch_cfg<T, MODE, 64, 64, 8, 4, 4>(d, A, B, C, splits, kps, s);
+    return launch_cfg<T, MODE, 64, 32, 8, 4, 2>(d, A, B, C, splits, kps, s);
+  }
+}
+
+template <typename T>
+int tile_m(const Dev &d) { return sizeof(T) == 4 ? 128 : 64; }
+template <typename T>
+int tile_n(const Dev &d) {
+  if (sizeof(T) == 4) return d.N > 64 ? 128 : (d.N > 32 ? 64 : 32);
+  return d.N > 32 ? 64 : 32;
+}
+
+template <typename T>
+int fwd_t(const ConvGeom &g, const T *x, const T *w, T *y, cudaStream_t s) {
+  Dev d = make_dev(g, FWD);
+  if (d.M == 0 || d.N == 0) return kOk;
+  if (d.K == 0) {
+    OWL_CUDA(cudaMemsetAsync(y, 0, sizeof(T) * d.M * d.N, s));
+    return kOk;
+  }
+  return launch_any<T, FWD>(d, x, w, y, 1, d.K, s);
+}
+
+template <typename T>
+int bwdi_t(const ConvGeom &g, T *dx, const T *w, const T *dy, cudaStream_t s) {
+  Dev d = make_dev(g, BWDI);
+  if (d.M == 0 || d.N == 0) return kOk;
+  if (d.K == 0) {
+    OWL_CUDA(cudaMemsetAsync(dx, 0, sizeof(T) * d.M * d.N, s));
+    return kOk;
+  }
+  return launch_any<T, BWDI>(d, dy, w, dx, 1, d.K, s);
+}
+
+template <typename T>
+int bwdk_t(const ConvGeom &g, const T *x, T *dw, const T *dy, cudaStream_t s) {
+  Dev d = make_dev(g, BWDK);
+  if (d.M == 0 || d.N == 0) return kOk;
+  if (d.K == 0) {
+    OWL_CUDA(cudaMemsetAsync(dw, 0, sizeof(T) * d.M * d.N, s));
+    return kOk;
+  }
+  // Split the pixel reduction so that ~4 waves of CTAs cover 152 SMs, with
+  // each split at least 8 K-tiles deep.
+  int64_t tiles = ceil_div(d.M, tile_m<T>(d)) * ceil_div(d.N, tile_n<T>(d));
+  int64_t want = ceil_div(4 * 152, tiles);
+  int64_t max_by_k = ceil_div(d.K, 64);
+  int splits = (int)std::max<int64_t>(1, std::min<int64_t>(want, std::min<int64_t>(max_by_k, 256)));
+  int64_t kps = ceil_div(ceil_div(d.K, splits), 8) * 8;
+  splits = (int)ceil_div(d.K, kps);
+  if (splits == 1) return launch_any<T, BWDK>(d, x, dy, dw, 1, kps, s);
+  void *ws = nullptr;
+  size_t bytes = sizeof(T) * (size_t)splits * d.M * d.N;
+  int rc = scratch_alloc(&ws, bytes, s);
+  if (rc) return rc;
+  rc = launch_any<T, BWDK>(d, x, dy, (T *)ws, splits, kps, s);
+  if (rc == kOk) {
+    int64_t n = d.M * d.N;
+    int blocks = (int)std::min<int64_t>(ceil_div(n, 256), 4 * 152);
+    splitk_reduce_kernel<T><<<blocks, 256, 0, s>>>((const T *)ws, dw, n, splits);
+    cudaError_t e = cudaGetLastError();
+    note_launch();
+    if (e != cudaSuccess) rc = cuda_fail(e, "splitk_reduce_kernel");
+  }
+  scratch_free(ws, s);
+  return rc;
+}
+
+}  // namespace
+
+int simt_conv_fwd(Dtype dt, const ConvGeom &g, const void *x, const void *w, void *y,
+                  cudaStream_t s) {
+  return dt == F32 ? fwd_t<float>(g, (const float *)x, (const float *)w, (float *)y, s)
+                   : fwd_t<double>(g, (const double *)x, (const double *)w, (double *)y, s);
+}
+
+int simt_conv_bwd_input(Dtype dt, const ConvGeom &g, void *dx, const void *w, const void *dy,
+                        cudaStream_t s) {
+  return dt == F32 ? bwdi_t<float>(g, (float *)dx, (const float *)w, (const float *)dy, s)
+                   : bwdi_t<double>(g, (double *)dx, (const double *)w, (const double *)dy, s);
+}
+
+int simt_conv_bwd_kernel(Dtype dt, const ConvGeom &g, const void *x, void *dw, const void *dy,
+                         cudaStream_t s) {
+  return dt == F32 ? bwdk_t<float>(g, (const float *)x, (float *)dw, (const float *)dy, s)
+                   : bwdk_t<double>(g, (const double *)x, (double *)dw, (const double *)dy, s);
+}
+
+}  // namespace owlgpu
