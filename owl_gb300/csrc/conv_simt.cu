@@ -87,6 +87,7 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
       s_base[1][i] = s_base[0][i];
       s_c[1][i] = s_c[0][i]; s_r[1][i] = s_r[0][i]; s_d[1][i] = s_d[0][i];
     }
+    __syncthreads();  // rows decoded by one thread are gathered by others
   }
 
   T a_reg[A_PER], b_reg[B_PER];

@@ -84,7 +84,7 @@ def parse_file(path: Path) -> list[dict]:
     text = path.read_text()
     comments = _strip_comments(text)
     cases = []
-    for mod in re.finditer(r"module (To_test_\w+) = struct(.*?)\nend", text, re.S):
+    for mod in re.finditer(r"module (To_test_\w+) = struct(.*?)\n\s*end\b", text, re.S):
         mname, body = mod.group(1), mod.group(2)
         base = mod.start(2)
         starts = [m for m in re.finditer(r"let (fun\d+) \(\) =", body)]
