@@ -699,6 +699,28 @@ int owlgpu_float64_ndarray_avgpool_cuboid_backward(
     long output_cols, long output_rows, long output_dpts, long col_stride,
     long row_stride, long dpt_stride, long padding OWLGPU_DEVICE_ARGS);
 
+/* ======================================================================
+ * Allocation-free entry point.  No counterpart in the reference: Owl's C
+ * stubs allocate their own scratch with malloc.  This is the float32 2-D
+ * conv backward_kernel (same arguments and results as
+ * owlgpu_float32_ndarray_conv_spatial_backward_kernel at FP32) for callers
+ * that cannot let a library allocate GPU memory mid-call: programs whose HBM
+ * is owned by another allocator's arena, and latency- or budget-bound code
+ * that must not touch the driver allocator.  Its split-K scratch is a fixed
+ * 16 MiB device array held by every GPU that loads the library until exit;
+ * kernels with more than 4,194,304 elements (kernel_cols * kernel_rows *
+ * in_channel * out_channel) are rejected with OWLGPU_ERR_INVALID.  The first
+ * call on a device looks up the array's device address, so make it before
+ * any stream capture; calls that overlap on the GPU share the array and
+ * race, so serialise them.  Device pointers; asynchronous on `stream`.
+ * ====================================================================== */
+int owlgpu_float32_ndarray_conv_spatial_backward_kernel_noalloc(
+    const float *input, float *kernel_grad, const float *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride, void *stream);
+
 #if defined(__GNUC__)
 #pragma GCC visibility pop
 #endif

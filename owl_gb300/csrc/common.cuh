@@ -107,6 +107,12 @@ int simt_conv_bwd_input(Dtype dt, const ConvGeom &g, void *dx, const void *w, co
 int simt_conv_bwd_kernel(Dtype dt, const ConvGeom &g, const void *x, void *dw, const void *dy,
                          cudaStream_t s);
 
+// backward_kernel (float32, SIMT) with split-K partials in a caller-provided
+// workspace of ws_elems floats; splits are capped to fit it.
+int simt_conv_bwd_kernel_f32_into(const ConvGeom &g, const float *x, float *dw,
+                                  const float *dy, float *ws, int64_t ws_elems,
+                                  cudaStream_t s);
+
 // Tensor-core (tcgen05) implementations for float32 data.  Return
 // kErrUnsupported when a geometry is outside what the kernels handle, in
 // which case the caller reports the error (there is no silent fallback).

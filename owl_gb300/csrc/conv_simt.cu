@@ -405,7 +405,44 @@ int bwdk_t(const ConvGeom &g, const T *x, T *dw, const T *dy, cudaStream_t s) {
   return rc;
 }
 
+// backward_kernel, float32, with the split-K partials written into a
+// caller-provided workspace of `ws_elems` floats instead of an allocation.
+// The split count is capped so that splits * |dW| fits the workspace; every
+// partial element is written before it is read, so the workspace needs no
+// clearing between calls.
+int bwdk_f32_into(const ConvGeom &g, const float *x, float *dw, const float *dy, float *ws,
+                  int64_t ws_elems, cudaStream_t s) {
+  Dev d = make_dev(g, BWDK);
+  if (d.M == 0 || d.N == 0) return kOk;
+  if (d.K == 0) {
+    OWL_CUDA(cudaMemsetAsync(dw, 0, sizeof(float) * d.M * d.N, s));
+    return kOk;
+  }
+  int64_t tiles = ceil_div(d.M, tile_m<float>(d)) * ceil_div(d.N, tile_n<float>(d));
+  int64_t want = ceil_div(4 * 152, tiles);
+  int64_t max_by_k = ceil_div(d.K, 64);
+  int64_t max_by_ws = ws_elems / (d.M * d.N);
+  int splits = (int)std::max<int64_t>(
+      1, std::min<int64_t>(std::min<int64_t>(want, max_by_ws), std::min<int64_t>(max_by_k, 256)));
+  int64_t kps = ceil_div(ceil_div(d.K, splits), 8) * 8;
+  splits = (int)ceil_div(d.K, kps);
+  if (splits == 1) return launch_any<float, BWDK>(d, x, dy, dw, 1, kps, s);
+  int rc = launch_any<float, BWDK>(d, x, dy, ws, splits, kps, s);
+  if (rc != kOk) return rc;
+  int64_t n = d.M * d.N;
+  int blocks = (int)std::min<int64_t>(ceil_div(n, 256), 4 * 152);
+  splitk_reduce_kernel<float><<<blocks, 256, 0, s>>>(ws, dw, n, splits);
+  OWL_CHECK_LAUNCH("splitk_reduce_kernel");
+  return kOk;
+}
+
 }  // namespace
+
+int simt_conv_bwd_kernel_f32_into(const ConvGeom &g, const float *x, float *dw,
+                                  const float *dy, float *ws, int64_t ws_elems,
+                                  cudaStream_t s) {
+  return bwdk_f32_into(g, x, dw, dy, ws, ws_elems, s);
+}
 
 int simt_conv_fwd(Dtype dt, const ConvGeom &g, const void *x, const void *w, void *y,
                   cudaStream_t s) {
