@@ -72,6 +72,13 @@ int owlgpu_get_precision(void);
 /* Number of kernel launches issued by this library since the process began
  * (all threads).  Lets a caller count GPU work inside a timed region. */
 uint64_t owlgpu_launch_count(void);
+/* Kernel family that ran the calling thread's last convolution:
+ * 0 = CUDA cores (FP32 / FP64), 1 = tcgen05 tensor cores, -1 = none yet. */
+int owlgpu_last_conv_path(void);
+/* Synchronise the host drop-in stream and report OWLGPU_ERR_TIMEOUT if a
+ * tensor-core kernel abandoned a bounded pipeline wait since the last check
+ * (the host drop-in entry points check this themselves). */
+int owlgpu_device_status(void);
 /* Device ordinal used by the host drop-in entry points (default 0). */
 int owlgpu_set_device(int device);
 /* Release cached device/pinned staging memory held by the host drop-in. */

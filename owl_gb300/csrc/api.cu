@@ -53,12 +53,24 @@ void scratch_free(void *p, cudaStream_t s) {
 
 static bool tc_requested(Dtype dt, int prec) { return dt == F32 && prec != OWLGPU_PREC_FP32; }
 
+// Kernel family used by the calling thread's last convolution (reported by
+// owlgpu_last_conv_path): 0 = CUDA-core (FP32/FP64), 1 = tcgen05 tensor cores.
+static thread_local int t_last_path = -1;
+
+// A float32 request for tensor-core precision runs on tcgen05 when the
+// geometry is one the tensor-core kernels implement (stride 1 today);
+// otherwise it runs on the FP32 CUDA-core kernels, which are at least as
+// accurate.  The path taken is visible through owlgpu_last_conv_path().
 int conv_fwd(Dtype dt, int prec, const ConvGeom &g, const void *x, const void *w, void *y,
              cudaStream_t s) {
   if (tc_requested(dt, prec)) {
     int rc = tc_conv_fwd(prec, g, (const float *)x, (const float *)w, (float *)y, s);
-    if (rc != kErrUnsupported) return rc;
+    if (rc != kErrUnsupported) {
+      t_last_path = 1;
+      return rc;
+    }
   }
+  t_last_path = 0;
   return simt_conv_fwd(dt, g, x, w, y, s);
 }
 
@@ -66,8 +78,12 @@ int conv_bwd_input(Dtype dt, int prec, const ConvGeom &g, void *dx, const void *
                    const void *dy, cudaStream_t s) {
   if (tc_requested(dt, prec)) {
     int rc = tc_conv_bwd_input(prec, g, (float *)dx, (const float *)w, (const float *)dy, s);
-    if (rc != kErrUnsupported) return rc;
+    if (rc != kErrUnsupported) {
+      t_last_path = 1;
+      return rc;
+    }
   }
+  t_last_path = 0;
   return simt_conv_bwd_input(dt, g, dx, w, dy, s);
 }
 
@@ -75,8 +91,12 @@ int conv_bwd_kernel(Dtype dt, int prec, const ConvGeom &g, const void *x, void *
                     const void *dy, cudaStream_t s) {
   if (tc_requested(dt, prec)) {
     int rc = tc_conv_bwd_kernel(prec, g, (const float *)x, (float *)dw, (const float *)dy, s);
-    if (rc != kErrUnsupported) return rc;
+    if (rc != kErrUnsupported) {
+      t_last_path = 1;
+      return rc;
+    }
   }
+  t_last_path = 0;
   return simt_conv_bwd_kernel(dt, g, x, dw, dy, s);
 }
 
@@ -238,6 +258,14 @@ static int host_call(std::vector<Buf> bufs, F body) {
   for (auto &b : bufs) scratch_free(b.dev, s);
   cudaError_t e = cudaStreamSynchronize(s);
   if (rc == kOk && e != cudaSuccess) rc = cuda_fail(e, "cudaStreamSynchronize");
+  if (rc == kOk) {
+    int st = 0;
+    rc = tc_read_status(&st, s);
+    if (rc == kOk && st) {
+      set_error("a tensor-core kernel gave up waiting on one of its pipeline barriers");
+      rc = kErrTimeout;
+    }
+  }
   return rc;
 }
 
@@ -320,6 +348,20 @@ int owlgpu_set_precision(int p) {
 }
 int owlgpu_get_precision(void) { return default_precision(); }
 uint64_t owlgpu_launch_count(void) { return g_launches.load(); }
+int owlgpu_last_conv_path(void) { return t_last_path; }
+int owlgpu_device_status(void) {
+  cudaStream_t s;
+  int rc = host_stream(&s);
+  if (rc) return rc;
+  int v = 0;
+  rc = tc_read_status(&v, s);
+  if (rc) return rc;
+  if (v) {
+    set_error("a tensor-core kernel gave up waiting on one of its pipeline barriers");
+    return kErrTimeout;
+  }
+  return kOk;
+}
 int owlgpu_set_device(int d) {
   int n = 0;
   OWL_CUDA(cudaGetDeviceCount(&n));

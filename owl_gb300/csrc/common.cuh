@@ -123,6 +123,9 @@ int tc_conv_bwd_input(int prec, const ConvGeom &g, float *dx, const float *w, co
 int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, const float *dy,
                        cudaStream_t s);
 
+// Read (and clear) the tensor-core kernels' device error word on stream s.
+int tc_read_status(int *out, cudaStream_t s);
+
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
 }  // namespace owlgpu

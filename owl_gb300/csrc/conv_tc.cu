@@ -1,16 +1,657 @@
-// conv_tc.cu -- tcgen05 tensor-core convolutions (placeholder until the
-// kernels land): report the geometry as unsupported so the dispatcher runs
-// the FP32 CUDA-core kernels.
+// conv_tc.cu -- tcgen05 tensor-core convolutions for float32 data
+// (precisions BF16, TF32 and split BF16 "BF16X3"), forward and backward-input,
+// stride 1, any dilation, 2-D and 3-D.
+//
+// Design: persistent, warp-specialised "halo" implicit GEMM.
+//   * An output tile is 16*MH positions along one spatial axis (u) by 8 along
+//     another (v); each group of 8 v-positions is one 8-row core-matrix band
+//     of the MMA's M = 128 rows.  MH (1 or 2) M=128 halves share every B tile.
+//   * Producer warps load the input halo the tile needs for one block of
+//     channels -- once -- from the float32 activation, convert it (bf16 RN,
+//     tf32 RNA, or bf16 hi + lo) and store it in shared memory as
+//     [16-byte channel chunk][halo pixel][16 B].  Any 8 consecutive v-pixels
+//     then form a K-major core matrix, so the A operand for every tap is the
+//     same halo seen through a shifted descriptor: each staged pixel feeds all
+//     KC*KR*KD taps with no im2col copy anywhere.
+//   * The kernel tensor is re-laid out once per call (prep_weights) into the
+//     exact shared-memory image of each (channel block, tap) B tile, which one
+//     thread streams with cp.async.bulk (TMA engine) into a ring of stages.
+//   * One thread issues tcgen05.mma (M=128, N=BN, K=16/8 per instruction)
+//     into a double-buffered TMEM accumulator; four epilogue warps drain the
+//     other buffer (tcgen05.ld) and write float32 results to HBM.
+//   * Every wait is bounded: a stuck barrier sets an error word and the CTA
+//     unwinds (waits for its in-flight copies and MMAs, frees TMEM, returns).
+//
+// Backward-input with stride 1 is the same computation on dY with the kernel
+// flipped in every spatial axis and its channel axes exchanged:
+//   dX[i] = sum_t dY[i + p - t*d] W[t]^T = sum_t' dY[i - ((K-1)d - p) + t'd] W[K-1-t']^T.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <mutex>
+
+#include "../../include/owlgpu.h"
 #include "common.cuh"
+#include "tc_ptx.cuh"
 
 namespace owlgpu {
-int tc_conv_fwd(int, const ConvGeom &, const float *, const float *, float *, cudaStream_t) {
+namespace {
+
+using namespace ptx;
+
+constexpr int kProducerWarps = 8;
+constexpr int kMmaWarp = kProducerWarps;
+constexpr int kLoadWarp = kProducerWarps + 1;
+constexpr int kThreads = (kProducerWarps + 2 + 4) * 32;  // + MMA, loader, 4 epilogue warps
+constexpr int kProducerThreads = kProducerWarps * 32;
+constexpr int kSmemMax = 232448;  // 227 KB opt-in dynamic shared memory
+constexpr long long kSpinLimit = 4000000000LL;  // cycles (~2 s) before a wait gives up
+
+enum Kind { K_BF16 = 0, K_TF32 = 1, K_BF16X3 = 2 };
+
+struct TcParams {
+  const float *x;
+  float *y;
+  const uint8_t *wt_hi, *wt_lo;
+  int *status;
+  int B, IW, IU, IV, OW, OU, OV, KW, KU, KV, dw, du, dv, pw, pu, pv;
+  long long xsb, xsw, xsu, xsv, ysb, ysw, ysu, ysv;  // pixel strides
+  int Cin, Cout;
+  int BN, CB, NCH, CPB, NCB, T, MH;
+  int HW, HU, HV, HP, PS;
+  int n_tiles, u_tiles, v_tiles;
+  long long total_tiles;
+  unsigned halo_bytes, b_bytes;
+  int NH, NB;
+  unsigned idesc, tmem_cols;
+  int vec_in, vec_out;
+};
+
+__device__ int g_tc_status;
+
+// Bounded mbarrier wait.  Returns false when the CTA is aborting.
+__device__ __forceinline__ bool wait_bar(uint32_t bar, uint32_t parity, volatile int *abort_flag,
+                                         int *status) {
+  if (mbar_try_wait(bar, parity)) return true;
+  long long t0 = clock64();
+  while (true) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*abort_flag) return false;
+    if (clock64() - t0 > kSpinLimit) {
+      *abort_flag = 1;
+      atomicExch(status, 1);
+      return false;
+    }
+  }
+}
+
+struct Tile {
+  int nt, b, ow, u0, v0;
+};
+
+__device__ __forceinline__ Tile decode_tile(const TcParams &p, long long t) {
+  Tile r;
+  r.nt = (int)(t % p.n_tiles);
+  t /= p.n_tiles;
+  r.v0 = (int)(t % p.v_tiles) * 8;
+  t /= p.v_tiles;
+  r.u0 = (int)(t % p.u_tiles) * 16 * p.MH;
+  t /= p.u_tiles;
+  r.ow = (int)(t % p.OW);
+  r.b = (int)(t / p.OW);
+  return r;
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t *>(&h);
+}
+__device__ __forceinline__ float bf16_round(float a) {
+  return __bfloat162float(__float2bfloat16_rn(a));
+}
+__device__ __forceinline__ uint32_t to_tf32(float a) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(a));
+  return r;
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) {
+  constexpr int EPC = (KIND == K_TF32) ? 4 : 8;  // channels per 16-byte chunk
+  constexpr int PARTS = (KIND == K_BF16X3) ? 2 : 1;
+  extern __shared__ __align__(1024) uint8_t smem[];
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint8_t *halo = smem;
+  uint8_t *bring = smem + (size_t)p.NH * PARTS * p.halo_bytes;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(bring + (size_t)p.NB * PARTS * p.b_bytes);
+  uint64_t *halo_full = bars;
+  uint64_t *halo_empty = halo_full + p.NH;
+  uint64_t *b_full = halo_empty + p.NH;
+  uint64_t *b_empty = b_full + p.NB;
+  uint64_t *acc_full = b_empty + p.NB;
+  uint64_t *acc_empty = acc_full + 2;
+  uint64_t *drain = acc_empty + 2;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(drain + 1);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < p.NH; ++i) {
+      mbar_init(smem_u32(&halo_full[i]), kProducerThreads);
+      mbar_init(smem_u32(&halo_empty[i]), 1);
+    }
+    for (int i = 0; i < p.NB; ++i) {
+      mbar_init(smem_u32(&b_full[i]), 1);
+      mbar_init(smem_u32(&b_empty[i]), 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(smem_u32(&acc_full[i]), 1);
+      mbar_init(smem_u32(&acc_empty[i]), 128);
+    }
+    mbar_init(smem_u32(drain), 1);
+    *abort_flag = 0;
+    fence_barrier_init();
+  }
+  if (warp == kMmaWarp) {
+    tmem_alloc(smem_u32(tmem_slot), p.tmem_cols);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+
+  if (warp < kProducerWarps) {
+    // ===================== halo producers =====================
+    const int ptid = threadIdx.x;
+    const int nchunks = p.HP * p.NCH;
+    long long k = 0;  // halo stage counter
+    for (long long t = blockIdx.x; t < p.total_tiles; t += gridDim.x) {
+      const Tile tl = decode_tile(p, t);
+      for (int cb = 0; cb < p.NCB; ++cb, ++k) {
+        const int hs = (int)(k % p.NH);
+        const uint32_t ph = (uint32_t)((k / p.NH) & 1);
+        if (!wait_bar(smem_u32(&halo_empty[hs]), ph ^ 1, abort_flag, p.status)) goto done;
+        uint8_t *dst = halo + (size_t)hs * PARTS * p.halo_bytes;
+        const int cbase = cb * p.CPB;
+        for (int idx0 = ptid; idx0 < nchunks; idx0 += 4 * kProducerThreads) {
+          float v[4][EPC];
+          int off[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int idx = idx0 + q * kProducerThreads;
+#pragma unroll
+            for (int e = 0; e < EPC; ++e) v[q][e] = 0.f;
+            off[q] = -1;
+            if (idx < nchunks) {
+              const int hp = idx / p.NCH, j = idx - hp * p.NCH;
+              off[q] = j * p.PS * 16 + hp * 16;
+              const int hv = hp % p.HV, t2 = hp / p.HV;
+              const int hu = t2 % p.HU, hw = t2 / p.HU;
+              const int iw = tl.ow - p.pw + hw, iu = tl.u0 - p.pu + hu, iv = tl.v0 - p.pv + hv;
+              const int c = cbase + j * EPC;
+              if (iw >= 0 && iw < p.IW && iu >= 0 && iu < p.IU && iv >= 0 && iv < p.IV &&
+                  c < p.Cin) {
+                const float *src = p.x + ((long long)tl.b * p.xsb + iw * p.xsw + iu * p.xsu +
+                                          iv * p.xsv) * p.Cin + c;
+                if (p.vec_in && c + EPC <= p.Cin) {
+#pragma unroll
+                  for (int e = 0; e < EPC; e += 4) {
+                    float4 f = __ldg(reinterpret_cast<const float4 *>(src + e));
+                    v[q][e] = f.x; v[q][e + 1] = f.y; v[q][e + 2] = f.z; v[q][e + 3] = f.w;
+                  }
+                } else {
+#pragma unroll
+                  for (int e = 0; e < EPC; ++e)
+                    if (c + e < p.Cin) v[q][e] = __ldg(src + e);
+                }
+              }
+            }
+          }
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            if (off[q] < 0) continue;
+            uint4 hi;
+            if (KIND == K_TF32) {
+              hi = make_uint4(to_tf32(v[q][0]), to_tf32(v[q][1]), to_tf32(v[q][2]),
+                              to_tf32(v[q][3]));
+            } else {
+              hi = make_uint4(pack_bf16(v[q][0], v[q][1]), pack_bf16(v[q][2], v[q][3]),
+                              pack_bf16(v[q][4], v[q][5]), pack_bf16(v[q][6], v[q][7]));
+            }
+            *reinterpret_cast<uint4 *>(dst + off[q]) = hi;
+            if (KIND == K_BF16X3) {
+              float r[8];
+#pragma unroll
+              for (int e = 0; e < 8; ++e) r[e] = v[q][e] - bf16_round(v[q][e]);
+              uint4 lo = make_uint4(pack_bf16(r[0], r[1]), pack_bf16(r[2], r[3]),
+                                    pack_bf16(r[4], r[5]), pack_bf16(r[6], r[7]));
+              *reinterpret_cast<uint4 *>(dst + p.halo_bytes + off[q]) = lo;
+            }
+          }
+        }
+        fence_proxy_async();
+        mbar_arrive(smem_u32(&halo_full[hs]));
+      }
+    }
+  } else if (warp == kMmaWarp) {
+    // ===================== MMA issuer =====================
+    if (lane == 0) {
+      long long kh = 0, kb = 0;
+      int tc = 0;
+      const uint32_t halo0 = smem_u32(halo), b0 = smem_u32(bring);
+      const uint32_t a_lbo = (uint32_t)p.PS * 16, a_sbo = (uint32_t)p.HV * 16;
+      const uint32_t b_lbo = (uint32_t)p.BN * 16;
+      const int ksteps = p.NCH / 2;
+      for (long long t = blockIdx.x; t < p.total_tiles; t += gridDim.x, ++tc) {
+        const int abuf = tc & 1;
+        const uint32_t aph = (uint32_t)((tc >> 1) & 1);
+        if (!wait_bar(smem_u32(&acc_empty[abuf]), aph ^ 1, abort_flag, p.status)) break;
+        tc_fence_after();
+        const uint32_t d0 = tmem_base + (uint32_t)(abuf * p.MH * p.BN);
+        uint32_t acc = 0;
+        bool ok = true;
+        for (int cb = 0; cb < p.NCB && ok; ++cb, ++kh) {
+          const int hs = (int)(kh % p.NH);
+          if (!wait_bar(smem_u32(&halo_full[hs]), (uint32_t)((kh / p.NH) & 1), abort_flag,
+                        p.status)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t hbase = halo0 + (uint32_t)hs * PARTS * p.halo_bytes;
+          for (int tap = 0; tap < p.T; ++tap, ++kb) {
+            const int bs = (int)(kb % p.NB);
+            if (!wait_bar(smem_u32(&b_full[bs]), (uint32_t)((kb / p.NB) & 1), abort_flag,
+                          p.status)) { ok = false; break; }
+            tc_fence_after();
+            const uint32_t bbase = b0 + (uint32_t)bs * PARTS * p.b_bytes;
+            const int kv = tap % p.KV, ku = (tap / p.KV) % p.KU, kw = tap / (p.KV * p.KU);
+            for (int s = 0; s < ksteps; ++s) {
+              const uint64_t bd = smem_desc(bbase + (uint32_t)(2 * s) * b_lbo, b_lbo, 128);
+              const uint64_t bd_lo =
+                  smem_desc(bbase + p.b_bytes + (uint32_t)(2 * s) * b_lbo, b_lbo, 128);
+              for (int h = 0; h < p.MH; ++h) {
+                const int pix = (kw * p.dw * p.HU + h * 16 + ku * p.du) * p.HV + kv * p.dv;
+                const uint32_t aaddr = hbase + (uint32_t)(2 * s) * a_lbo + (uint32_t)pix * 16;
+                const uint64_t ad = smem_desc(aaddr, a_lbo, a_sbo);
+                const uint32_t d = d0 + (uint32_t)(h * p.BN);
+                if (KIND == K_TF32) {
+                  mma_tf32(d, ad, bd, p.idesc, acc);
+                } else {
+                  mma_bf16(d, ad, bd, p.idesc, acc);
+                  if (KIND == K_BF16X3) {
+                    const uint64_t ad_lo = smem_desc(aaddr + p.halo_bytes, a_lbo, a_sbo);
+                    mma_bf16(d, ad, bd_lo, p.idesc, 1);
+                    mma_bf16(d, ad_lo, bd, p.idesc, 1);
+                  }
+                }
+              }
+              acc = 1;
+            }
+            mma_commit(smem_u32(&b_empty[bs]));
+          }
+          if (!ok) break;
+          mma_commit(smem_u32(&halo_empty[hs]));
+        }
+        if (!ok) break;
+        mma_commit(smem_u32(&acc_full[abuf]));
+      }
+      // Drain: every MMA issued above has completed before TMEM is freed.
+      mma_commit(smem_u32(drain));
+      long long t0 = clock64();
+      while (!mbar_try_wait(smem_u32(drain), 0) && clock64() - t0 < kSpinLimit) {
+      }
+    }
+  } else if (warp == kLoadWarp) {
+    // ===================== B (kernel) loader =====================
+    if (lane == 0) {
+      long long kb = 0;
+      const uint32_t b0 = smem_u32(bring);
+      for (long long t = blockIdx.x; t < p.total_tiles; t += gridDim.x) {
+        const Tile tl = decode_tile(p, t);
+        for (int cb = 0; cb < p.NCB; ++cb)
+          for (int tap = 0; tap < p.T; ++tap, ++kb) {
+            const int bs = (int)(kb % p.NB);
+            if (!wait_bar(smem_u32(&b_empty[bs]), (uint32_t)(((kb / p.NB) & 1) ^ 1), abort_flag,
+                          p.status))
+              goto loader_done;
+            const uint32_t bar = smem_u32(&b_full[bs]);
+            mbar_arrive_expect_tx(bar, PARTS * p.b_bytes);
+            const size_t src = ((size_t)(tl.nt * p.NCB + cb) * p.T + tap) * p.b_bytes;
+            const uint32_t dst = b0 + (uint32_t)bs * PARTS * p.b_bytes;
+            bulk_g2s(dst, p.wt_hi + src, p.b_bytes, bar);
+            if (PARTS == 2) bulk_g2s(dst + p.b_bytes, p.wt_lo + src, p.b_bytes, bar);
+          }
+      }
+    loader_done:
+      // Wait (bounded) for the copies still in flight before the CTA exits.
+      if (*abort_flag) {
+        const long long first = kb > p.NB ? kb - p.NB : 0;
+        for (long long q = first; q < kb; ++q) {
+          long long t0 = clock64();
+          const int bs = (int)(q % p.NB);
+          while (!mbar_try_wait(smem_u32(&b_full[bs]), (uint32_t)((q / p.NB) & 1)) &&
+                 clock64() - t0 < kSpinLimit) {
+          }
+        }
+      }
+    }
+  } else {
+    // ===================== epilogue =====================
+    const int q = warp & 3;  // TMEM lane quadrant this warp may access
+    const int row = q * 32 + lane;
+    const int g = row >> 3, vv = row & 7;
+    int tc = 0;
+    for (long long t = blockIdx.x; t < p.total_tiles; t += gridDim.x, ++tc) {
+      const Tile tl = decode_tile(p, t);
+      const int abuf = tc & 1;
+      if (!wait_bar(smem_u32(&acc_full[abuf]), (uint32_t)((tc >> 1) & 1), abort_flag, p.status))
+        break;
+      tc_fence_after();
+      const int n0 = tl.nt * p.BN;
+      for (int h = 0; h < p.MH; ++h) {
+        const int u = tl.u0 + h * 16 + g, v = tl.v0 + vv;
+        const bool valid = u < p.OU && v < p.OV;
+        float *out = p.y + ((long long)tl.b * p.ysb + (long long)tl.ow * p.ysw +
+                            (long long)u * p.ysu + (long long)v * p.ysv) * p.Cout + n0;
+        const uint32_t tcol = tmem_base + ((uint32_t)(q * 32) << 16) +
+                              (uint32_t)((abuf * p.MH + h) * p.BN);
+        for (int c0 = 0; c0 < p.BN; c0 += 16) {
+          uint32_t r[16];
+          tmem_ld16(tcol + (uint32_t)c0, r);
+          tmem_ld_wait();
+          if (valid) {
+            if (p.vec_out && n0 + c0 + 16 <= p.Cout) {
+#pragma unroll
+              for (int e = 0; e < 16; e += 4)
+                *reinterpret_cast<float4 *>(out + c0 + e) =
+                    make_float4(__uint_as_float(r[e]), __uint_as_float(r[e + 1]),
+                                __uint_as_float(r[e + 2]), __uint_as_float(r[e + 3]));
+            } else {
+#pragma unroll
+              for (int e = 0; e < 16; ++e)
+                if (n0 + c0 + e < p.Cout) out[c0 + e] = __uint_as_float(r[e]);
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(smem_u32(&acc_empty[abuf]));
+    }
+  }
+done:
+  tc_fence_before();
+  __syncthreads();
+  if (warp == kMmaWarp) {
+    tc_fence_after();
+    tmem_dealloc(tmem_base, p.tmem_cols);
+  }
+}
+
+// Re-lay the kernel tensor into B-tile images: [ntile][cblock][tap][chunk j]
+// [n < BN][16 B], element (n, k) with k = cb*CPB + j*EPC + e.  FWD reads
+// W[tap][k][n]; BWDI reads the flipped, channel-exchanged kernel
+// W[T-1-tap][n][k] (kernel layout [tap][Ci][Co]).
+template <int KIND>
+__global__ void prep_weights(const float *__restrict__ w, uint8_t *__restrict__ hi,
+                             uint8_t *__restrict__ lo, int T, int Ci, int Co, int K, int N,
+                             int BN, int CPB, int NCB, int n_tiles, int bwd_input) {
+  constexpr int EPC = (KIND == K_TF32) ? 4 : 8;
+  const int NCH = CPB / EPC;
+  const long long total = (long long)n_tiles * NCB * T * NCH * BN;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    long long r = i;
+    const int n = (int)(r % BN); r /= BN;
+    const int j = (int)(r % NCH); r /= NCH;
+    const int tap = (int)(r % T); r /= T;
+    const int cb = (int)(r % NCB);
+    const int nt = (int)(r / NCB);
+    const int ng = nt * BN + n;
+    float v[EPC];
+#pragma unroll
+    for (int e = 0; e < EPC; ++e) {
+      const int k = cb * CPB + j * EPC + e;
+      float val = 0.f;
+      if (k < K && ng < N) {
+        val = bwd_input ? w[((long long)(T - 1 - tap) * Ci + ng) * Co + k]
+                        : w[((long long)tap * Ci + k) * Co + ng];
+      }
+      v[e] = val;
+    }
+    uint4 h4, l4;
+    if (KIND == K_TF32) {
+      h4 = make_uint4(to_tf32(v[0]), to_tf32(v[1]), to_tf32(v[2]), to_tf32(v[3]));
+    } else {
+      h4 = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]),
+                      pack_bf16(v[6], v[7]));
+      if (KIND == K_BF16X3) {
+        float rr[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) rr[e] = v[e] - bf16_round(v[e]);
+        l4 = make_uint4(pack_bf16(rr[0], rr[1]), pack_bf16(rr[2], rr[3]), pack_bf16(rr[4], rr[5]),
+                        pack_bf16(rr[6], rr[7]));
+      }
+    }
+    // byte offset of (nt, cb, tap) tile, then chunk j, row n
+    const long long tile = ((long long)nt * NCB + cb) * T + tap;
+    const long long off = tile * (long long)NCH * BN * 16 + ((long long)j * BN + n) * 16;
+    *reinterpret_cast<uint4 *>(hi + off) = h4;
+    if (KIND == K_BF16X3) *reinterpret_cast<uint4 *>(lo + off) = l4;
+  }
+}
+
+// A convolution seen as (w, u, v) spatial axes plus channels.
+struct View {
+  int B, IW, IU, IV, OW, OU, OV, KW, KU, KV, dw, du, dv, pw, pu, pv;
+  long long xsb, xsw, xsu, xsv, ysb, ysw, ysu, ysv;
+  int Cin, Cout;
+};
+
+// Map Owl's (cols, rows, dpts) onto (w, u, v): the 8-wide core-matrix axis v
+// is the innermost non-trivial spatial axis.
+View make_view(const ConvGeom &g, bool bwd_input) {
+  // "in" = the array the conv reads, "out" = the array it writes.
+  const long long iC = bwd_input ? g.OC : g.IC, iR = bwd_input ? g.OR : g.IR,
+                  iD = bwd_input ? g.OD : g.ID;
+  const long long oC = bwd_input ? g.IC : g.OC, oR = bwd_input ? g.IR : g.OR,
+                  oD = bwd_input ? g.ID : g.OD;
+  auto pad = [](long long k, int d, int p, bool bi) {
+    return bi ? (int)((k - 1) * d - p) : p;
+  };
+  View v;
+  v.B = (int)g.B;
+  v.Cin = (int)(bwd_input ? g.Co : g.Ci);
+  v.Cout = (int)(bwd_input ? g.Ci : g.Co);
+  const bool flat = (iD == 1 && oD == 1 && g.KD == 1);
+  if (flat) {
+    v.IW = 1; v.IU = (int)iC; v.IV = (int)iR;
+    v.OW = 1; v.OU = (int)oC; v.OV = (int)oR;
+    v.KW = 1; v.KU = (int)g.KC; v.KV = (int)g.KR;
+    v.dw = 1; v.du = g.dc; v.dv = g.dr;
+    v.pw = 0; v.pu = pad(g.KC, g.dc, g.pc, bwd_input); v.pv = pad(g.KR, g.dr, g.pr, bwd_input);
+    v.xsw = 1; v.xsu = iR; v.xsv = 1;
+    v.ysw = 1; v.ysu = oR; v.ysv = 1;
+  } else {
+    v.IW = (int)iC; v.IU = (int)iR; v.IV = (int)iD;
+    v.OW = (int)oC; v.OU = (int)oR; v.OV = (int)oD;
+    v.KW = (int)g.KC; v.KU = (int)g.KR; v.KV = (int)g.KD;
+    v.dw = g.dc; v.du = g.dr; v.dv = g.dd;
+    v.pw = pad(g.KC, g.dc, g.pc, bwd_input); v.pu = pad(g.KR, g.dr, g.pr, bwd_input);
+    v.pv = pad(g.KD, g.dd, g.pd, bwd_input);
+    v.xsw = iR * iD; v.xsu = iD; v.xsv = 1;
+    v.ysw = oR * oD; v.ysu = oD; v.ysv = 1;
+  }
+  v.xsb = iC * iR * iD;
+  v.ysb = oC * oR * oD;
+  return v;
+}
+
+int num_sms() {
+  static int n[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (n[dev] == 0) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    n[dev] = v > 0 ? v : 148;
+  }
+  return n[dev];
+}
+
+int *status_ptr() {
+  static int *p[64] = {nullptr};
+  static std::mutex mu;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!p[dev]) {
+    void *q = nullptr;
+    if (cudaGetSymbolAddress(&q, g_tc_status) != cudaSuccess) return nullptr;
+    p[dev] = static_cast<int *>(q);
+  }
+  return p[dev];
+}
+
+// Choose tile and pipeline sizes; false if no configuration fits.
+bool plan(TcParams &p, const View &v, int kind) {
+  const int EB = (kind == K_TF32) ? 4 : 2;
+  const int parts = (kind == K_BF16X3) ? 2 : 1;
+  p.CB = std::min(128, (int)((v.Cin * EB + 31) / 32 * 32));
+  p.CPB = p.CB / EB;
+  p.NCH = p.CB / 16;
+  p.NCB = (v.Cin + p.CPB - 1) / p.CPB;
+  p.BN = std::min(128, (v.Cout + 15) / 16 * 16);
+  p.n_tiles = (v.Cout + p.BN - 1) / p.BN;
+  p.T = v.KW * v.KU * v.KV;
+  p.b_bytes = (unsigned)(p.BN * p.CB);
+  p.NH = 2;
+  for (int mh = (v.OU > 16 ? 2 : 1); mh >= 1; --mh) {
+    p.MH = mh;
+    p.HW = (v.KW - 1) * v.dw + 1;
+    p.HU = 16 * mh + (v.KU - 1) * v.du;
+    p.HV = 8 + (v.KV - 1) * v.dv;
+    p.HP = p.HW * p.HU * p.HV;
+    p.PS = p.HP + (((1 - p.HP) % 8) + 8) % 8;  // plane stride = 1 (mod 8) pixels
+    if (p.PS >= 16384 || p.HV >= 16384) continue;
+    p.halo_bytes = (unsigned)p.PS * 16u * (unsigned)p.NCH;
+    long long fixed = (long long)p.NH * parts * p.halo_bytes + 512;
+    long long room = kSmemMax - fixed;
+    int nb = (int)std::min<long long>(8, room / ((long long)parts * p.b_bytes));
+    if (nb < 2) continue;
+    p.NB = nb;
+    p.tmem_cols = 32;
+    while (p.tmem_cols < (unsigned)(2 * p.MH * p.BN)) p.tmem_cols <<= 1;
+    if (p.tmem_cols > 512) continue;
+    return true;
+  }
+  return false;
+}
+
+template <int KIND>
+int launch(const TcParams &p, size_t smem, cudaStream_t s) {
+  static bool attr_set[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+    OWL_CUDA(cudaFuncSetAttribute(conv_tc_kernel<KIND>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemMax));
+    attr_set[dev] = true;
+  }
+  int grid = (int)std::min<long long>(p.total_tiles, num_sms());
+  conv_tc_kernel<KIND><<<grid, kThreads, smem, s>>>(p);
+  OWL_CHECK_LAUNCH("conv_tc_kernel");
+  return kOk;
+}
+
+int run(int prec, const ConvGeom &g, bool bwd_input, const float *x, const float *w, float *y,
+        cudaStream_t s) {
+  if (g.sc != 1 || g.sr != 1 || g.sd != 1) return kErrUnsupported;
+  const int kind = prec == OWLGPU_PREC_TF32 ? K_TF32 : (prec == OWLGPU_PREC_BF16X3 ? K_BF16X3 : K_BF16);
+  const View v = make_view(g, bwd_input);
+  if (v.OW * (long long)v.OU * v.OV * v.B == 0 || v.Cout == 0) return kOk;
+  TcParams p{};
+  if (v.Cin == 0 || !plan(p, v, kind)) return kErrUnsupported;
+  p.x = x; p.y = y;
+  p.B = v.B; p.IW = v.IW; p.IU = v.IU; p.IV = v.IV; p.OW = v.OW; p.OU = v.OU; p.OV = v.OV;
+  p.KW = v.KW; p.KU = v.KU; p.KV = v.KV; p.dw = v.dw; p.du = v.du; p.dv = v.dv;
+  p.pw = v.pw; p.pu = v.pu; p.pv = v.pv;
+  p.xsb = v.xsb; p.xsw = v.xsw; p.xsu = v.xsu; p.xsv = v.xsv;
+  p.ysb = v.ysb; p.ysw = v.ysw; p.ysu = v.ysu; p.ysv = v.ysv;
+  p.Cin = v.Cin; p.Cout = v.Cout;
+  p.u_tiles = (v.OU + 16 * p.MH - 1) / (16 * p.MH);
+  p.v_tiles = (v.OV + 7) / 8;
+  p.total_tiles = (long long)v.B * v.OW * p.u_tiles * p.v_tiles * p.n_tiles;
+  p.idesc = instr_desc(kind == K_TF32 ? 2u : 1u, (uint32_t)p.BN);
+  p.vec_in = ((uintptr_t)x % 16 == 0) && (v.Cin % 4 == 0);
+  p.vec_out = ((uintptr_t)y % 16 == 0) && (v.Cout % 4 == 0);
+  p.status = status_ptr();
+  if (!p.status) {
+    set_error("conv_tc: cannot locate device status word");
+    return kErrCuda;
+  }
+  const int parts = kind == K_BF16X3 ? 2 : 1;
+  const size_t wt_bytes = (size_t)p.n_tiles * p.NCB * p.T * p.b_bytes;
+  void *wt = nullptr;
+  int rc = scratch_alloc(&wt, wt_bytes * parts, s);
+  if (rc) return rc;
+  p.wt_hi = (const uint8_t *)wt;
+  p.wt_lo = parts == 2 ? (const uint8_t *)wt + wt_bytes : nullptr;
+  {
+    const long long n = (long long)p.n_tiles * p.NCB * p.T * p.NCH * p.BN;
+    const int blocks = (int)std::min<long long>((n + 255) / 256, 4096);
+    const int K = v.Cin, N = v.Cout;
+    const int Ci = (int)g.Ci, Co = (int)g.Co;
+    if (kind == K_TF32)
+      prep_weights<K_TF32><<<blocks, 256, 0, s>>>(w, (uint8_t *)wt, nullptr, p.T, Ci, Co, K, N,
+                                                  p.BN, p.CPB, p.NCB, p.n_tiles, bwd_input);
+    else if (kind == K_BF16X3)
+      prep_weights<K_BF16X3><<<blocks, 256, 0, s>>>(w, (uint8_t *)wt, (uint8_t *)wt + wt_bytes,
+                                                    p.T, Ci, Co, K, N, p.BN, p.CPB, p.NCB,
+                                                    p.n_tiles, bwd_input);
+    else
+      prep_weights<K_BF16><<<blocks, 256, 0, s>>>(w, (uint8_t *)wt, nullptr, p.T, Ci, Co, K, N,
+                                                  p.BN, p.CPB, p.NCB, p.n_tiles, bwd_input);
+    cudaError_t e = cudaGetLastError();
+    note_launch();
+    if (e != cudaSuccess) {
+      scratch_free(wt, s);
+      return cuda_fail(e, "prep_weights");
+    }
+  }
+  const size_t smem = (size_t)p.NH * parts * p.halo_bytes + (size_t)p.NB * parts * p.b_bytes +
+                      (2 * p.NH + 2 * p.NB + 5) * 8 + 16;
+  if (kind == K_TF32) rc = launch<K_TF32>(p, smem, s);
+  else if (kind == K_BF16X3) rc = launch<K_BF16X3>(p, smem, s);
+  else rc = launch<K_BF16>(p, smem, s);
+  scratch_free(wt, s);
+  return rc;
+}
+
+}  // namespace
+
+int tc_conv_fwd(int prec, const ConvGeom &g, const float *x, const float *w, float *y,
+                cudaStream_t s) {
+  return run(prec, g, false, x, w, y, s);
+}
+
+int tc_conv_bwd_input(int prec, const ConvGeom &g, float *dx, const float *w, const float *dy,
+                      cudaStream_t s) {
+  return run(prec, g, true, dy, w, dx, s);
+}
+
+int tc_conv_bwd_kernel(int, const ConvGeom &, const float *, float *, const float *,
+                       cudaStream_t) {
   return kErrUnsupported;
 }
-int tc_conv_bwd_input(int, const ConvGeom &, float *, const float *, const float *, cudaStream_t) {
-  return kErrUnsupported;
+
+int tc_read_status(int *out, cudaStream_t s) {
+  int *p = status_ptr();
+  if (!p) return kErrCuda;
+  OWL_CUDA(cudaMemcpyAsync(out, p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  OWL_CUDA(cudaStreamSynchronize(s));
+  if (*out) OWL_CUDA(cudaMemsetAsync(p, 0, sizeof(int), s));
+  return kOk;
 }
-int tc_conv_bwd_kernel(int, const ConvGeom &, const float *, float *, const float *, cudaStream_t) {
-  return kErrUnsupported;
-}
+
 }  // namespace owlgpu
