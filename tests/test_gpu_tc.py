@@ -3,7 +3,10 @@ against the float64 oracle (Owl's D path restated).
 
 Tolerances (error = max|gpu - f64| / max|f64|), written here as the
 acceptance bar for each precision:
-  BF16   <= 1e-2    TF32 <= 5e-3    BF16X3 (hi*hi + hi*lo + lo*hi) <= 1e-5
+  BF16   <= 1e-2    TF32 <= 5e-3    BF16X3 (hi*hi + hi*lo + lo*hi) <= 2e-5
+BF16X3 drops lo*lo and the bf16 rounding of lo itself, about 3 * 2^-18
+relative per product; with random signs the worst element of a K = 3250
+reduction (5x5x130 taps) lands near 1.4e-5 of max|y|, hence 2e-5 here.
 Every case also asserts that the tensor-core kernel (not the CUDA-core
 fallback) ran, through owlgpu_last_conv_path().
 """
@@ -14,7 +17,7 @@ import pytest
 from gpu_util import from_dev, rel, to_dev
 
 pytestmark = pytest.mark.gpu
-TOL = {"bf16": 1e-2, "tf32": 5e-3, "bf16x3": 1e-5}
+TOL = {"bf16": 1e-2, "tf32": 5e-3, "bf16x3": 2e-5}
 SAME, VALID = "SAME", "VALID"
 
 CASES2D = [
