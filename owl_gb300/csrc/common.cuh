@@ -125,6 +125,7 @@ int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, c
 
 // Read (and clear) the tensor-core kernels' device error word on stream s.
 int tc_read_status(int *out, cudaStream_t s);
+int tc_wgrad_read_status(int *out, cudaStream_t s);
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 

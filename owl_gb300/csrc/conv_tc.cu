@@ -640,17 +640,16 @@ int tc_conv_bwd_input(int prec, const ConvGeom &g, float *dx, const float *w, co
   return run(prec, g, true, dy, w, dx, s);
 }
 
-int tc_conv_bwd_kernel(int, const ConvGeom &, const float *, float *, const float *,
-                       cudaStream_t) {
-  return kErrUnsupported;
-}
-
 int tc_read_status(int *out, cudaStream_t s) {
   int *p = status_ptr();
   if (!p) return kErrCuda;
   OWL_CUDA(cudaMemcpyAsync(out, p, sizeof(int), cudaMemcpyDeviceToHost, s));
   OWL_CUDA(cudaStreamSynchronize(s));
   if (*out) OWL_CUDA(cudaMemsetAsync(p, 0, sizeof(int), s));
+  int wg = 0;
+  int rc = tc_wgrad_read_status(&wg, s);
+  if (rc) return rc;
+  *out |= wg;
   return kOk;
 }
 

@@ -1,0 +1,511 @@
+// conv_tc_wgrad.cu -- tcgen05 backward-kernel (weight gradient) for float32
+// data in BF16, TF32 or split-BF16 precision, stride 1, any dilation, 2-D/3-D.
+//
+//   dW[t][ci][co] = sum over output pixels p of X[p + off(t)][ci] * dY[p][co]
+//
+// Per tap this is a GEMM with M = ci (128 per MMA), N = co (BN), and the
+// reduction K running over output pixels.  Both operands are staged from the
+// float32 activations by producer warps in the same [16-byte channel chunk]
+// [pixel][16 B] layout as the forward kernel's halo.  Read MN-major, 8
+// consecutive pixels x 8 channels of that layout form one core matrix, so
+// every tap of a tap group reads the same X halo through a shifted descriptor
+// and all of them share one staged dY tile.
+//
+// Work split: a CTA owns (tap group, ci block, co block, pixel range).  It
+// accumulates the group's taps in TMEM (TG * BN columns) over all the pixel
+// tiles of its range, then writes the partial dW of its range.  A second
+// kernel sums the ranges in a fixed order, so the result is deterministic.
+// CTAs that share a pixel range are launched next to each other, so the
+// activations they re-read come from L2.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+
+#include "../../include/owlgpu.h"
+#include "common.cuh"
+#include "tc_ptx.cuh"
+
+namespace owlgpu {
+namespace {
+
+using namespace ptx;
+
+constexpr int kProducerWarps = 8;
+constexpr int kMmaWarp = kProducerWarps;
+constexpr int kThreads = (kProducerWarps + 1 + 4) * 32;  // + MMA warp + 4 epilogue warps
+constexpr int kProducerThreads = kProducerWarps * 32;
+constexpr int kSmemMax = 232448;
+constexpr long long kSpinLimit = 4000000000LL;
+constexpr int kTilePix = 128;  // output pixels per reduction tile (16 u x 8 v)
+
+enum Kind { K_BF16 = 0, K_TF32 = 1, K_BF16X3 = 2 };
+
+struct WgParams {
+  const float *x, *dy;
+  float *out;
+  int *status;
+  int B, IW, IU, IV, OW, OU, OV, KW, KU, KV, dw, du, dv, pw, pu, pv;
+  long long xsb, xsw, xsu, xsv, ysb, ysw, ysu, ysv;
+  int Ci, Co, T, TG, n_tg, BN, n_nb, n_mb, R;
+  int u_tiles, v_tiles;
+  long long total_tiles, tiles_per_range;
+  int PS;                 // X halo plane stride in pixels (max over groups)
+  unsigned x_bytes, y_bytes;  // per stage, per precision part
+  int NS;
+  unsigned idesc, tmem_cols;
+  int vec_x, vec_y;
+};
+
+__device__ int g_tc_status_wg;
+
+__device__ __forceinline__ bool wait_bar(uint32_t bar, uint32_t parity, volatile int *abort_flag,
+                                         int *status) {
+  if (mbar_try_wait(bar, parity)) return true;
+  long long t0 = clock64();
+  while (true) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*abort_flag) return false;
+    if (clock64() - t0 > kSpinLimit) {
+      *abort_flag = 1;
+      atomicExch(status, 1);
+      return false;
+    }
+  }
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t *>(&h);
+}
+__device__ __forceinline__ float bf16_round(float a) {
+  return __bfloat162float(__float2bfloat16_rn(a));
+}
+__device__ __forceinline__ uint32_t to_tf32(float a) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(a));
+  return r;
+}
+
+// Convert EPC floats and store one 16-byte chunk (plus its lo part).
+template <int KIND, int EPC>
+__device__ __forceinline__ void put_chunk(uint8_t *dst, uint32_t lo_off, const float (&v)[EPC]) {
+  uint4 hi;
+  if (KIND == K_TF32) {
+    hi = make_uint4(to_tf32(v[0]), to_tf32(v[1]), to_tf32(v[2]), to_tf32(v[3]));
+  } else {
+    hi = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]),
+                    pack_bf16(v[6], v[7]));
+  }
+  *reinterpret_cast<uint4 *>(dst) = hi;
+  if (KIND == K_BF16X3) {
+    float r[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) r[e] = v[e] - bf16_round(v[e]);
+    *reinterpret_cast<uint4 *>(dst + lo_off) = make_uint4(
+        pack_bf16(r[0], r[1]), pack_bf16(r[2], r[3]), pack_bf16(r[4], r[5]), pack_bf16(r[6], r[7]));
+  }
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p) {
+  constexpr int EB = (KIND == K_TF32) ? 4 : 2;
+  constexpr int EPC = 16 / EB;
+  constexpr int PARTS = (KIND == K_BF16X3) ? 2 : 1;
+  constexpr int XPL = 128 * EB / 16;  // planes for 128 input channels
+  constexpr int KSTEP_PIX = 32 / EB;  // pixels per MMA (K = 16 bf16 / 8 tf32)
+  extern __shared__ __align__(1024) uint8_t smem[];
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int YPL = p.BN * EB / 16;
+
+  // ---- work unit of this CTA ----
+  long long u = blockIdx.x;
+  const int tg = (int)(u % p.n_tg); u /= p.n_tg;
+  const int nb = (int)(u % p.n_nb); u /= p.n_nb;
+  const int mb = (int)(u % p.n_mb);
+  const int r = (int)(u / p.n_mb);
+  const long long t_begin = (long long)r * p.tiles_per_range;
+  const long long t_end = min(p.total_tiles, t_begin + p.tiles_per_range);
+  const int tap0 = tg * p.TG;
+  const int ntap = min(p.TG, p.T - tap0);
+
+  // bounding box of this group's tap offsets -> halo extents
+  int minw = 1 << 30, minu = 1 << 30, minv = 1 << 30, maxw = -1, maxu = -1, maxv = -1;
+  for (int i = 0; i < ntap; ++i) {
+    const int t = tap0 + i;
+    const int kv = t % p.KV, ku = (t / p.KV) % p.KU, kw = t / (p.KV * p.KU);
+    minw = min(minw, kw * p.dw); maxw = max(maxw, kw * p.dw);
+    minu = min(minu, ku * p.du); maxu = max(maxu, ku * p.du);
+    minv = min(minv, kv * p.dv); maxv = max(maxv, kv * p.dv);
+  }
+  const int HW = maxw - minw + 1, HU = 16 + maxu - minu, HV = 8 + maxv - minv;
+  const int HP = HW * HU * HV;
+
+  uint8_t *xs = smem;
+  uint8_t *ys = smem + (size_t)p.NS * PARTS * p.x_bytes;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(ys + (size_t)p.NS * PARTS * p.y_bytes);
+  uint64_t *full = bars;
+  uint64_t *empty = full + p.NS;
+  uint64_t *acc_full = empty + p.NS;
+  uint64_t *drain = acc_full + 1;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(drain + 1);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < p.NS; ++i) {
+      mbar_init(smem_u32(&full[i]), kProducerThreads);
+      mbar_init(smem_u32(&empty[i]), 1);
+    }
+    mbar_init(smem_u32(acc_full), 1);
+    mbar_init(smem_u32(drain), 1);
+    *abort_flag = 0;
+    fence_barrier_init();
+  }
+  if (warp == kMmaWarp) {
+    tmem_alloc(smem_u32(tmem_slot), p.tmem_cols);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+
+  if (warp < kProducerWarps) {
+    // ===================== producers: X halo + dY tile =====================
+    const int ptid = threadIdx.x;
+    long long k = 0;
+    for (long long t = t_begin; t < t_end; ++t, ++k) {
+      long long q = t;
+      const int v0 = (int)(q % p.v_tiles) * 8; q /= p.v_tiles;
+      const int u0 = (int)(q % p.u_tiles) * 16; q /= p.u_tiles;
+      const int ow = (int)(q % p.OW);
+      const int b = (int)(q / p.OW);
+      const int st = (int)(k % p.NS);
+      if (!wait_bar(smem_u32(&empty[st]), (uint32_t)(((k / p.NS) & 1) ^ 1), abort_flag,
+                    p.status))
+        goto done;
+      uint8_t *xd = xs + (size_t)st * PARTS * p.x_bytes;
+      uint8_t *yd = ys + (size_t)st * PARTS * p.y_bytes;
+      // X halo: HP pixels x 128 channels of ci block mb
+      const int xchunks = HP * XPL;
+      for (int idx = ptid; idx < xchunks; idx += kProducerThreads) {
+        const int hp = idx / XPL, j = idx - hp * XPL;
+        const int hv = hp % HV, t2 = hp / HV;
+        const int hu = t2 % HU, hw = t2 / HU;
+        const int iw = ow - p.pw + minw + hw, iu = u0 - p.pu + minu + hu,
+                  iv = v0 - p.pv + minv + hv;
+        const int c = mb * 128 + j * EPC;
+        float v[EPC];
+#pragma unroll
+        for (int e = 0; e < EPC; ++e) v[e] = 0.f;
+        if (iw >= 0 && iw < p.IW && iu >= 0 && iu < p.IU && iv >= 0 && iv < p.IV && c < p.Ci) {
+          const float *src =
+              p.x + ((long long)b * p.xsb + iw * p.xsw + iu * p.xsu + iv * p.xsv) * p.Ci + c;
+          if (p.vec_x && c + EPC <= p.Ci) {
+#pragma unroll
+            for (int e = 0; e < EPC; e += 4) {
+              float4 f = __ldg(reinterpret_cast<const float4 *>(src + e));
+              v[e] = f.x; v[e + 1] = f.y; v[e + 2] = f.z; v[e + 3] = f.w;
+            }
+          } else {
+#pragma unroll
+            for (int e = 0; e < EPC; ++e)
+              if (c + e < p.Ci) v[e] = __ldg(src + e);
+          }
+        }
+        put_chunk<KIND, EPC>(xd + (size_t)j * p.PS * 16 + (size_t)hp * 16, p.x_bytes, v);
+      }
+      // dY tile: 128 output pixels x BN channels of co block nb
+      const int ychunks = kTilePix * YPL;
+      for (int idx = ptid; idx < ychunks; idx += kProducerThreads) {
+        const int kp = idx / YPL, j = idx - kp * YPL;
+        const int ou = u0 + (kp >> 3), ov = v0 + (kp & 7);
+        const int c = nb * p.BN + j * EPC;
+        float v[EPC];
+#pragma unroll
+        for (int e = 0; e < EPC; ++e) v[e] = 0.f;
+        if (ou < p.OU && ov < p.OV && c < p.Co) {
+          const float *src =
+              p.dy + ((long long)b * p.ysb + ow * p.ysw + ou * p.ysu + ov * p.ysv) * p.Co + c;
+          if (p.vec_y && c + EPC <= p.Co) {
+#pragma unroll
+            for (int e = 0; e < EPC; e += 4) {
+              float4 f = __ldg(reinterpret_cast<const float4 *>(src + e));
+              v[e] = f.x; v[e + 1] = f.y; v[e + 2] = f.z; v[e + 3] = f.w;
+            }
+          } else {
+#pragma unroll
+            for (int e = 0; e < EPC; ++e)
+              if (c + e < p.Co) v[e] = __ldg(src + e);
+          }
+        }
+        put_chunk<KIND, EPC>(yd + (size_t)j * kTilePix * 16 + (size_t)kp * 16, p.y_bytes, v);
+      }
+      fence_proxy_async();
+      mbar_arrive(smem_u32(&full[st]));
+    }
+  } else if (warp == kMmaWarp) {
+    // ===================== MMA issuer =====================
+    if (lane == 0) {
+      const uint32_t x0 = smem_u32(xs), y0 = smem_u32(ys);
+      const uint32_t a_lbo = (uint32_t)HV * 16, a_sbo = (uint32_t)p.PS * 16;
+      const uint32_t b_lbo = 128, b_sbo = kTilePix * 16;
+      long long k = 0;
+      uint32_t acc = 0;
+      bool ok = true;
+      for (long long t = t_begin; t < t_end; ++t, ++k) {
+        const int st = (int)(k % p.NS);
+        if (!wait_bar(smem_u32(&full[st]), (uint32_t)((k / p.NS) & 1), abort_flag, p.status)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t xb = x0 + (uint32_t)st * PARTS * p.x_bytes;
+        const uint32_t yb = y0 + (uint32_t)st * PARTS * p.y_bytes;
+        for (int s = 0; s < kTilePix / KSTEP_PIX; ++s) {
+          const int g0 = (s * KSTEP_PIX) >> 3;  // first u-group of this K step
+          const uint32_t baddr = yb + (uint32_t)(s * KSTEP_PIX) * 16;
+          const uint64_t bd = smem_desc(baddr, b_lbo, b_sbo);
+          const uint64_t bd_lo = smem_desc(baddr + p.y_bytes, b_lbo, b_sbo);
+          for (int i = 0; i < ntap; ++i) {
+            const int tt = tap0 + i;
+            const int kv = tt % p.KV, ku = (tt / p.KV) % p.KU, kw = tt / (p.KV * p.KU);
+            const int pix = ((kw * p.dw - minw) * HU + (ku * p.du - minu) + g0) * HV +
+                            (kv * p.dv - minv);
+            const uint32_t aaddr = xb + (uint32_t)pix * 16;
+            const uint64_t ad = smem_desc(aaddr, a_lbo, a_sbo);
+            const uint32_t d = tmem_base + (uint32_t)(i * p.BN);
+            if (KIND == K_TF32) {
+              mma_tf32(d, ad, bd, p.idesc, acc);
+            } else {
+              mma_bf16(d, ad, bd, p.idesc, acc);
+              if (KIND == K_BF16X3) {
+                mma_bf16(d, ad, bd_lo, p.idesc, 1);
+                mma_bf16(d, smem_desc(aaddr + p.x_bytes, a_lbo, a_sbo), bd, p.idesc, 1);
+              }
+            }
+          }
+          acc = 1;
+        }
+        mma_commit(smem_u32(&empty[st]));
+      }
+      if (ok) mma_commit(smem_u32(acc_full));
+      mma_commit(smem_u32(drain));
+      long long t0 = clock64();
+      while (!mbar_try_wait(smem_u32(drain), 0) && clock64() - t0 < kSpinLimit) {
+      }
+    }
+  } else {
+    // ===================== epilogue: TMEM -> partial dW =====================
+    const int q = warp & 3;
+    const int ci = mb * 128 + q * 32 + lane;
+    if (wait_bar(smem_u32(acc_full), 0, abort_flag, p.status)) {
+      tc_fence_after();
+      for (int i = 0; i < ntap; ++i) {
+        const int tt = tap0 + i;
+        float *out = p.out + (((long long)r * p.T + tt) * p.Ci + ci) * p.Co + nb * p.BN;
+        const uint32_t tcol = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(i * p.BN);
+        for (int c0 = 0; c0 < p.BN; c0 += 16) {
+          uint32_t rr[16];
+          tmem_ld16(tcol + (uint32_t)c0, rr);
+          tmem_ld_wait();
+          if (ci < p.Ci) {
+            const int n0 = nb * p.BN + c0;
+            if (p.vec_y && n0 + 16 <= p.Co && ((uintptr_t)(out + c0) % 16 == 0)) {
+#pragma unroll
+              for (int e = 0; e < 16; e += 4)
+                *reinterpret_cast<float4 *>(out + c0 + e) =
+                    make_float4(__uint_as_float(rr[e]), __uint_as_float(rr[e + 1]),
+                                __uint_as_float(rr[e + 2]), __uint_as_float(rr[e + 3]));
+            } else {
+#pragma unroll
+              for (int e = 0; e < 16; ++e)
+                if (n0 + e < p.Co) out[c0 + e] = __uint_as_float(rr[e]);
+            }
+          }
+        }
+      }
+      tc_fence_before();
+    }
+  }
+done:
+  tc_fence_before();
+  __syncthreads();
+  if (warp == kMmaWarp) {
+    tc_fence_after();
+    tmem_dealloc(tmem_base, p.tmem_cols);
+  }
+}
+
+// out[i] = sum_r part[r][i] in increasing r (deterministic).
+__global__ void wgrad_reduce(const float *__restrict__ part, float *__restrict__ out, long long n,
+                             int R) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    float s = part[i];
+    for (int r = 1; r < R; ++r) s += part[(long long)r * n + i];
+    out[i] = s;
+  }
+}
+
+int sm_count() {
+  int dev = 0, n = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  return n > 0 ? n : 148;
+}
+
+int *status_word() {
+  static int *p[64] = {nullptr};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return nullptr;
+  if (!p[dev]) {
+    void *q = nullptr;
+    if (cudaGetSymbolAddress(&q, g_tc_status_wg) != cudaSuccess) return nullptr;
+    p[dev] = static_cast<int *>(q);
+  }
+  return p[dev];
+}
+
+template <int KIND>
+int launch(const WgParams &p, size_t smem, int grid, cudaStream_t s) {
+  static bool attr[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !attr[dev]) {
+    OWL_CUDA(cudaFuncSetAttribute(wgrad_tc_kernel<KIND>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemMax));
+    attr[dev] = true;
+  }
+  wgrad_tc_kernel<KIND><<<grid, kThreads, smem, s>>>(p);
+  OWL_CHECK_LAUNCH("wgrad_tc_kernel");
+  return kOk;
+}
+
+}  // namespace
+
+int tc_wgrad_read_status(int *out, cudaStream_t s) {
+  int *p = status_word();
+  if (!p) return kErrCuda;
+  OWL_CUDA(cudaMemcpyAsync(out, p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  OWL_CUDA(cudaStreamSynchronize(s));
+  if (*out) OWL_CUDA(cudaMemsetAsync(p, 0, sizeof(int), s));
+  return kOk;
+}
+
+int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, const float *dy,
+                       cudaStream_t s) {
+  if (g.sc != 1 || g.sr != 1 || g.sd != 1) return kErrUnsupported;
+  const int kind = prec == OWLGPU_PREC_TF32 ? K_TF32 : (prec == OWLGPU_PREC_BF16X3 ? K_BF16X3 : K_BF16);
+  const int EB = kind == K_TF32 ? 4 : 2;
+  const int parts = kind == K_BF16X3 ? 2 : 1;
+  if (g.Ci == 0 || g.Co == 0 || g.taps() == 0) return kErrUnsupported;
+  if (g.out_pixels() == 0) return kErrUnsupported;
+  WgParams p{};
+  p.x = x; p.dy = dy;
+  p.B = (int)g.B;
+  p.Ci = (int)g.Ci; p.Co = (int)g.Co;
+  const bool flat = (g.ID == 1 && g.OD == 1 && g.KD == 1);
+  if (flat) {
+    p.IW = 1; p.IU = (int)g.IC; p.IV = (int)g.IR; p.OW = 1; p.OU = (int)g.OC; p.OV = (int)g.OR;
+    p.KW = 1; p.KU = (int)g.KC; p.KV = (int)g.KR; p.dw = 1; p.du = g.dc; p.dv = g.dr;
+    p.pw = 0; p.pu = g.pc; p.pv = g.pr;
+    p.xsw = 1; p.xsu = g.IR; p.xsv = 1; p.ysw = 1; p.ysu = g.OR; p.ysv = 1;
+  } else {
+    p.IW = (int)g.IC; p.IU = (int)g.IR; p.IV = (int)g.ID;
+    p.OW = (int)g.OC; p.OU = (int)g.OR; p.OV = (int)g.OD;
+    p.KW = (int)g.KC; p.KU = (int)g.KR; p.KV = (int)g.KD;
+    p.dw = g.dc; p.du = g.dr; p.dv = g.dd; p.pw = g.pc; p.pu = g.pr; p.pv = g.pd;
+    p.xsw = g.IR * g.ID; p.xsu = g.ID; p.xsv = 1;
+    p.ysw = g.OR * g.OD; p.ysu = g.OD; p.ysv = 1;
+  }
+  p.xsb = g.IC * g.IR * g.ID;
+  p.ysb = g.OC * g.OR * g.OD;
+  p.T = (int)g.taps();
+  p.n_mb = (p.Ci + 127) / 128;
+  p.u_tiles = (p.OU + 15) / 16;
+  p.v_tiles = (p.OV + 7) / 8;
+  p.total_tiles = (long long)p.B * p.OW * p.u_tiles * p.v_tiles;
+
+  // Plan: BN (co block), TG (taps per CTA, TG*BN <= 512 TMEM columns), NS = 2.
+  // Prefer wide co blocks and many taps per CTA; shrink until the two stages
+  // of X halo + dY tile fit in shared memory.
+  bool planned = false;
+  for (int bn : {128, 64, 32, 16}) {
+    p.BN = std::min(bn, (p.Co + 15) / 16 * 16);
+    for (int tg = std::min(p.T, 16); tg >= 1 && !planned; --tg) {
+      if (p.T % tg != 0 || tg * p.BN > 512) continue;
+      p.TG = tg;
+      p.n_tg = p.T / tg;
+      int maxHP = 0;
+      for (int gi = 0; gi < p.n_tg; ++gi) {
+        int mnw = 1 << 30, mnu = 1 << 30, mnv = 1 << 30, mxw = -1, mxu = -1, mxv = -1;
+        for (int i = 0; i < tg; ++i) {
+          const int t = gi * tg + i;
+          const int kv = t % p.KV, ku = (t / p.KV) % p.KU, kw = t / (p.KV * p.KU);
+          mnw = std::min(mnw, kw * p.dw); mxw = std::max(mxw, kw * p.dw);
+          mnu = std::min(mnu, ku * p.du); mxu = std::max(mxu, ku * p.du);
+          mnv = std::min(mnv, kv * p.dv); mxv = std::max(mxv, kv * p.dv);
+        }
+        maxHP = std::max(maxHP, (mxw - mnw + 1) * (16 + mxu - mnu) * (8 + mxv - mnv));
+      }
+      p.PS = maxHP + (((1 - maxHP) % 8) + 8) % 8;
+      if (p.PS >= 16384) continue;
+      p.x_bytes = (unsigned)(128 * EB / 16) * (unsigned)p.PS * 16u;
+      p.y_bytes = (unsigned)(p.BN * EB / 16) * (unsigned)kTilePix * 16u;
+      p.NS = 2;
+      const size_t need = (size_t)p.NS * parts * (p.x_bytes + p.y_bytes) + 256;
+      if (need <= (size_t)kSmemMax) planned = true;
+    }
+    if (planned) break;
+  }
+  if (!planned) return kErrUnsupported;
+  p.n_nb = (p.Co + p.BN - 1) / p.BN;
+  p.tmem_cols = 32;
+  while (p.tmem_cols < (unsigned)(p.TG * p.BN)) p.tmem_cols <<= 1;
+  // pixel ranges: enough CTAs to fill the GPU once
+  const long long units = (long long)p.n_tg * p.n_nb * p.n_mb;
+  const int sms = sm_count();
+  long long R = std::max<long long>(1, sms / std::max<long long>(1, units));
+  R = std::min<long long>(R, p.total_tiles);
+  p.tiles_per_range = (p.total_tiles + R - 1) / R;
+  R = (p.total_tiles + p.tiles_per_range - 1) / p.tiles_per_range;
+  p.R = (int)R;
+  uint32_t idesc = instr_desc(kind == K_TF32 ? 2u : 1u, (uint32_t)p.BN);
+  idesc |= (1u << 15) | (1u << 16);  // A and B MN-major
+  p.idesc = idesc;
+  p.vec_x = ((uintptr_t)x % 16 == 0) && (p.Ci % 4 == 0);
+  p.vec_y = ((uintptr_t)dy % 16 == 0) && (p.Co % 4 == 0);
+  p.status = status_word();
+  if (!p.status) {
+    set_error("wgrad_tc: cannot locate device status word");
+    return kErrCuda;
+  }
+  const long long welems = (long long)p.T * p.Ci * p.Co;
+  float *part = nullptr;
+  if (p.R > 1) {
+    int rc = scratch_alloc((void **)&part, sizeof(float) * (size_t)welems * p.R, s);
+    if (rc) return rc;
+    p.out = part;
+  } else {
+    p.out = dw;
+  }
+  const size_t smem = (size_t)p.NS * parts * (p.x_bytes + p.y_bytes) + (2 * p.NS + 2) * 8 + 16;
+  const int grid = (int)(units * p.R);
+  int rc;
+  if (kind == K_TF32) rc = launch<K_TF32>(p, smem, grid, s);
+  else if (kind == K_BF16X3) rc = launch<K_BF16X3>(p, smem, grid, s);
+  else rc = launch<K_BF16>(p, smem, grid, s);
+  if (rc == kOk && p.R > 1) {
+    const int blocks = (int)std::min<long long>((welems + 255) / 256, 4 * 152);
+    wgrad_reduce<<<blocks, 256, 0, s>>>(part, dw, welems, p.R);
+    cudaError_t e = cudaGetLastError();
+    note_launch();
+    if (e != cudaSuccess) rc = cuda_fail(e, "wgrad_reduce");
+  }
+  if (part) scratch_free(part, s);
+  return rc;
+}
+
+}  // namespace owlgpu

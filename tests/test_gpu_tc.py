@@ -85,6 +85,15 @@ def test_conv2d_tc(gpu_lib, f64_nn, prec, case):
         assert _path() == 1
         dx64 = f64_nn.conv2d_backward_input(x64, w64, [1, 1], dy.astype(np.float64))
     assert rel(dx, dx64) <= TOL[prec]
+    if rate:
+        dw = from_dev(G.dilated_conv2d_backward_kernel(xd, wd, [1, 1], list(rate), dyd))
+        assert _path() == 1
+        dw64 = f64_nn.dilated_conv2d_backward_kernel(x64, w64, [1, 1], list(rate), dy.astype(np.float64))
+    else:
+        dw = from_dev(G.conv2d_backward_kernel(xd, wd, [1, 1], dyd))
+        assert _path() == 1
+        dw64 = f64_nn.conv2d_backward_kernel(x64, w64, [1, 1], dy.astype(np.float64))
+    assert rel(dw, dw64) <= TOL[prec]
 
 
 @pytest.mark.parametrize("prec", ["bf16", "tf32", "bf16x3"])
@@ -114,6 +123,14 @@ def test_conv3d_tc(gpu_lib, f64_nn, prec, case):
         dx = from_dev(G.conv3d_backward_input(xd, wd, st, to_dev(dy)))
         dx64 = f64_nn.conv3d_backward_input(x64, w64, st, dy.astype(np.float64))
     assert rel(dx, dx64) <= TOL[prec]
+    if rate:
+        dw = from_dev(G.dilated_conv3d_backward_kernel(xd, wd, st, list(rate), to_dev(dy)))
+        dw64 = f64_nn.dilated_conv3d_backward_kernel(x64, w64, st, list(rate), dy.astype(np.float64))
+    else:
+        dw = from_dev(G.conv3d_backward_kernel(xd, wd, st, to_dev(dy)))
+        dw64 = f64_nn.conv3d_backward_kernel(x64, w64, st, dy.astype(np.float64))
+    assert _path() == 1
+    assert rel(dw, dw64) <= TOL[prec]
 
 
 def test_tc_repeatable_and_host_dropin(gpu_lib, f64_nn):
