@@ -8,7 +8,9 @@ BF16X3 drops lo*lo and the bf16 rounding of lo itself, about 3 * 2^-18
 relative per product; with random signs the worst element of a K = 3250
 reduction (5x5x130 taps) lands near 1.4e-5 of max|y|, hence 2e-5 here.
 Every case also asserts that the tensor-core kernel (not the CUDA-core
-fallback) ran, through owlgpu_last_conv_path().
+fallback) ran, through owlgpu_last_conv_path(), and that no tensor-core
+kernel abandoned a pipeline wait (owlgpu_device_status).  A TF32 request for
+backward_kernel runs the split-BF16 kernel (MN-major operands).
 """
 
 import numpy as np
@@ -52,7 +54,9 @@ def _nn(prec):
 def _path():
     from owl_gb300 import _lib
 
-    return _lib.lib().owlgpu_last_conv_path()
+    L = _lib.lib()
+    assert L.owlgpu_device_status() == 0, _lib.last_error()
+    return L.owlgpu_last_conv_path()
 
 
 @pytest.mark.parametrize("prec", ["bf16", "tf32", "bf16x3"])
