@@ -58,7 +58,8 @@ struct TcParams {
   long long xsb, xsw, xsu, xsv, ysb, ysw, ysu, ysv;  // pixel strides
   int Cin, Cout;
   int BN, CB, NCH, CPB, NCB, T, MH;
-  int HW, HU, HV, HP, PS;
+  int sw, su, sv;          // strides along w, u, v
+  int HW, HU, HV, HVR, HP, PS;  // halo rows along w, u; pixels per u-row (= sv * HVR)
   int n_tiles, u_tiles, v_tiles;
   long long total_tiles;
   unsigned halo_bytes, b_bytes;
@@ -186,9 +187,12 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
             if (idx < nchunks) {
               const int hp = idx / p.NCH, j = idx - hp * p.NCH;
               off[q] = j * p.PS * 16 + hp * 16;
-              const int hv = hp % p.HV, t2 = hp / p.HV;
-              const int hu = t2 % p.HU, hw = t2 / p.HU;
-              const int iw = tl.ow - p.pw + hw, iu = tl.u0 - p.pu + hu, iv = tl.v0 - p.pv + hv;
+              // halo pixel -> (w row, u row, v residue class, column within class)
+              const int hc = hp % p.HVR, t2 = hp / p.HVR;
+              const int hr = t2 % p.sv, t3 = t2 / p.sv;
+              const int hu = t3 % p.HU, hw = t3 / p.HU;
+              const int iw = tl.ow * p.sw - p.pw + hw, iu = tl.u0 * p.su - p.pu + hu;
+              const int iv = tl.v0 * p.sv - p.pv + hr + hc * p.sv;
               const int c = cbase + j * EPC;
               if (iw >= 0 && iw < p.IW && iu >= 0 && iu < p.IU && iv >= 0 && iv < p.IV &&
                   c < p.Cin) {
@@ -240,7 +244,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
       long long kh = 0, kb = 0;
       int tc = 0;
       const uint32_t halo0 = smem_u32(halo), b0 = smem_u32(bring);
-      const uint32_t a_lbo = (uint32_t)p.PS * 16, a_sbo = (uint32_t)p.HV * 16;
+      const uint32_t a_lbo = (uint32_t)p.PS * 16, a_sbo = (uint32_t)(p.su * p.HV) * 16;
       const uint32_t b_lbo = (uint32_t)p.BN * 16;
       const int ksteps = p.NCH / 2;
       for (long long t = blockIdx.x; t < p.total_tiles; t += gridDim.x, ++tc) {
@@ -269,7 +273,9 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
               const uint64_t bd_lo =
                   smem_desc(bbase + p.b_bytes + (uint32_t)(2 * s) * b_lbo, b_lbo, 128);
               for (int h = 0; h < p.MH; ++h) {
-                const int pix = (kw * p.dw * p.HU + h * 16 + ku * p.du) * p.HV + kv * p.dv;
+                const int qv = kv * p.dv;
+                const int pix = (kw * p.dw * p.HU + h * 16 * p.su + ku * p.du) * p.HV +
+                                (qv % p.sv) * p.HVR + qv / p.sv;
                 const uint32_t aaddr = hbase + (uint32_t)(2 * s) * a_lbo + (uint32_t)pix * 16;
                 const uint64_t ad = smem_desc(aaddr, a_lbo, a_sbo);
                 const uint32_t d = d0 + (uint32_t)(h * p.BN);
@@ -439,9 +445,24 @@ __global__ void prep_weights(const float *__restrict__ w, uint8_t *__restrict__ 
   }
 }
 
+// dY [B][OC][OR][OD][Co] -> zero-filled dilated copy with dY[o] at o*stride.
+__global__ void dilate_dy(const float *__restrict__ dy, float *__restrict__ out, long long B,
+                          long long OC, long long OR, long long OD, long long Co, int sc, int sr,
+                          int sd, long long DC, long long DR, long long DD) {
+  const long long n = B * OC * OR * OD * Co;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    long long c = i % Co, t = i / Co;
+    long long od = t % OD; t /= OD;
+    long long orr = t % OR; t /= OR;
+    long long oc = t % OC, b = t / OC;
+    out[((((b * DC) + oc * sc) * DR + orr * sr) * DD + od * sd) * Co + c] = dy[i];
+  }
+}
+
 // A convolution seen as (w, u, v) spatial axes plus channels.
 struct View {
-  int B, IW, IU, IV, OW, OU, OV, KW, KU, KV, dw, du, dv, pw, pu, pv;
+  int B, IW, IU, IV, OW, OU, OV, KW, KU, KV, dw, du, dv, pw, pu, pv, sw, su, sv;
   long long xsb, xsw, xsu, xsv, ysb, ysw, ysu, ysv;
   int Cin, Cout;
 };
@@ -467,6 +488,7 @@ View make_view(const ConvGeom &g, bool bwd_input) {
     v.OW = 1; v.OU = (int)oC; v.OV = (int)oR;
     v.KW = 1; v.KU = (int)g.KC; v.KV = (int)g.KR;
     v.dw = 1; v.du = g.dc; v.dv = g.dr;
+    v.sw = 1; v.su = bwd_input ? 1 : g.sc; v.sv = bwd_input ? 1 : g.sr;
     v.pw = 0; v.pu = pad(g.KC, g.dc, g.pc, bwd_input); v.pv = pad(g.KR, g.dr, g.pr, bwd_input);
     v.xsw = 1; v.xsu = iR; v.xsv = 1;
     v.ysw = 1; v.ysu = oR; v.ysv = 1;
@@ -475,6 +497,7 @@ View make_view(const ConvGeom &g, bool bwd_input) {
     v.OW = (int)oC; v.OU = (int)oR; v.OV = (int)oD;
     v.KW = (int)g.KC; v.KU = (int)g.KR; v.KV = (int)g.KD;
     v.dw = g.dc; v.du = g.dr; v.dv = g.dd;
+    v.sw = bwd_input ? 1 : g.sc; v.su = bwd_input ? 1 : g.sr; v.sv = bwd_input ? 1 : g.sd;
     v.pw = pad(g.KC, g.dc, g.pc, bwd_input); v.pu = pad(g.KR, g.dr, g.pr, bwd_input);
     v.pv = pad(g.KD, g.dd, g.pd, bwd_input);
     v.xsw = iR * iD; v.xsu = iD; v.xsv = 1;
@@ -529,8 +552,9 @@ bool plan(TcParams &p, const View &v, int kind) {
   for (int mh = (v.OU > 16 ? 2 : 1); mh >= 1; --mh) {
     p.MH = mh;
     p.HW = (v.KW - 1) * v.dw + 1;
-    p.HU = 16 * mh + (v.KU - 1) * v.du;
-    p.HV = 8 + (v.KV - 1) * v.dv;
+    p.HU = (16 * mh - 1) * v.su + (v.KU - 1) * v.du + 1;
+    p.HVR = 8 + ((v.KV - 1) * v.dv) / v.sv;
+    p.HV = v.sv * p.HVR;
     p.HP = p.HW * p.HU * p.HV;
     p.PS = p.HP + (((1 - p.HP) % 8) + 8) % 8;  // plane stride = 1 (mod 8) pixels
     if (p.PS >= 16384 || p.HV >= 16384) continue;
@@ -566,7 +590,10 @@ int launch(const TcParams &p, size_t smem, cudaStream_t s) {
 
 int run(int prec, const ConvGeom &g, bool bwd_input, const float *x, const float *w, float *y,
         cudaStream_t s) {
-  if (g.sc != 1 || g.sr != 1 || g.sd != 1) return kErrUnsupported;
+  // backward-input reads dY; with stride > 1 the caller passes dY dilated
+  // with zeros to a stride-1 geometry (dilate_dy), so strides are 1 here.
+  if (bwd_input && (g.sc != 1 || g.sr != 1 || g.sd != 1)) return kErrUnsupported;
+  if (g.sc > 8 || g.sr > 8 || g.sd > 8) return kErrUnsupported;
   const int kind = prec == OWLGPU_PREC_TF32 ? K_TF32 : (prec == OWLGPU_PREC_BF16X3 ? K_BF16X3 : K_BF16);
   const View v = make_view(g, bwd_input);
   if (v.OW * (long long)v.OU * v.OV * v.B == 0 || v.Cout == 0) return kOk;
@@ -576,6 +603,7 @@ int run(int prec, const ConvGeom &g, bool bwd_input, const float *x, const float
   p.B = v.B; p.IW = v.IW; p.IU = v.IU; p.IV = v.IV; p.OW = v.OW; p.OU = v.OU; p.OV = v.OV;
   p.KW = v.KW; p.KU = v.KU; p.KV = v.KV; p.dw = v.dw; p.du = v.du; p.dv = v.dv;
   p.pw = v.pw; p.pu = v.pu; p.pv = v.pv;
+  p.sw = v.sw; p.su = v.su; p.sv = v.sv;
   p.xsb = v.xsb; p.xsw = v.xsw; p.xsu = v.xsu; p.xsv = v.xsv;
   p.ysb = v.ysb; p.ysw = v.ysw; p.ysu = v.ysu; p.ysv = v.ysv;
   p.Cin = v.Cin; p.Cout = v.Cout;
@@ -637,7 +665,39 @@ int tc_conv_fwd(int prec, const ConvGeom &g, const float *x, const float *w, flo
 
 int tc_conv_bwd_input(int prec, const ConvGeom &g, float *dx, const float *w, const float *dy,
                       cudaStream_t s) {
-  return run(prec, g, true, dy, w, dx, s);
+  if (g.sc == 1 && g.sr == 1 && g.sd == 1) return run(prec, g, true, dy, w, dx, s);
+  // Strided: dX = stride-1 backward-input of dY dilated by the stride
+  // (dY[o] placed at o*s, zeros between); the padding rule is unchanged
+  // because (s*(O-1) + k_eff - I)/2 = (1*(O'-1) + k_eff - I)/2 with O' = s*(O-1)+1.
+  ConvGeom d = g;
+  d.OC = g.OC > 0 ? (g.OC - 1) * g.sc + 1 : 0;
+  d.OR = g.OR > 0 ? (g.OR - 1) * g.sr + 1 : 0;
+  d.OD = g.OD > 0 ? (g.OD - 1) * g.sd + 1 : 0;
+  d.sc = d.sr = d.sd = 1;
+  const long long n = d.B * d.OC * d.OR * d.OD * d.Co;
+  float *dyd = nullptr;
+  int rc = scratch_alloc((void **)&dyd, sizeof(float) * (size_t)std::max<long long>(n, 1), s);
+  if (rc) return rc;
+  cudaError_t e = cudaMemsetAsync(dyd, 0, sizeof(float) * (size_t)n, s);
+  if (e != cudaSuccess) {
+    scratch_free(dyd, s);
+    return cuda_fail(e, "cudaMemsetAsync(dilated dY)");
+  }
+  const long long m = g.y_elems();
+  if (m > 0) {
+    const int blocks = (int)std::min<long long>((m + 255) / 256, 152 * 16);
+    dilate_dy<<<blocks, 256, 0, s>>>(dy, dyd, g.B, g.OC, g.OR, g.OD, g.Co, g.sc, g.sr, g.sd, d.OC,
+                                     d.OR, d.OD);
+    e = cudaGetLastError();
+    note_launch();
+    if (e != cudaSuccess) {
+      scratch_free(dyd, s);
+      return cuda_fail(e, "dilate_dy");
+    }
+  }
+  rc = run(prec, d, true, dyd, w, dx, s);
+  scratch_free(dyd, s);
+  return rc;
 }
 
 int tc_read_status(int *out, cudaStream_t s) {

@@ -36,7 +36,6 @@ constexpr int kThreads = (kProducerWarps + 1 + 4) * 32;  // + MMA warp + 4 epilo
 constexpr int kProducerThreads = kProducerWarps * 32;
 constexpr int kSmemMax = 232448;
 constexpr long long kSpinLimit = 4000000000LL;
-constexpr int kTilePix = 128;  // output pixels per reduction tile (16 u x 8 v)
 
 enum Kind { K_BF16 = 0, K_TF32 = 1, K_BF16X3 = 2 };
 
@@ -44,9 +43,10 @@ struct WgParams {
   const float *x, *dy;
   float *out;
   int *status;
-  int B, IW, IU, IV, OW, OU, OV, KW, KU, KV, dw, du, dv, pw, pu, pv;
+  int B, IW, IU, IV, OW, OU, OV, KW, KU, KV, dw, du, dv, pw, pu, pv, sw, su, sv;
   long long xsb, xsw, xsu, xsv, ysb, ysw, ysu, ysv;
   int Ci, Co, T, TG, n_tg, BN, n_nb, n_mb, R;
+  int TU, TP;             // reduction tile: TU output rows (u) x 8 columns (v) = TP pixels
   int u_tiles, v_tiles;
   long long total_tiles, tiles_per_range;
   int PS;                 // X halo plane stride in pixels (max over groups)
@@ -138,7 +138,11 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
     minu = min(minu, ku * p.du); maxu = max(maxu, ku * p.du);
     minv = min(minv, kv * p.dv); maxv = max(maxv, kv * p.dv);
   }
-  const int HW = maxw - minw + 1, HU = 16 + maxu - minu, HV = 8 + maxv - minv;
+  // X halo rows: w (one output w per tile), u (16 output rows at stride su);
+  // along v the halo is split into sv residue classes of HVR columns so that
+  // 8 consecutive output columns are 8 consecutive stored pixels.
+  const int HW = maxw - minw + 1, HU = (p.TU - 1) * p.su + (maxu - minu) + 1;
+  const int HVR = 8 + (maxv - minv) / p.sv, HV = p.sv * HVR;
   const int HP = HW * HU * HV;
 
   uint8_t *xs = smem;
@@ -177,7 +181,7 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
     for (long long t = t_begin; t < t_end; ++t, ++k) {
       long long q = t;
       const int v0 = (int)(q % p.v_tiles) * 8; q /= p.v_tiles;
-      const int u0 = (int)(q % p.u_tiles) * 16; q /= p.u_tiles;
+      const int u0 = (int)(q % p.u_tiles) * p.TU; q /= p.u_tiles;
       const int ow = (int)(q % p.OW);
       const int b = (int)(q / p.OW);
       const int st = (int)(k % p.NS);
@@ -190,10 +194,11 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
       const int xchunks = HP * XPL;
       for (int idx = ptid; idx < xchunks; idx += kProducerThreads) {
         const int hp = idx / XPL, j = idx - hp * XPL;
-        const int hv = hp % HV, t2 = hp / HV;
-        const int hu = t2 % HU, hw = t2 / HU;
-        const int iw = ow - p.pw + minw + hw, iu = u0 - p.pu + minu + hu,
-                  iv = v0 - p.pv + minv + hv;
+        const int hc = hp % HVR, t2 = hp / HVR;
+        const int hr = t2 % p.sv, t3 = t2 / p.sv;
+        const int hu = t3 % HU, hw = t3 / HU;
+        const int iw = ow * p.sw - p.pw + minw + hw, iu = u0 * p.su - p.pu + minu + hu,
+                  iv = v0 * p.sv - p.pv + minv + hr + hc * p.sv;
         const int c = mb * 128 + j * EPC;
         float v[EPC];
 #pragma unroll
@@ -215,8 +220,8 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
         }
         put_chunk<KIND, EPC>(xd + (size_t)j * p.PS * 16 + (size_t)hp * 16, p.x_bytes, v);
       }
-      // dY tile: 128 output pixels x BN channels of co block nb
-      const int ychunks = kTilePix * YPL;
+      // dY tile: TP output pixels x BN channels of co block nb
+      const int ychunks = p.TP * YPL;
       for (int idx = ptid; idx < ychunks; idx += kProducerThreads) {
         const int kp = idx / YPL, j = idx - kp * YPL;
         const int ou = u0 + (kp >> 3), ov = v0 + (kp & 7);
@@ -239,7 +244,7 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
               if (c + e < p.Co) v[e] = __ldg(src + e);
           }
         }
-        put_chunk<KIND, EPC>(yd + (size_t)j * kTilePix * 16 + (size_t)kp * 16, p.y_bytes, v);
+        put_chunk<KIND, EPC>(yd + (size_t)j * p.TP * 16 + (size_t)kp * 16, p.y_bytes, v);
       }
       fence_proxy_async();
       mbar_arrive(smem_u32(&full[st]));
@@ -248,8 +253,8 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
     // ===================== MMA issuer =====================
     if (lane == 0) {
       const uint32_t x0 = smem_u32(xs), y0 = smem_u32(ys);
-      const uint32_t a_lbo = (uint32_t)HV * 16, a_sbo = (uint32_t)p.PS * 16;
-      const uint32_t b_lbo = 128, b_sbo = kTilePix * 16;
+      const uint32_t a_lbo = (uint32_t)(p.su * HV) * 16, a_sbo = (uint32_t)p.PS * 16;
+      const uint32_t b_lbo = 128, b_sbo = (uint32_t)p.TP * 16;
       long long k = 0;
       uint32_t acc = 0;
       bool ok = true;
@@ -262,7 +267,7 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
         tc_fence_after();
         const uint32_t xb = x0 + (uint32_t)st * PARTS * p.x_bytes;
         const uint32_t yb = y0 + (uint32_t)st * PARTS * p.y_bytes;
-        for (int s = 0; s < kTilePix / KSTEP_PIX; ++s) {
+        for (int s = 0; s < p.TP / KSTEP_PIX; ++s) {
           const int g0 = (s * KSTEP_PIX) >> 3;  // first u-group of this K step
           const uint32_t baddr = yb + (uint32_t)(s * KSTEP_PIX) * 16;
           const uint64_t bd = smem_desc(baddr, b_lbo, b_sbo);
@@ -270,8 +275,9 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
           for (int i = 0; i < ntap; ++i) {
             const int tt = tap0 + i;
             const int kv = tt % p.KV, ku = (tt / p.KV) % p.KU, kw = tt / (p.KV * p.KU);
-            const int pix = ((kw * p.dw - minw) * HU + (ku * p.du - minu) + g0) * HV +
-                            (kv * p.dv - minv);
+            const int qv = kv * p.dv - minv;
+            const int pix = ((kw * p.dw - minw) * HU + (ku * p.du - minu) + g0 * p.su) * HV +
+                            (qv % p.sv) * HVR + qv / p.sv;
             const uint32_t aaddr = xb + (uint32_t)pix * 16;
             const uint64_t ad = smem_desc(aaddr, a_lbo, a_sbo);
             const uint32_t d = tmem_base + (uint32_t)(i * p.BN);
@@ -396,7 +402,7 @@ int tc_wgrad_read_status(int *out, cudaStream_t s) {
 
 int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, const float *dy,
                        cudaStream_t s) {
-  if (g.sc != 1 || g.sr != 1 || g.sd != 1) return kErrUnsupported;
+  if (g.sc > 8 || g.sr > 8 || g.sd > 8) return kErrUnsupported;
   // The weight gradient reads both operands MN-major, which the TF32 MMA
   // kind does not accept here; a TF32 request runs the split-BF16 kernel,
   // whose error (~1e-5) is below TF32's (~1e-3).
@@ -414,12 +420,14 @@ int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, c
     p.IW = 1; p.IU = (int)g.IC; p.IV = (int)g.IR; p.OW = 1; p.OU = (int)g.OC; p.OV = (int)g.OR;
     p.KW = 1; p.KU = (int)g.KC; p.KV = (int)g.KR; p.dw = 1; p.du = g.dc; p.dv = g.dr;
     p.pw = 0; p.pu = g.pc; p.pv = g.pr;
+    p.sw = 1; p.su = g.sc; p.sv = g.sr;
     p.xsw = 1; p.xsu = g.IR; p.xsv = 1; p.ysw = 1; p.ysu = g.OR; p.ysv = 1;
   } else {
     p.IW = (int)g.IC; p.IU = (int)g.IR; p.IV = (int)g.ID;
     p.OW = (int)g.OC; p.OU = (int)g.OR; p.OV = (int)g.OD;
     p.KW = (int)g.KC; p.KU = (int)g.KR; p.KV = (int)g.KD;
     p.dw = g.dc; p.du = g.dr; p.dv = g.dd; p.pw = g.pc; p.pu = g.pr; p.pv = g.pd;
+    p.sw = g.sc; p.su = g.sr; p.sv = g.sd;
     p.xsw = g.IR * g.ID; p.xsu = g.ID; p.xsv = 1;
     p.ysw = g.OR * g.OD; p.ysu = g.OD; p.ysv = 1;
   }
@@ -427,14 +435,15 @@ int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, c
   p.ysb = g.OC * g.OR * g.OD;
   p.T = (int)g.taps();
   p.n_mb = (p.Ci + 127) / 128;
-  p.u_tiles = (p.OU + 15) / 16;
-  p.v_tiles = (p.OV + 7) / 8;
-  p.total_tiles = (long long)p.B * p.OW * p.u_tiles * p.v_tiles;
 
   // Plan: BN (co block), TG (taps per CTA, TG*BN <= 512 TMEM columns), NS = 2.
   // Prefer wide co blocks and many taps per CTA; shrink until the two stages
   // of X halo + dY tile fit in shared memory.
   bool planned = false;
+  for (int tu : {16, 8, 4, 2}) {
+  if (planned) break;
+  p.TU = tu;
+  p.TP = tu * 8;
   for (int bn : {128, 64, 32, 16}) {
     p.BN = std::min(bn, (p.Co + 15) / 16 * 16);
     for (int tg = std::min(p.T, 16); tg >= 1 && !planned; --tg) {
@@ -451,19 +460,24 @@ int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, c
           mnu = std::min(mnu, ku * p.du); mxu = std::max(mxu, ku * p.du);
           mnv = std::min(mnv, kv * p.dv); mxv = std::max(mxv, kv * p.dv);
         }
-        maxHP = std::max(maxHP, (mxw - mnw + 1) * (16 + mxu - mnu) * (8 + mxv - mnv));
+        maxHP = std::max(maxHP, (mxw - mnw + 1) * ((tu - 1) * p.su + mxu - mnu + 1) *
+                                    (p.sv * (8 + (mxv - mnv) / p.sv)));
       }
       p.PS = maxHP + (((1 - maxHP) % 8) + 8) % 8;
       if (p.PS >= 16384) continue;
       p.x_bytes = (unsigned)(128 * EB / 16) * (unsigned)p.PS * 16u;
-      p.y_bytes = (unsigned)(p.BN * EB / 16) * (unsigned)kTilePix * 16u;
+      p.y_bytes = (unsigned)(p.BN * EB / 16) * (unsigned)p.TP * 16u;
       p.NS = 2;
       const size_t need = (size_t)p.NS * parts * (p.x_bytes + p.y_bytes) + 256;
       if (need <= (size_t)kSmemMax) planned = true;
     }
     if (planned) break;
   }
+  }
   if (!planned) return kErrUnsupported;
+  p.u_tiles = (p.OU + p.TU - 1) / p.TU;
+  p.v_tiles = (p.OV + 7) / 8;
+  p.total_tiles = (long long)p.B * p.OW * p.u_tiles * p.v_tiles;
   p.n_nb = (p.Co + p.BN - 1) / p.BN;
   p.tmem_cols = 32;
   while (p.tmem_cols < (unsigned)(p.TG * p.BN)) p.tmem_cols <<= 1;

@@ -151,12 +151,60 @@ def test_tc_repeatable_and_host_dropin(gpu_lib, f64_nn):
     assert np.array_equal(a, h)
 
 
-def test_strided_request_runs_on_cuda_cores(gpu_lib, f64_nn):
-    """Stride-2 geometries are not on the tensor-core path yet: a bf16
-    request runs the FP32 CUDA-core kernel, reported by the path query."""
-    rng = np.random.default_rng(24)
-    x = rng.uniform(-1, 1, (2, 15, 15, 16)).astype(np.float32)
-    w = rng.uniform(-1, 1, (3, 3, 16, 8)).astype(np.float32)
-    y = from_dev(_nn("bf16").conv2d(to_dev(x), to_dev(w), [2, 2], VALID))
-    assert _path() == 0
-    assert rel(y, f64_nn.conv2d(x.astype(np.float64), w.astype(np.float64), [2, 2], VALID)) <= 1e-4
+STRIDED = [
+    # input, kernel, stride, rate, padding
+    ((2, 15, 15, 16), (3, 3, 16, 8), (2, 2), (1, 1), VALID),
+    ((2, 28, 28, 64), (3, 3, 64, 128), (2, 2), (1, 1), VALID),
+    ((2, 17, 13, 24), (3, 2, 24, 40), (2, 3), (1, 2), SAME),
+    ((1, 20, 22, 32), (5, 5, 32, 48), (3, 2), (2, 1), SAME),
+    ((2, 16, 16, 64), (1, 1, 64, 128), (2, 2), (1, 1), SAME),
+]
+
+
+@pytest.mark.parametrize("prec", ["bf16", "tf32", "bf16x3"])
+@pytest.mark.parametrize("case", STRIDED)
+def test_strided_conv2d_tc(gpu_lib, f64_nn, prec, case):
+    """Strided geometries: forward stages the halo in stride residue classes,
+    backward_input runs on dY dilated by the stride, backward_kernel stages X
+    in residue classes -- all on tcgen05."""
+    xs, ks, st, rate, pad = case
+    rng = np.random.default_rng(25)
+    x = rng.uniform(-1, 1, xs).astype(np.float32)
+    w = (rng.standard_normal(ks) * np.sqrt(2.0 / np.prod(ks[:3]))).astype(np.float32)
+    G = _nn(prec)
+    x64, w64 = x.astype(np.float64), w.astype(np.float64)
+    xd, wd = to_dev(x), to_dev(w)
+    st, rate = list(st), list(rate)
+    y = from_dev(G.dilated_conv2d(xd, wd, st, rate, pad))
+    assert _path() == 1
+    y64 = f64_nn.dilated_conv2d(x64, w64, st, rate, pad)
+    assert rel(y, y64) <= TOL[prec]
+    dy = rng.standard_normal(y64.shape).astype(np.float32)
+    dx = from_dev(G.dilated_conv2d_backward_input(xd, wd, st, rate, to_dev(dy)))
+    assert _path() == 1
+    assert rel(dx, f64_nn.dilated_conv2d_backward_input(x64, w64, st, rate,
+                                                        dy.astype(np.float64))) <= TOL[prec]
+    dw = from_dev(G.dilated_conv2d_backward_kernel(xd, wd, st, rate, to_dev(dy)))
+    assert _path() == 1
+    assert rel(dw, f64_nn.dilated_conv2d_backward_kernel(x64, w64, st, rate,
+                                                         dy.astype(np.float64))) <= TOL[prec]
+
+
+def test_strided_conv3d_tc(gpu_lib, f64_nn):
+    rng = np.random.default_rng(26)
+    x = rng.uniform(-1, 1, (2, 9, 9, 8, 16)).astype(np.float32)
+    w = (rng.standard_normal((3, 3, 3, 16, 32)) * 0.07).astype(np.float32)
+    G = _nn("bf16")
+    st = [2, 2, 2]
+    x64, w64 = x.astype(np.float64), w.astype(np.float64)
+    y = from_dev(G.conv3d(to_dev(x), to_dev(w), st, SAME))
+    assert _path() == 1
+    y64 = f64_nn.conv3d(x64, w64, st, SAME)
+    assert rel(y, y64) <= TOL["bf16"]
+    dy = rng.standard_normal(y64.shape).astype(np.float32)
+    dx = from_dev(G.conv3d_backward_input(to_dev(x), to_dev(w), st, to_dev(dy)))
+    assert _path() == 1
+    assert rel(dx, f64_nn.conv3d_backward_input(x64, w64, st, dy.astype(np.float64))) <= 1e-2
+    dw = from_dev(G.conv3d_backward_kernel(to_dev(x), to_dev(w), st, to_dev(dy)))
+    assert _path() == 1
+    assert rel(dw, f64_nn.conv3d_backward_kernel(x64, w64, st, dy.astype(np.float64))) <= 1e-2
