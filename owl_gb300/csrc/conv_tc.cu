@@ -536,38 +536,45 @@ int *status_ptr() {
   return p[dev];
 }
 
-// Choose tile and pipeline sizes; false if no configuration fits.
+// Choose tile and pipeline sizes; false if no configuration fits.  Prefers
+// two M-halves and wide channel blocks, narrowing the channel block (fewer
+// bytes of K per halo stage) before giving up.
 bool plan(TcParams &p, const View &v, int kind) {
   const int EB = (kind == K_TF32) ? 4 : 2;
   const int parts = (kind == K_BF16X3) ? 2 : 1;
-  p.CB = std::min(128, (int)((v.Cin * EB + 31) / 32 * 32));
-  p.CPB = p.CB / EB;
-  p.NCH = p.CB / 16;
-  p.NCB = (v.Cin + p.CPB - 1) / p.CPB;
   p.BN = std::min(128, (v.Cout + 15) / 16 * 16);
   p.n_tiles = (v.Cout + p.BN - 1) / p.BN;
   p.T = v.KW * v.KU * v.KV;
-  p.b_bytes = (unsigned)(p.BN * p.CB);
   p.NH = 2;
+  const int cb0 = std::min(128, (int)((v.Cin * EB + 31) / 32 * 32));
   for (int mh = (v.OU > 16 ? 2 : 1); mh >= 1; --mh) {
-    p.MH = mh;
-    p.HW = (v.KW - 1) * v.dw + 1;
-    p.HU = (16 * mh - 1) * v.su + (v.KU - 1) * v.du + 1;
-    p.HVR = 8 + ((v.KV - 1) * v.dv) / v.sv;
-    p.HV = v.sv * p.HVR;
-    p.HP = p.HW * p.HU * p.HV;
-    p.PS = p.HP + (((1 - p.HP) % 8) + 8) % 8;  // plane stride = 1 (mod 8) pixels
-    if (p.PS >= 16384 || p.HV >= 16384) continue;
-    p.halo_bytes = (unsigned)p.PS * 16u * (unsigned)p.NCH;
-    long long fixed = (long long)p.NH * parts * p.halo_bytes + 512;
-    long long room = kSmemMax - fixed;
-    int nb = (int)std::min<long long>(8, room / ((long long)parts * p.b_bytes));
-    if (nb < 2) continue;
-    p.NB = nb;
-    p.tmem_cols = 32;
-    while (p.tmem_cols < (unsigned)(2 * p.MH * p.BN)) p.tmem_cols <<= 1;
-    if (p.tmem_cols > 512) continue;
-    return true;
+    for (int cb = cb0; cb >= 32; cb -= 32) {
+      if (cb != cb0 && cb % 64 != 0 && cb != 32) continue;  // try cb0, then 64, 32
+      p.MH = mh;
+      p.CB = cb;
+      p.CPB = p.CB / EB;
+      p.NCH = p.CB / 16;
+      p.NCB = (v.Cin + p.CPB - 1) / p.CPB;
+      p.b_bytes = (unsigned)(p.BN * p.CB);
+      p.HW = (v.KW - 1) * v.dw + 1;
+      p.HU = (16 * mh - 1) * v.su + (v.KU - 1) * v.du + 1;
+      p.HVR = 8 + ((v.KV - 1) * v.dv) / v.sv;
+      p.HV = v.sv * p.HVR;
+      p.HP = p.HW * p.HU * p.HV;
+      p.PS = p.HP + (((1 - p.HP) % 8) + 8) % 8;  // plane stride = 1 (mod 8) pixels
+      if (p.PS >= 16384 || p.HV >= 16384) continue;
+      p.halo_bytes = (unsigned)p.PS * 16u * (unsigned)p.NCH;
+      long long fixed = (long long)p.NH * parts * p.halo_bytes + 512;
+      long long room = kSmemMax - fixed;
+      if (room <= 0) continue;
+      int nb = (int)std::min<long long>(8, room / ((long long)parts * p.b_bytes));
+      if (nb < 2) continue;
+      p.NB = nb;
+      p.tmem_cols = 32;
+      while (p.tmem_cols < (unsigned)(2 * p.MH * p.BN)) p.tmem_cols <<= 1;
+      if (p.tmem_cols > 512) continue;
+      return true;
+    }
   }
   return false;
 }
