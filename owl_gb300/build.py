@@ -25,7 +25,8 @@ LIB = PKG / "libowlgpu.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-              "-Xcompiler", "-fvisibility=hidden", "--expt-relaxed-constexpr"]
+              "-Xcompiler", "-fvisibility=hidden", "--expt-relaxed-constexpr",
+              "--expt-extended-lambda"]
 
 
 def nvcc() -> str:

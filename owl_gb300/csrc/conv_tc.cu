@@ -164,8 +164,14 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
 
   if (warp < kProducerWarps) {
     // ===================== halo producers =====================
-    const int ptid = threadIdx.x;
-    const int nchunks = p.HP * p.NCH;
+    // Each warp stages whole halo rows: a row is one (w, u, residue) line of
+    // HVR pixels whose global addresses advance by a fixed step, so the row
+    // bounds are checked once and each lane only adds offsets.  Two rows per
+    // pass give every lane up to 2*kSlots chunk loads in flight.
+    const int nrows = p.HW * p.HU * p.sv;
+    const int S = p.HVR * p.NCH;  // chunk slots per row
+    const int nsh = (p.NCH & (p.NCH - 1)) == 0 ? __ffs(p.NCH) - 1 : -1;
+    const long long vstep = (long long)p.sv * p.xsv * p.Cin;  // floats between row pixels
     long long k = 0;  // halo stage counter
     for (long long t = blockIdx.x; t < p.total_tiles; t += gridDim.x) {
       const Tile tl = decode_tile(p, t);
@@ -175,62 +181,117 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
         if (!wait_bar(smem_u32(&halo_empty[hs]), ph ^ 1, abort_flag, p.status)) goto done;
         uint8_t *dst = halo + (size_t)hs * PARTS * p.halo_bytes;
         const int cbase = cb * p.CPB;
-        for (int idx0 = ptid; idx0 < nchunks; idx0 += 4 * kProducerThreads) {
-          float v[4][EPC];
-          int off[4];
+        for (int r0 = warp * 2; r0 < nrows; r0 += 2 * kProducerWarps) {
+          constexpr int kSlots = 3;  // slots per lane per row per pass
+          float v[2][kSlots][EPC];
+          int off[2][kSlots];
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const int idx = idx0 + q * kProducerThreads;
+          for (int rr = 0; rr < 2; ++rr) {
+            const int r = r0 + rr;
+            // row -> (w row, u row, residue class)
+            const int hr = r % p.sv, t3 = r / p.sv;
+            const int hu = t3 % p.HU, hw = t3 / p.HU;
+            const int iw = tl.ow * p.sw - p.pw + hw, iu = tl.u0 * p.su - p.pu + hu;
+            const int ivs = tl.v0 * p.sv - p.pv + hr;  // global v of the row's pixel 0
+            const bool row_ok = r < nrows && iw >= 0 && iw < p.IW && iu >= 0 && iu < p.IU;
+            const float *rowp =
+                p.x + ((long long)tl.b * p.xsb + (long long)iw * p.xsw + (long long)iu * p.xsu +
+                       (long long)ivs * p.xsv) * p.Cin + cbase;
 #pragma unroll
-            for (int e = 0; e < EPC; ++e) v[q][e] = 0.f;
-            off[q] = -1;
-            if (idx < nchunks) {
-              const int hp = idx / p.NCH, j = idx - hp * p.NCH;
-              off[q] = j * p.PS * 16 + hp * 16;
-              // halo pixel -> (w row, u row, v residue class, column within class)
-              const int hc = hp % p.HVR, t2 = hp / p.HVR;
-              const int hr = t2 % p.sv, t3 = t2 / p.sv;
-              const int hu = t3 % p.HU, hw = t3 / p.HU;
-              const int iw = tl.ow * p.sw - p.pw + hw, iu = tl.u0 * p.su - p.pu + hu;
-              const int iv = tl.v0 * p.sv - p.pv + hr + hc * p.sv;
-              const int c = cbase + j * EPC;
-              if (iw >= 0 && iw < p.IW && iu >= 0 && iu < p.IU && iv >= 0 && iv < p.IV &&
-                  c < p.Cin) {
-                const float *src = p.x + ((long long)tl.b * p.xsb + iw * p.xsw + iu * p.xsu +
-                                          iv * p.xsv) * p.Cin + c;
-                if (p.vec_in && c + EPC <= p.Cin) {
+            for (int q = 0; q < kSlots; ++q) {
+              const int sl = lane + 32 * q;
 #pragma unroll
-                  for (int e = 0; e < EPC; e += 4) {
-                    float4 f = __ldg(reinterpret_cast<const float4 *>(src + e));
-                    v[q][e] = f.x; v[q][e + 1] = f.y; v[q][e + 2] = f.z; v[q][e + 3] = f.w;
+              for (int e = 0; e < EPC; ++e) v[rr][q][e] = 0.f;
+              off[rr][q] = -1;
+              if (r < nrows && sl < S) {
+                const int hc = nsh >= 0 ? (sl >> nsh) : sl / p.NCH;
+                const int j = sl - hc * p.NCH;
+                off[rr][q] = j * p.PS * 16 + (r * p.HVR + hc) * 16;
+                const int iv = ivs + hc * p.sv;
+                const int c = cbase + j * EPC;
+                if (row_ok && iv >= 0 && iv < p.IV && c < p.Cin) {
+                  const float *src = rowp + hc * vstep + j * EPC;
+                  if (p.vec_in && c + EPC <= p.Cin) {
+#pragma unroll
+                    for (int e = 0; e < EPC; e += 4) {
+                      float4 f = __ldg(reinterpret_cast<const float4 *>(src + e));
+                      v[rr][q][e] = f.x; v[rr][q][e + 1] = f.y;
+                      v[rr][q][e + 2] = f.z; v[rr][q][e + 3] = f.w;
+                    }
+                  } else {
+#pragma unroll
+                    for (int e = 0; e < EPC; ++e)
+                      if (c + e < p.Cin) v[rr][q][e] = __ldg(src + e);
                   }
-                } else {
-#pragma unroll
-                  for (int e = 0; e < EPC; ++e)
-                    if (c + e < p.Cin) v[q][e] = __ldg(src + e);
                 }
               }
             }
           }
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            if (off[q] < 0) continue;
-            uint4 hi;
-            if (KIND == K_TF32) {
-              hi = make_uint4(to_tf32(v[q][0]), to_tf32(v[q][1]), to_tf32(v[q][2]),
-                              to_tf32(v[q][3]));
-            } else {
-              hi = make_uint4(pack_bf16(v[q][0], v[q][1]), pack_bf16(v[q][2], v[q][3]),
-                              pack_bf16(v[q][4], v[q][5]), pack_bf16(v[q][6], v[q][7]));
-            }
-            *reinterpret_cast<uint4 *>(dst + off[q]) = hi;
-            if (KIND == K_BF16X3) {
-              float r[8];
+          for (int rr = 0; rr < 2; ++rr)
 #pragma unroll
-              for (int e = 0; e < 8; ++e) r[e] = v[q][e] - bf16_round(v[q][e]);
-              uint4 lo = make_uint4(pack_bf16(r[0], r[1]), pack_bf16(r[2], r[3]),
-                                    pack_bf16(r[4], r[5]), pack_bf16(r[6], r[7]));
-              *reinterpret_cast<uint4 *>(dst + p.halo_bytes + off[q]) = lo;
+            for (int q = 0; q < kSlots; ++q) {
+              if (off[rr][q] < 0) continue;
+              uint4 hi;
+              if (KIND == K_TF32) {
+                hi = make_uint4(to_tf32(v[rr][q][0]), to_tf32(v[rr][q][1]),
+                                to_tf32(v[rr][q][2]), to_tf32(v[rr][q][3]));
+              } else {
+                hi = make_uint4(pack_bf16(v[rr][q][0], v[rr][q][1]),
+                                pack_bf16(v[rr][q][2], v[rr][q][3]),
+                                pack_bf16(v[rr][q][4], v[rr][q][5]),
+                                pack_bf16(v[rr][q][6], v[rr][q][7]));
+              }
+              *reinterpret_cast<uint4 *>(dst + off[rr][q]) = hi;
+              if (KIND == K_BF16X3) {
+                float rs[8];
+#pragma unroll
+                for (int e = 0; e < 8; ++e) rs[e] = v[rr][q][e] - bf16_round(v[rr][q][e]);
+                uint4 lo = make_uint4(pack_bf16(rs[0], rs[1]), pack_bf16(rs[2], rs[3]),
+                                      pack_bf16(rs[4], rs[5]), pack_bf16(rs[6], rs[7]));
+                *reinterpret_cast<uint4 *>(dst + p.halo_bytes + off[rr][q]) = lo;
+              }
+            }
+          // rows wider than 32*kSlots chunk slots: stage the remainder one
+          // slot at a time (large dilations / long kernel rows only)
+          for (int rr = 0; rr < 2; ++rr) {
+            const int r = r0 + rr;
+            if (r >= nrows) break;
+            for (int sl = lane + 32 * kSlots; sl < S; sl += 32) {
+              const int hr = r % p.sv, t3 = r / p.sv;
+              const int hu = t3 % p.HU, hw = t3 / p.HU;
+              const int iw = tl.ow * p.sw - p.pw + hw, iu = tl.u0 * p.su - p.pu + hu;
+              const int hc = sl / p.NCH, j = sl - hc * p.NCH;
+              const int iv = tl.v0 * p.sv - p.pv + hr + hc * p.sv;
+              const int c = cbase + j * EPC;
+              float w8[EPC];
+#pragma unroll
+              for (int e = 0; e < EPC; ++e) w8[e] = 0.f;
+              if (iw >= 0 && iw < p.IW && iu >= 0 && iu < p.IU && iv >= 0 && iv < p.IV) {
+                const float *src = p.x + ((long long)tl.b * p.xsb + (long long)iw * p.xsw +
+                                          (long long)iu * p.xsu + (long long)iv * p.xsv) *
+                                             p.Cin + c;
+#pragma unroll
+                for (int e = 0; e < EPC; ++e)
+                  if (c + e < p.Cin) w8[e] = __ldg(src + e);
+              }
+              const int o = j * p.PS * 16 + (r * p.HVR + hc) * 16;
+              uint4 hi;
+              if (KIND == K_TF32) {
+                hi = make_uint4(to_tf32(w8[0]), to_tf32(w8[1]), to_tf32(w8[2]), to_tf32(w8[3]));
+              } else {
+                hi = make_uint4(pack_bf16(w8[0], w8[1]), pack_bf16(w8[2], w8[3]),
+                                pack_bf16(w8[4], w8[5]), pack_bf16(w8[6], w8[7]));
+              }
+              *reinterpret_cast<uint4 *>(dst + o) = hi;
+              if (KIND == K_BF16X3) {
+                float rs[8];
+#pragma unroll
+                for (int e = 0; e < 8; ++e) rs[e] = w8[e] - bf16_round(w8[e]);
+                *reinterpret_cast<uint4 *>(dst + p.halo_bytes + o) =
+                    make_uint4(pack_bf16(rs[0], rs[1]), pack_bf16(rs[2], rs[3]),
+                               pack_bf16(rs[4], rs[5]), pack_bf16(rs[6], rs[7]));
+              }
             }
           }
         }

@@ -24,6 +24,7 @@
 #include "../../include/owlgpu.h"
 #include "common.cuh"
 #include "tc_ptx.cuh"
+#include "tc_stage.cuh"
 
 namespace owlgpu {
 namespace {
@@ -176,7 +177,6 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
 
   if (warp < kProducerWarps) {
     // ===================== producers: X halo + dY tile =====================
-    const int ptid = threadIdx.x;
     long long k = 0;
     for (long long t = t_begin; t < t_end; ++t, ++k) {
       long long q = t;
@@ -190,61 +190,44 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
         goto done;
       uint8_t *xd = xs + (size_t)st * PARTS * p.x_bytes;
       uint8_t *yd = ys + (size_t)st * PARTS * p.y_bytes;
-      // X halo: HP pixels x 128 channels of ci block mb
-      const int xchunks = HP * XPL;
-      for (int idx = ptid; idx < xchunks; idx += kProducerThreads) {
-        const int hp = idx / XPL, j = idx - hp * XPL;
-        const int hc = hp % HVR, t2 = hp / HVR;
-        const int hr = t2 % p.sv, t3 = t2 / p.sv;
-        const int hu = t3 % HU, hw = t3 / HU;
-        const int iw = ow * p.sw - p.pw + minw + hw, iu = u0 * p.su - p.pu + minu + hu,
-                  iv = v0 * p.sv - p.pv + minv + hr + hc * p.sv;
-        const int c = mb * 128 + j * EPC;
-        float v[EPC];
-#pragma unroll
-        for (int e = 0; e < EPC; ++e) v[e] = 0.f;
-        if (iw >= 0 && iw < p.IW && iu >= 0 && iu < p.IU && iv >= 0 && iv < p.IV && c < p.Ci) {
-          const float *src =
-              p.x + ((long long)b * p.xsb + iw * p.xsw + iu * p.xsu + iv * p.xsv) * p.Ci + c;
-          if (p.vec_x && c + EPC <= p.Ci) {
-#pragma unroll
-            for (int e = 0; e < EPC; e += 4) {
-              float4 f = __ldg(reinterpret_cast<const float4 *>(src + e));
-              v[e] = f.x; v[e + 1] = f.y; v[e + 2] = f.z; v[e + 3] = f.w;
-            }
-          } else {
-#pragma unroll
-            for (int e = 0; e < EPC; ++e)
-              if (c + e < p.Ci) v[e] = __ldg(src + e);
-          }
-        }
-        put_chunk<KIND, EPC>(xd + (size_t)j * p.PS * 16 + (size_t)hp * 16, p.x_bytes, v);
+      // X halo: rows (w, u, residue class) of HVR pixels x 128 channels of ci block mb
+      {
+        const int cb0 = mb * 128;
+        stage::stage_rows<KIND, EPC, 6>(
+            xd, p.x_bytes, (uint32_t)p.PS * 16, HW * HU * p.sv, HVR, XPL, p.Ci - cb0,
+            p.vec_x != 0, warp, kProducerWarps, lane, [&](int r) {
+              const int hr = r % p.sv, t3 = r / p.sv;
+              const int hu = t3 % HU, hw = t3 / HU;
+              const int iw = ow * p.sw - p.pw + minw + hw, iu = u0 * p.su - p.pu + minu + hu;
+              const int ivs = v0 * p.sv - p.pv + minv + hr;
+              stage::Row row;
+              row.ok = iw >= 0 && iw < p.IW && iu >= 0 && iu < p.IU;
+              row.rowp = p.x + ((long long)b * p.xsb + (long long)iw * p.xsw +
+                                (long long)iu * p.xsu + (long long)ivs * p.xsv) * p.Ci + cb0;
+              row.pstep = (long long)p.sv * p.xsv * p.Ci;
+              row.vfirst = ivs;
+              row.vstride = p.sv;
+              row.vlim = p.IV;
+              return row;
+            });
       }
-      // dY tile: TP output pixels x BN channels of co block nb
-      const int ychunks = p.TP * YPL;
-      for (int idx = ptid; idx < ychunks; idx += kProducerThreads) {
-        const int kp = idx / YPL, j = idx - kp * YPL;
-        const int ou = u0 + (kp >> 3), ov = v0 + (kp & 7);
-        const int c = nb * p.BN + j * EPC;
-        float v[EPC];
-#pragma unroll
-        for (int e = 0; e < EPC; ++e) v[e] = 0.f;
-        if (ou < p.OU && ov < p.OV && c < p.Co) {
-          const float *src =
-              p.dy + ((long long)b * p.ysb + ow * p.ysw + ou * p.ysu + ov * p.ysv) * p.Co + c;
-          if (p.vec_y && c + EPC <= p.Co) {
-#pragma unroll
-            for (int e = 0; e < EPC; e += 4) {
-              float4 f = __ldg(reinterpret_cast<const float4 *>(src + e));
-              v[e] = f.x; v[e + 1] = f.y; v[e + 2] = f.z; v[e + 3] = f.w;
-            }
-          } else {
-#pragma unroll
-            for (int e = 0; e < EPC; ++e)
-              if (c + e < p.Co) v[e] = __ldg(src + e);
-          }
-        }
-        put_chunk<KIND, EPC>(yd + (size_t)j * p.TP * 16 + (size_t)kp * 16, p.y_bytes, v);
+      // dY tile: TU rows (u) of 8 output pixels x BN channels of co block nb
+      {
+        const int cb0 = nb * p.BN;
+        stage::stage_rows<KIND, EPC, 4>(
+            yd, p.y_bytes, (uint32_t)p.TP * 16, p.TU, 8, YPL, p.Co - cb0, p.vec_y != 0, warp,
+            kProducerWarps, lane, [&](int r) {
+              const int ou = u0 + r;
+              stage::Row row;
+              row.ok = ou < p.OU;
+              row.rowp = p.dy + ((long long)b * p.ysb + (long long)ow * p.ysw +
+                                 (long long)ou * p.ysu + (long long)v0 * p.ysv) * p.Co + cb0;
+              row.pstep = p.ysv * p.Co;
+              row.vfirst = v0;
+              row.vstride = 1;
+              row.vlim = p.OV;
+              return row;
+            });
       }
       fence_proxy_async();
       mbar_arrive(smem_u32(&full[st]));
