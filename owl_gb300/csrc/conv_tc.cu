@@ -4,8 +4,11 @@
 //
 // Design: persistent, warp-specialised "halo" implicit GEMM.
 //   * An output tile is 16*MH positions along one spatial axis (u) by 8 along
-//     another (v); each group of 8 v-positions is one 8-row core-matrix band
-//     of the MMA's M = 128 rows.  MH (1 or 2) M=128 halves share every B tile.
+//     another (v): N = 128*MH pixels, each group of 8 v-positions one 8-row
+//     core-matrix band of the MMA's N dimension.  The kernel tile (128 output
+//     channels) is the M = 128 operand.  tcgen05.mma costs the same number of
+//     cycles for N = 64..256 at M = 128, so the pixel dimension goes on N and
+//     uses the full N = 256 whenever the output is at least 17 rows tall.
 //   * Producer warps load the input halo the tile needs for one block of
 //     channels -- once -- from the float32 activation, convert it (bf16 RN,
 //     tf32 RNA, or bf16 hi + lo) and store it in shared memory as
@@ -16,9 +19,11 @@
 //   * The kernel tensor is re-laid out once per call (prep_weights) into the
 //     exact shared-memory image of each (channel block, tap) B tile, which one
 //     thread streams with cp.async.bulk (TMA engine) into a ring of stages.
-//   * One thread issues tcgen05.mma (M=128, N=BN, K=16/8 per instruction)
-//     into a double-buffered TMEM accumulator; four epilogue warps drain the
-//     other buffer (tcgen05.ld) and write float32 results to HBM.
+//   * One thread issues tcgen05.mma (M=128 channels, N=128*MH pixels, K=16/8
+//     per instruction) into a double-buffered TMEM accumulator; four epilogue
+//     warps drain the other buffer (tcgen05.ld, one TMEM lane per output
+//     channel) and write float32 results to HBM, 32 consecutive channels of a
+//     pixel per warp store.
 //   * Every wait is bounded: a stuck barrier sets an error word and the CTA
 //     unwinds (waits for its in-flight copies and MMAs, frees TMEM, returns).
 //
@@ -313,7 +318,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
         const uint32_t aph = (uint32_t)((tc >> 1) & 1);
         if (!wait_bar(smem_u32(&acc_empty[abuf]), aph ^ 1, abort_flag, p.status)) break;
         tc_fence_after();
-        const uint32_t d0 = tmem_base + (uint32_t)(abuf * p.MH * p.BN);
+        const uint32_t d0 = tmem_base + (uint32_t)(abuf * p.MH * 128);
         uint32_t acc = 0;
         bool ok = true;
         for (int cb = 0; cb < p.NCB && ok; ++cb, ++kh) {
@@ -327,28 +332,26 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
             if (!wait_bar(smem_u32(&b_full[bs]), (uint32_t)((kb / p.NB) & 1), abort_flag,
                           p.status)) { ok = false; break; }
             tc_fence_after();
-            const uint32_t bbase = b0 + (uint32_t)bs * PARTS * p.b_bytes;
+            const uint32_t wbase = b0 + (uint32_t)bs * PARTS * p.b_bytes;
             const int kv = tap % p.KV, ku = (tap / p.KV) % p.KU, kw = tap / (p.KV * p.KU);
+            const int qv = kv * p.dv;
+            const int pix = (kw * p.dw * p.HU + ku * p.du) * p.HV + (qv % p.sv) * p.HVR + qv / p.sv;
             for (int s = 0; s < ksteps; ++s) {
-              const uint64_t bd = smem_desc(bbase + (uint32_t)(2 * s) * b_lbo, b_lbo, 128);
-              const uint64_t bd_lo =
-                  smem_desc(bbase + p.b_bytes + (uint32_t)(2 * s) * b_lbo, b_lbo, 128);
-              for (int h = 0; h < p.MH; ++h) {
-                const int qv = kv * p.dv;
-                const int pix = (kw * p.dw * p.HU + h * 16 * p.su + ku * p.du) * p.HV +
-                                (qv % p.sv) * p.HVR + qv / p.sv;
-                const uint32_t aaddr = hbase + (uint32_t)(2 * s) * a_lbo + (uint32_t)pix * 16;
-                const uint64_t ad = smem_desc(aaddr, a_lbo, a_sbo);
-                const uint32_t d = d0 + (uint32_t)(h * p.BN);
-                if (KIND == K_TF32) {
-                  mma_tf32(d, ad, bd, p.idesc, acc);
-                } else {
-                  mma_bf16(d, ad, bd, p.idesc, acc);
-                  if (KIND == K_BF16X3) {
-                    const uint64_t ad_lo = smem_desc(aaddr + p.halo_bytes, a_lbo, a_sbo);
-                    mma_bf16(d, ad, bd_lo, p.idesc, 1);
-                    mma_bf16(d, ad_lo, bd, p.idesc, 1);
-                  }
+              // A: 128 output channels of this kernel tile (K-major)
+              const uint64_t wd = smem_desc(wbase + (uint32_t)(2 * s) * b_lbo, b_lbo, 128);
+              // B: the 16*MH groups of 8 output pixels, read out of the halo
+              const uint32_t xaddr = hbase + (uint32_t)(2 * s) * a_lbo + (uint32_t)pix * 16;
+              const uint64_t xd = smem_desc(xaddr, a_lbo, a_sbo);
+              if (KIND == K_TF32) {
+                mma_tf32(d0, wd, xd, p.idesc, acc);
+              } else {
+                mma_bf16(d0, wd, xd, p.idesc, acc);
+                if (KIND == K_BF16X3) {
+                  const uint64_t wd_lo =
+                      smem_desc(wbase + p.b_bytes + (uint32_t)(2 * s) * b_lbo, b_lbo, 128);
+                  const uint64_t xd_lo = smem_desc(xaddr + p.halo_bytes, a_lbo, a_sbo);
+                  mma_bf16(d0, wd_lo, xd, p.idesc, 1);
+                  mma_bf16(d0, wd, xd_lo, p.idesc, 1);
                 }
               }
               acc = 1;
@@ -404,8 +407,6 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
   } else {
     // ===================== epilogue =====================
     const int q = warp & 3;  // TMEM lane quadrant this warp may access
-    const int row = q * 32 + lane;
-    const int g = row >> 3, vv = row & 7;
     int tc = 0;
     for (long long t = blockIdx.x; t < p.total_tiles; t += gridDim.x, ++tc) {
       const Tile tl = decode_tile(p, t);
@@ -413,31 +414,21 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
       if (!wait_bar(smem_u32(&acc_full[abuf]), (uint32_t)((tc >> 1) & 1), abort_flag, p.status))
         break;
       tc_fence_after();
-      const int n0 = tl.nt * p.BN;
-      for (int h = 0; h < p.MH; ++h) {
-        const int u = tl.u0 + h * 16 + g, v = tl.v0 + vv;
-        const bool valid = u < p.OU && v < p.OV;
-        float *out = p.y + ((long long)tl.b * p.ysb + (long long)tl.ow * p.ysw +
-                            (long long)u * p.ysu + (long long)v * p.ysv) * p.Cout + n0;
-        const uint32_t tcol = tmem_base + ((uint32_t)(q * 32) << 16) +
-                              (uint32_t)((abuf * p.MH + h) * p.BN);
-        for (int c0 = 0; c0 < p.BN; c0 += 16) {
-          uint32_t r[16];
-          tmem_ld16(tcol + (uint32_t)c0, r);
-          tmem_ld_wait();
-          if (valid) {
-            if (p.vec_out && n0 + c0 + 16 <= p.Cout) {
+      // TMEM lane = output channel, column = pixel (group g = col / 8, v = col % 8)
+      const int co = tl.nt * 128 + q * 32 + lane;
+      const bool co_ok = co < p.Cout;
+      const uint32_t tcol = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(abuf * p.MH * 128);
+      float *ybase = p.y + ((long long)tl.b * p.ysb + (long long)tl.ow * p.ysw) * p.Cout + co;
+      for (int c0 = 0; c0 < p.MH * 128; c0 += 16) {
+        uint32_t r[16];
+        tmem_ld16(tcol + (uint32_t)c0, r);
+        tmem_ld_wait();
 #pragma unroll
-              for (int e = 0; e < 16; e += 4)
-                *reinterpret_cast<float4 *>(out + c0 + e) =
-                    make_float4(__uint_as_float(r[e]), __uint_as_float(r[e + 1]),
-                                __uint_as_float(r[e + 2]), __uint_as_float(r[e + 3]));
-            } else {
-#pragma unroll
-              for (int e = 0; e < 16; ++e)
-                if (n0 + c0 + e < p.Cout) out[c0 + e] = __uint_as_float(r[e]);
-            }
-          }
+        for (int e = 0; e < 16; ++e) {
+          const int c = c0 + e;
+          const int u = tl.u0 + (c >> 3), v = tl.v0 + (c & 7);
+          if (co_ok && u < p.OU && v < p.OV)
+            ybase[((long long)u * p.ysu + (long long)v * p.ysv) * p.Cout] = __uint_as_float(r[e]);
         }
       }
       tc_fence_before();
@@ -603,7 +594,7 @@ int *status_ptr() {
 bool plan(TcParams &p, const View &v, int kind) {
   const int EB = (kind == K_TF32) ? 4 : 2;
   const int parts = (kind == K_BF16X3) ? 2 : 1;
-  p.BN = std::min(128, (v.Cout + 15) / 16 * 16);
+  p.BN = 128;  // output channels per tile = the MMA's M
   p.n_tiles = (v.Cout + p.BN - 1) / p.BN;
   p.T = v.KW * v.KU * v.KV;
   p.NH = 2;
@@ -632,7 +623,7 @@ bool plan(TcParams &p, const View &v, int kind) {
       if (nb < 2) continue;
       p.NB = nb;
       p.tmem_cols = 32;
-      while (p.tmem_cols < (unsigned)(2 * p.MH * p.BN)) p.tmem_cols <<= 1;
+      while (p.tmem_cols < (unsigned)(2 * p.MH * 128)) p.tmem_cols <<= 1;
       if (p.tmem_cols > 512) continue;
       return true;
     }
@@ -678,7 +669,7 @@ int run(int prec, const ConvGeom &g, bool bwd_input, const float *x, const float
   p.u_tiles = (v.OU + 16 * p.MH - 1) / (16 * p.MH);
   p.v_tiles = (v.OV + 7) / 8;
   p.total_tiles = (long long)v.B * v.OW * p.u_tiles * p.v_tiles * p.n_tiles;
-  p.idesc = instr_desc(kind == K_TF32 ? 2u : 1u, (uint32_t)p.BN);
+  p.idesc = instr_desc(kind == K_TF32 ? 2u : 1u, (uint32_t)(128 * p.MH));
   p.vec_in = ((uintptr_t)x % 16 == 0) && (v.Cin % 4 == 0);
   p.vec_out = ((uintptr_t)y % 16 == 0) && (v.Cout % 4 == 0);
   p.status = status_ptr();

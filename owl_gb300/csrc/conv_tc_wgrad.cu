@@ -3,7 +3,7 @@
 //
 //   dW[t][ci][co] = sum over output pixels p of X[p + off(t)][ci] * dY[p][co]
 //
-// Per tap this is a GEMM with M = ci (128 per MMA), N = co (BN), and the
+// Per tap this is a GEMM with M = ci (128 per MMA), N = co (BN <= 256), and the
 // reduction K running over output pixels.  Both operands are staged from the
 // float32 activations by producer warps in the same [16-byte channel chunk]
 // [pixel][16 B] layout as the forward kernel's halo.  Read MN-major, 8
@@ -427,7 +427,7 @@ int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, c
   if (planned) break;
   p.TU = tu;
   p.TP = tu * 8;
-  for (int bn : {128, 64, 32, 16}) {
+  for (int bn : {256, 128, 64, 32, 16}) {
     p.BN = std::min(bn, (p.Co + 15) / 16 * 16);
     for (int tg = std::min(p.T, 16); tg >= 1 && !planned; --tg) {
       if (p.T % tg != 0 || tg * p.BN > 512) continue;
