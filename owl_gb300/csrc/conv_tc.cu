@@ -140,7 +140,14 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
   uint64_t *drain = acc_empty + 2;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(drain + 1);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+  uint32_t *tap_off = tmem_slot + 2;  // per-tap start pixel in the halo (16-byte units)
 
+  for (int tap = threadIdx.x; tap < p.T; tap += blockDim.x) {
+    const int kv = tap % p.KV, ku = (tap / p.KV) % p.KU, kw = tap / (p.KV * p.KU);
+    const int qv = kv * p.dv;
+    tap_off[tap] =
+        (uint32_t)((kw * p.dw * p.HU + ku * p.du) * p.HV + (qv % p.sv) * p.HVR + qv / p.sv);
+  }
   if (threadIdx.x == 0) {
     for (int i = 0; i < p.NH; ++i) {
       mbar_init(smem_u32(&halo_full[i]), kProducerThreads);
@@ -313,6 +320,10 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
       const uint32_t a_lbo = (uint32_t)p.PS * 16, a_sbo = (uint32_t)(p.su * p.HV) * 16;
       const uint32_t b_lbo = (uint32_t)p.BN * 16;
       const int ksteps = p.NCH / 2;
+      // descriptor increments in 16-byte units
+      const uint64_t wd_ring = smem_desc(b0, b_lbo, 128);
+      const uint32_t wslot16 = (PARTS * p.b_bytes) >> 4, wstep16 = (2 * b_lbo) >> 4;
+      const uint32_t wlo16 = p.b_bytes >> 4, xstep16 = (2 * a_lbo) >> 4, xlo16 = p.halo_bytes >> 4;
       for (long long t = blockIdx.x; t < p.total_tiles; t += gridDim.x, ++tc) {
         const int abuf = tc & 1;
         const uint32_t aph = (uint32_t)((tc >> 1) & 1);
@@ -326,32 +337,28 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
           if (!wait_bar(smem_u32(&halo_full[hs]), (uint32_t)((kh / p.NH) & 1), abort_flag,
                         p.status)) { ok = false; break; }
           tc_fence_after();
-          const uint32_t hbase = halo0 + (uint32_t)hs * PARTS * p.halo_bytes;
+          // Descriptors advance by plain adds: the start-address field is the
+          // low 14 bits (16-byte units) and never carries out of them here.
+          const uint64_t xd_stage =
+              smem_desc(halo0 + (uint32_t)hs * PARTS * p.halo_bytes, a_lbo, a_sbo);
           for (int tap = 0; tap < p.T; ++tap, ++kb) {
             const int bs = (int)(kb % p.NB);
             if (!wait_bar(smem_u32(&b_full[bs]), (uint32_t)((kb / p.NB) & 1), abort_flag,
                           p.status)) { ok = false; break; }
             tc_fence_after();
-            const uint32_t wbase = b0 + (uint32_t)bs * PARTS * p.b_bytes;
-            const int kv = tap % p.KV, ku = (tap / p.KV) % p.KU, kw = tap / (p.KV * p.KU);
-            const int qv = kv * p.dv;
-            const int pix = (kw * p.dw * p.HU + ku * p.du) * p.HV + (qv % p.sv) * p.HVR + qv / p.sv;
+            const uint64_t wd0 = wd_ring + (uint64_t)(bs * wslot16);
+            const uint64_t xd0 = xd_stage + (uint64_t)tap_off[tap];
+#pragma unroll 4
             for (int s = 0; s < ksteps; ++s) {
-              // A: 128 output channels of this kernel tile (K-major)
-              const uint64_t wd = smem_desc(wbase + (uint32_t)(2 * s) * b_lbo, b_lbo, 128);
-              // B: the 16*MH groups of 8 output pixels, read out of the halo
-              const uint32_t xaddr = hbase + (uint32_t)(2 * s) * a_lbo + (uint32_t)pix * 16;
-              const uint64_t xd = smem_desc(xaddr, a_lbo, a_sbo);
+              const uint64_t wd = wd0 + (uint64_t)(s * wstep16);  // A: 128 output channels
+              const uint64_t xd = xd0 + (uint64_t)(s * xstep16);  // B: 16*MH groups of 8 pixels
               if (KIND == K_TF32) {
                 mma_tf32(d0, wd, xd, p.idesc, acc);
               } else {
                 mma_bf16(d0, wd, xd, p.idesc, acc);
                 if (KIND == K_BF16X3) {
-                  const uint64_t wd_lo =
-                      smem_desc(wbase + p.b_bytes + (uint32_t)(2 * s) * b_lbo, b_lbo, 128);
-                  const uint64_t xd_lo = smem_desc(xaddr + p.halo_bytes, a_lbo, a_sbo);
-                  mma_bf16(d0, wd_lo, xd, p.idesc, 1);
-                  mma_bf16(d0, wd, xd_lo, p.idesc, 1);
+                  mma_bf16(d0, wd + (uint64_t)wlo16, xd, p.idesc, 1);
+                  mma_bf16(d0, wd, xd + (uint64_t)xlo16, p.idesc, 1);
                 }
               }
               acc = 1;
@@ -616,7 +623,7 @@ bool plan(TcParams &p, const View &v, int kind) {
       p.PS = p.HP + (((1 - p.HP) % 8) + 8) % 8;  // plane stride = 1 (mod 8) pixels
       if (p.PS >= 16384 || p.HV >= 16384) continue;
       p.halo_bytes = (unsigned)p.PS * 16u * (unsigned)p.NCH;
-      long long fixed = (long long)p.NH * parts * p.halo_bytes + 512;
+      long long fixed = (long long)p.NH * parts * p.halo_bytes + 512 + 4LL * p.T;
       long long room = kSmemMax - fixed;
       if (room <= 0) continue;
       int nb = (int)std::min<long long>(8, room / ((long long)parts * p.b_bytes));
@@ -707,7 +714,7 @@ int run(int prec, const ConvGeom &g, bool bwd_input, const float *x, const float
     }
   }
   const size_t smem = (size_t)p.NH * parts * p.halo_bytes + (size_t)p.NB * parts * p.b_bytes +
-                      (2 * p.NH + 2 * p.NB + 5) * 8 + 16;
+                      (2 * p.NH + 2 * p.NB + 5) * 8 + 16 + 4 * (size_t)p.T;
   if (kind == K_TF32) rc = launch<K_TF32>(p, smem, s);
   else if (kind == K_BF16X3) rc = launch<K_BF16X3>(p, smem, s);
   else rc = launch<K_BF16>(p, smem, s);

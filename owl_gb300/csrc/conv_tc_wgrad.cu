@@ -155,6 +155,15 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
   uint64_t *drain = acc_full + 1;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(drain + 1);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+  uint32_t *tap_off = tmem_slot + 2;  // per-tap start pixel in the X halo (16-byte units)
+
+  for (int i = threadIdx.x; i < ntap; i += blockDim.x) {
+    const int tt = tap0 + i;
+    const int kv = tt % p.KV, ku = (tt / p.KV) % p.KU, kw = tt / (p.KV * p.KU);
+    const int qv = kv * p.dv - minv;
+    tap_off[i] = (uint32_t)(((kw * p.dw - minw) * HU + (ku * p.du - minu)) * HV +
+                            (qv % p.sv) * HVR + qv / p.sv);
+  }
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < p.NS; ++i) {
@@ -238,6 +247,7 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
       const uint32_t x0 = smem_u32(xs), y0 = smem_u32(ys);
       const uint32_t a_lbo = (uint32_t)(p.su * HV) * 16, a_sbo = (uint32_t)p.PS * 16;
       const uint32_t b_lbo = 128, b_sbo = (uint32_t)p.TP * 16;
+      const uint32_t xlo16 = p.x_bytes >> 4, ylo16 = p.y_bytes >> 4;
       long long k = 0;
       uint32_t acc = 0;
       bool ok = true;
@@ -248,29 +258,25 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
           break;
         }
         tc_fence_after();
-        const uint32_t xb = x0 + (uint32_t)st * PARTS * p.x_bytes;
-        const uint32_t yb = y0 + (uint32_t)st * PARTS * p.y_bytes;
-        for (int s = 0; s < p.TP / KSTEP_PIX; ++s) {
-          const int g0 = (s * KSTEP_PIX) >> 3;  // first u-group of this K step
-          const uint32_t baddr = yb + (uint32_t)(s * KSTEP_PIX) * 16;
-          const uint64_t bd = smem_desc(baddr, b_lbo, b_sbo);
-          const uint64_t bd_lo = smem_desc(baddr + p.y_bytes, b_lbo, b_sbo);
+        // descriptors advance by adds of 16-byte units (start-address field)
+        const uint64_t xd_st = smem_desc(x0 + (uint32_t)st * PARTS * p.x_bytes, a_lbo, a_sbo);
+        const uint64_t yd_st = smem_desc(y0 + (uint32_t)st * PARTS * p.y_bytes, b_lbo, b_sbo);
+        const int nks = p.TP / KSTEP_PIX;
+        for (int s = 0; s < nks; ++s) {
+          // K step s covers output pixels [s*KSTEP_PIX, +KSTEP_PIX): u-groups from g0
+          const int g0 = (s * KSTEP_PIX) >> 3;
+          const uint64_t bd = yd_st + (uint64_t)(s * KSTEP_PIX);
+          const uint64_t xs_ = xd_st + (uint64_t)(g0 * p.su * HV);
           for (int i = 0; i < ntap; ++i) {
-            const int tt = tap0 + i;
-            const int kv = tt % p.KV, ku = (tt / p.KV) % p.KU, kw = tt / (p.KV * p.KU);
-            const int qv = kv * p.dv - minv;
-            const int pix = ((kw * p.dw - minw) * HU + (ku * p.du - minu) + g0 * p.su) * HV +
-                            (qv % p.sv) * HVR + qv / p.sv;
-            const uint32_t aaddr = xb + (uint32_t)pix * 16;
-            const uint64_t ad = smem_desc(aaddr, a_lbo, a_sbo);
+            const uint64_t ad = xs_ + (uint64_t)tap_off[i];
             const uint32_t d = tmem_base + (uint32_t)(i * p.BN);
             if (KIND == K_TF32) {
               mma_tf32(d, ad, bd, p.idesc, acc);
             } else {
               mma_bf16(d, ad, bd, p.idesc, acc);
               if (KIND == K_BF16X3) {
-                mma_bf16(d, ad, bd_lo, p.idesc, 1);
-                mma_bf16(d, smem_desc(aaddr + p.x_bytes, a_lbo, a_sbo), bd, p.idesc, 1);
+                mma_bf16(d, ad, bd + (uint64_t)ylo16, p.idesc, 1);
+                mma_bf16(d, ad + (uint64_t)xlo16, bd, p.idesc, 1);
               }
             }
           }
@@ -491,7 +497,8 @@ int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, c
   } else {
     p.out = dw;
   }
-  const size_t smem = (size_t)p.NS * parts * (p.x_bytes + p.y_bytes) + (2 * p.NS + 2) * 8 + 16;
+  const size_t smem =
+      (size_t)p.NS * parts * (p.x_bytes + p.y_bytes) + (2 * p.NS + 2) * 8 + 16 + 4 * (size_t)p.TG;
   const int grid = (int)(units * p.R);
   int rc;
   if (kind == K_BF16X3) rc = launch<K_BF16X3>(p, smem, grid, s);
