@@ -67,7 +67,9 @@ struct TcParams {
   int HW, HU, HV, HVR, HP, PS;  // halo rows along w, u; pixels per u-row (= sv * HVR)
   int n_tiles, u_tiles, v_tiles;
   long long total_tiles;
-  unsigned halo_bytes, b_bytes;
+  unsigned halo_bytes, b_bytes;  // one halo stage / one weight slot (TPS taps), per part
+  unsigned tile_bytes;           // one tap's weight tile (BN x CB)
+  int TPS, NSL;                  // taps per weight slot, slots per channel block
   int NH, NB;
   unsigned idesc, tmem_cols;
   int vec_in, vec_out;
@@ -323,6 +325,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
       // descriptor increments in 16-byte units
       const uint64_t wd_ring = smem_desc(b0, b_lbo, 128);
       const uint32_t wslot16 = (PARTS * p.b_bytes) >> 4, wstep16 = (2 * b_lbo) >> 4;
+      const uint32_t tile16 = p.tile_bytes >> 4;
       const uint32_t wlo16 = p.b_bytes >> 4, xstep16 = (2 * a_lbo) >> 4, xlo16 = p.halo_bytes >> 4;
       for (long long t = blockIdx.x; t < p.total_tiles; t += gridDim.x, ++tc) {
         const int abuf = tc & 1;
@@ -341,27 +344,31 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
           // low 14 bits (16-byte units) and never carries out of them here.
           const uint64_t xd_stage =
               smem_desc(halo0 + (uint32_t)hs * PARTS * p.halo_bytes, a_lbo, a_sbo);
-          for (int tap = 0; tap < p.T; ++tap, ++kb) {
+          for (int sl = 0; sl < p.NSL; ++sl, ++kb) {
             const int bs = (int)(kb % p.NB);
             if (!wait_bar(smem_u32(&b_full[bs]), (uint32_t)((kb / p.NB) & 1), abort_flag,
                           p.status)) { ok = false; break; }
             tc_fence_after();
-            const uint64_t wd0 = wd_ring + (uint64_t)(bs * wslot16);
-            const uint64_t xd0 = xd_stage + (uint64_t)tap_off[tap];
+            const int t0 = sl * p.TPS, t1 = min(p.T, t0 + p.TPS);
+            const uint64_t wslot = wd_ring + (uint64_t)(bs * wslot16);
+            for (int tap = t0; tap < t1; ++tap) {
+              const uint64_t wd0 = wslot + (uint64_t)((tap - t0) * tile16);
+              const uint64_t xd0 = xd_stage + (uint64_t)tap_off[tap];
 #pragma unroll 4
-            for (int s = 0; s < ksteps; ++s) {
-              const uint64_t wd = wd0 + (uint64_t)(s * wstep16);  // A: 128 output channels
-              const uint64_t xd = xd0 + (uint64_t)(s * xstep16);  // B: 16*MH groups of 8 pixels
-              if (KIND == K_TF32) {
-                mma_tf32(d0, wd, xd, p.idesc, acc);
-              } else {
-                mma_bf16(d0, wd, xd, p.idesc, acc);
-                if (KIND == K_BF16X3) {
-                  mma_bf16(d0, wd + (uint64_t)wlo16, xd, p.idesc, 1);
-                  mma_bf16(d0, wd, xd + (uint64_t)xlo16, p.idesc, 1);
+              for (int s = 0; s < ksteps; ++s) {
+                const uint64_t wd = wd0 + (uint64_t)(s * wstep16);  // A: 128 output channels
+                const uint64_t xd = xd0 + (uint64_t)(s * xstep16);  // B: 16*MH pixel groups
+                if (KIND == K_TF32) {
+                  mma_tf32(d0, wd, xd, p.idesc, acc);
+                } else {
+                  mma_bf16(d0, wd, xd, p.idesc, acc);
+                  if (KIND == K_BF16X3) {
+                    mma_bf16(d0, wd + (uint64_t)wlo16, xd, p.idesc, 1);
+                    mma_bf16(d0, wd, xd + (uint64_t)xlo16, p.idesc, 1);
+                  }
                 }
+                acc = 1;
               }
-              acc = 1;
             }
             mma_commit(smem_u32(&b_empty[bs]));
           }
@@ -385,17 +392,22 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
       for (long long t = blockIdx.x; t < p.total_tiles; t += gridDim.x) {
         const Tile tl = decode_tile(p, t);
         for (int cb = 0; cb < p.NCB; ++cb)
-          for (int tap = 0; tap < p.T; ++tap, ++kb) {
+          for (int sl = 0; sl < p.NSL; ++sl, ++kb) {
             const int bs = (int)(kb % p.NB);
             if (!wait_bar(smem_u32(&b_empty[bs]), (uint32_t)(((kb / p.NB) & 1) ^ 1), abort_flag,
                           p.status))
               goto loader_done;
+            const int t0 = sl * p.TPS, nt_ = min(p.T - t0, p.TPS);
+            const uint32_t bytes = (uint32_t)nt_ * p.tile_bytes;
             const uint32_t bar = smem_u32(&b_full[bs]);
-            mbar_arrive_expect_tx(bar, PARTS * p.b_bytes);
-            const size_t src = ((size_t)(tl.nt * p.NCB + cb) * p.T + tap) * p.b_bytes;
+            mbar_arrive_expect_tx(bar, PARTS * bytes);
+            const size_t src = ((size_t)(tl.nt * p.NCB + cb) * p.T + t0) * p.tile_bytes;
             const uint32_t dst = b0 + (uint32_t)bs * PARTS * p.b_bytes;
-            bulk_g2s(dst, p.wt_hi + src, p.b_bytes, bar);
-            if (PARTS == 2) bulk_g2s(dst + p.b_bytes, p.wt_lo + src, p.b_bytes, bar);
+            for (uint32_t o = 0; o < bytes; o += 32768u) {
+              const uint32_t n = min(32768u, bytes - o);
+              bulk_g2s(dst + o, p.wt_hi + src + o, n, bar);
+              if (PARTS == 2) bulk_g2s(dst + p.b_bytes + o, p.wt_lo + src + o, n, bar);
+            }
           }
       }
     loader_done:
@@ -595,9 +607,10 @@ int *status_ptr() {
   return p[dev];
 }
 
-// Choose tile and pipeline sizes; false if no configuration fits.  Prefers
-// two M-halves and wide channel blocks, narrowing the channel block (fewer
-// bytes of K per halo stage) before giving up.
+// Choose tile and pipeline sizes; false if no configuration fits.
+// Priorities: two 128-pixel halves (N = 256) first; then the most MMA work
+// per weight slot (taps per slot x K steps per tap), since every slot costs
+// one tcgen05.commit; then the wider channel block.
 bool plan(TcParams &p, const View &v, int kind) {
   const int EB = (kind == K_TF32) ? 4 : 2;
   const int parts = (kind == K_BF16X3) ? 2 : 1;
@@ -606,36 +619,53 @@ bool plan(TcParams &p, const View &v, int kind) {
   p.T = v.KW * v.KU * v.KV;
   p.NH = 2;
   const int cb0 = std::min(128, (int)((v.Cin * EB + 31) / 32 * 32));
-  for (int mh = (v.OU > 16 ? 2 : 1); mh >= 1; --mh) {
+  bool found = false;
+  TcParams best = p;
+  long long best_score = -1;
+  for (int mh = (v.OU > 16 ? 2 : 1); mh >= 1 && !found; --mh) {
     for (int cb = cb0; cb >= 32; cb -= 32) {
       if (cb != cb0 && cb % 64 != 0 && cb != 32) continue;  // try cb0, then 64, 32
-      p.MH = mh;
-      p.CB = cb;
-      p.CPB = p.CB / EB;
-      p.NCH = p.CB / 16;
-      p.NCB = (v.Cin + p.CPB - 1) / p.CPB;
-      p.b_bytes = (unsigned)(p.BN * p.CB);
-      p.HW = (v.KW - 1) * v.dw + 1;
-      p.HU = (16 * mh - 1) * v.su + (v.KU - 1) * v.du + 1;
-      p.HVR = 8 + ((v.KV - 1) * v.dv) / v.sv;
-      p.HV = v.sv * p.HVR;
-      p.HP = p.HW * p.HU * p.HV;
-      p.PS = p.HP + (((1 - p.HP) % 8) + 8) % 8;  // plane stride = 1 (mod 8) pixels
-      if (p.PS >= 16384 || p.HV >= 16384) continue;
-      p.halo_bytes = (unsigned)p.PS * 16u * (unsigned)p.NCH;
-      long long fixed = (long long)p.NH * parts * p.halo_bytes + 512 + 4LL * p.T;
-      long long room = kSmemMax - fixed;
+      TcParams q = p;
+      q.MH = mh;
+      q.CB = cb;
+      q.CPB = q.CB / EB;
+      q.NCH = q.CB / 16;
+      q.NCB = (v.Cin + q.CPB - 1) / q.CPB;
+      q.tile_bytes = (unsigned)(q.BN * q.CB);
+      q.HW = (v.KW - 1) * v.dw + 1;
+      q.HU = (16 * mh - 1) * v.su + (v.KU - 1) * v.du + 1;
+      q.HVR = 8 + ((v.KV - 1) * v.dv) / v.sv;
+      q.HV = v.sv * q.HVR;
+      q.HP = q.HW * q.HU * q.HV;
+      q.PS = q.HP + (((1 - q.HP) % 8) + 8) % 8;  // plane stride = 1 (mod 8) pixels
+      if (q.PS >= 16384 || q.HV >= 16384) continue;
+      q.halo_bytes = (unsigned)q.PS * 16u * (unsigned)q.NCH;
+      const long long fixed = (long long)q.NH * parts * q.halo_bytes + 512 + 4LL * q.T;
+      const long long room = kSmemMax - fixed;
       if (room <= 0) continue;
-      int nb = (int)std::min<long long>(8, room / ((long long)parts * p.b_bytes));
-      if (nb < 2) continue;
-      p.NB = nb;
-      p.tmem_cols = 32;
-      while (p.tmem_cols < (unsigned)(2 * p.MH * 128)) p.tmem_cols <<= 1;
-      if (p.tmem_cols > 512) continue;
-      return true;
+      // at least two weight slots
+      const long long tps = std::min<long long>(q.T, room / (2LL * parts * q.tile_bytes));
+      if (tps < 1) continue;
+      q.TPS = (int)tps;
+      q.NSL = (q.T + q.TPS - 1) / q.TPS;
+      q.TPS = (q.T + q.NSL - 1) / q.NSL;  // balance the slots
+      q.b_bytes = (unsigned)q.TPS * q.tile_bytes;
+      q.NB = (int)std::min<long long>(4, room / ((long long)parts * q.b_bytes));
+      if (q.NB < 2) continue;
+      q.tmem_cols = 32;
+      while (q.tmem_cols < (unsigned)(2 * q.MH * 128)) q.tmem_cols <<= 1;
+      if (q.tmem_cols > 512) continue;
+      const long long score = (long long)q.TPS * (q.NCH / 2) * 4 + q.CB / 32;
+      if (score > best_score) {
+        best_score = score;
+        best = q;
+      }
     }
+    if (best_score >= 0) found = true;
   }
-  return false;
+  if (!found) return false;
+  p = best;
+  return true;
 }
 
 template <int KIND>
@@ -685,7 +715,7 @@ int run(int prec, const ConvGeom &g, bool bwd_input, const float *x, const float
     return kErrCuda;
   }
   const int parts = kind == K_BF16X3 ? 2 : 1;
-  const size_t wt_bytes = (size_t)p.n_tiles * p.NCB * p.T * p.b_bytes;
+  const size_t wt_bytes = (size_t)p.n_tiles * p.NCB * p.T * p.tile_bytes;
   void *wt = nullptr;
   int rc = scratch_alloc(&wt, wt_bytes * parts, s);
   if (rc) return rc;
