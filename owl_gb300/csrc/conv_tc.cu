@@ -44,11 +44,22 @@ namespace {
 
 using namespace ptx;
 
-constexpr int kProducerWarps = 8;
-constexpr int kMmaWarp = kProducerWarps;
-constexpr int kLoadWarp = kProducerWarps + 1;
-constexpr int kThreads = (kProducerWarps + 2 + 4) * 32;  // + MMA, loader, 4 epilogue warps
+// Warp roles.  A warp's scheduler (SM sub-partition) is warp_id % 4.  The
+// MMA warp (0) shares scheduler 0 only with the weight loader (4), an idle
+// warp (8) and one epilogue warp (12): every instruction another warp issues
+// there would delay the next tcgen05.mma.  The nine producer warps sit on
+// schedulers 1-3; the epilogue warps 12-15 cover TMEM lane quadrants 0-3.
+constexpr int kWarps = 16;
+constexpr int kThreads = kWarps * 32;
+constexpr int kMmaWarp = 0;
+constexpr int kLoadWarp = 4;
+constexpr int kEpiWarp0 = 12;
+constexpr int kProducerWarps = 9;
 constexpr int kProducerThreads = kProducerWarps * 32;
+// producer index of a warp (warps 1-3, 5-7, 9-11), or -1
+__device__ __forceinline__ int producer_index(int warp) {
+  return (warp & 3) != 0 && warp < 12 ? (warp >> 2) * 3 + (warp & 3) - 1 : -1;
+}
 constexpr int kSmemMax = 232448;  // 227 KB opt-in dynamic shared memory
 constexpr long long kSpinLimit = 4000000000LL;  // cycles (~2 s) before a wait gives up
 
@@ -176,7 +187,8 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
 
-  if (warp < kProducerWarps) {
+  const int pidx = producer_index(warp);
+  if (pidx >= 0) {
     // ===================== halo producers =====================
     // Each warp stages whole halo rows: a row is one (w, u, residue) line of
     // HVR pixels whose global addresses advance by a fixed step, so the row
@@ -195,7 +207,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
         if (!wait_bar(smem_u32(&halo_empty[hs]), ph ^ 1, abort_flag, p.status)) goto done;
         uint8_t *dst = halo + (size_t)hs * PARTS * p.halo_bytes;
         const int cbase = cb * p.CPB;
-        for (int r0 = warp * 2; r0 < nrows; r0 += 2 * kProducerWarps) {
+        for (int r0 = pidx * 2; r0 < nrows; r0 += 2 * kProducerWarps) {
           constexpr int kSlots = 3;  // slots per lane per row per pass
           float v[2][kSlots][EPC];
           int off[2][kSlots];
@@ -423,7 +435,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
         }
       }
     }
-  } else {
+  } else if (warp >= kEpiWarp0) {
     // ===================== epilogue =====================
     const int q = warp & 3;  // TMEM lane quadrant this warp may access
     int tc = 0;
@@ -608,9 +620,9 @@ int *status_ptr() {
 }
 
 // Choose tile and pipeline sizes; false if no configuration fits.
-// Priorities: two 128-pixel halves (N = 256) first; then the most MMA work
-// per weight slot (taps per slot x K steps per tap), since every slot costs
-// one tcgen05.commit; then the wider channel block.
+// Priorities: two 128-pixel halves (N = 256) first; then the widest channel
+// block (fewer, fuller halo stages for the producers); then the most taps per
+// weight slot (fewer barrier polls between MMAs).
 bool plan(TcParams &p, const View &v, int kind) {
   const int EB = (kind == K_TF32) ? 4 : 2;
   const int parts = (kind == K_BF16X3) ? 2 : 1;
@@ -655,7 +667,7 @@ bool plan(TcParams &p, const View &v, int kind) {
       q.tmem_cols = 32;
       while (q.tmem_cols < (unsigned)(2 * q.MH * 128)) q.tmem_cols <<= 1;
       if (q.tmem_cols > 512) continue;
-      const long long score = (long long)q.TPS * (q.NCH / 2) * 4 + q.CB / 32;
+      const long long score = (long long)q.CB * 1000 + (long long)q.TPS * (q.NCH / 2);
       if (score > best_score) {
         best_score = score;
         best = q;

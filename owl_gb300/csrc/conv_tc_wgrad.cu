@@ -31,10 +31,18 @@ namespace {
 
 using namespace ptx;
 
-constexpr int kProducerWarps = 8;
-constexpr int kMmaWarp = kProducerWarps;
-constexpr int kThreads = (kProducerWarps + 1 + 4) * 32;  // + MMA warp + 4 epilogue warps
+// Warp roles as in the forward kernel: MMA warp 0 keeps scheduler 0 nearly
+// to itself (warps 4 and 8 idle, epilogue warp 12), nine producer warps on
+// schedulers 1-3, epilogue warps 12-15 on TMEM lane quadrants 0-3.
+constexpr int kWarps = 16;
+constexpr int kThreads = kWarps * 32;
+constexpr int kMmaWarp = 0;
+constexpr int kEpiWarp0 = 12;
+constexpr int kProducerWarps = 9;
 constexpr int kProducerThreads = kProducerWarps * 32;
+__device__ __forceinline__ int producer_index(int warp) {
+  return (warp & 3) != 0 && warp < 12 ? (warp >> 2) * 3 + (warp & 3) - 1 : -1;
+}
 constexpr int kSmemMax = 232448;
 constexpr long long kSpinLimit = 4000000000LL;
 
@@ -184,7 +192,8 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
 
-  if (warp < kProducerWarps) {
+  const int pidx = producer_index(warp);
+  if (pidx >= 0) {
     // ===================== producers: X halo + dY tile =====================
     long long k = 0;
     for (long long t = t_begin; t < t_end; ++t, ++k) {
@@ -204,7 +213,7 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
         const int cb0 = mb * 128;
         stage::stage_rows<KIND, EPC, 6>(
             xd, p.x_bytes, (uint32_t)p.PS * 16, HW * HU * p.sv, HVR, XPL, p.Ci - cb0,
-            p.vec_x != 0, warp, kProducerWarps, lane, [&](int r) {
+            p.vec_x != 0, pidx, kProducerWarps, lane, [&](int r) {
               const int hr = r % p.sv, t3 = r / p.sv;
               const int hu = t3 % HU, hw = t3 / HU;
               const int iw = ow * p.sw - p.pw + minw + hw, iu = u0 * p.su - p.pu + minu + hu;
@@ -224,7 +233,7 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
       {
         const int cb0 = nb * p.BN;
         stage::stage_rows<KIND, EPC, 4>(
-            yd, p.y_bytes, (uint32_t)p.TP * 16, p.TU, 8, YPL, p.Co - cb0, p.vec_y != 0, warp,
+            yd, p.y_bytes, (uint32_t)p.TP * 16, p.TU, 8, YPL, p.Co - cb0, p.vec_y != 0, pidx,
             kProducerWarps, lane, [&](int r) {
               const int ou = u0 + r;
               stage::Row row;
@@ -290,7 +299,7 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
       while (!mbar_try_wait(smem_u32(drain), 0) && clock64() - t0 < kSpinLimit) {
       }
     }
-  } else {
+  } else if (warp >= kEpiWarp0) {
     // ===================== epilogue: TMEM -> partial dW =====================
     const int q = warp & 3;
     const int ci = mb * 128 + q * 32 + lane;
