@@ -179,7 +179,7 @@ def cpu_baseline(budget_s: float = 12.0, batch: int = 2):
             run_layer(O, x, w, dy, st, r, p)
         steps += 1
         el = time.perf_counter() - t0
-        if el >= budget_s or steps >= 50:
+        if el >= budget_s or steps >= 1000:
             break
     return {"value": flops_step * steps / el / 1e12, "unit": "TFLOP/s", "cores": cores,
             "kind": "port",
@@ -187,6 +187,33 @@ def cpu_baseline(budget_s: float = 12.0, batch: int = 2):
                       f"(of 64), float32, OpenBLAS {oracle.blas_path() and 'bundled'} "
                       f"threads={cores}, {el:.1f} s",
             "seconds": el}
+
+
+def accuracy(nn, precision, batch=2):
+    """max|gpu - f64| / max|f64| per layer and pass, on a batch-2 sample of
+    each layer: the GPU runs at `precision` on float32 data, the oracle in
+    float64 (Owl's D path restated) on the same values."""
+    import torch
+
+    import oracle
+    from owl_gb300.dense import NN
+
+    O = NN(oracle.OracleBackend(threads=os.cpu_count() or 1))
+    out = {}
+    worst = 0.0
+    for i, (name, xs, ks, st, r, p) in enumerate(LAYERS):
+        x, w, dy = make_inputs(xs, ks, st, r, p, seed=500 + i, batch=batch)
+        dev = [torch.from_numpy(a).cuda() for a in (x, w, dy)]
+        g = [t.cpu().numpy() for t in run_layer(nn, *dev, st, r, p)]
+        ref = run_layer(O, x.astype(np.float64), w.astype(np.float64), dy.astype(np.float64),
+                        st, r, p)
+        for op, a, b in zip(("fwd", "bwd_input", "bwd_kernel"), g, ref):
+            e = float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+            out[f"{name}.{op}"] = e
+            worst = max(worst, e)
+    out["max"] = worst
+    out["sample"] = f"batch {batch} of each layer; oracle float64"
+    return out
 
 
 def run_reference(args):
@@ -213,10 +240,12 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default=os.environ.get("OWLGPU_BENCH_PRECISION", "fp32"),
+    ap.add_argument("--precision", default=os.environ.get("OWLGPU_BENCH_PRECISION", "bf16"),
                     choices=["fp32", "tf32", "bf16", "bf16x3"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the FP32-plain comparison and the float64 error check")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -316,6 +345,28 @@ def main():
         "clocks": clk.summary(),
     }
 
+    # ---- the plain FP32 CUDA-core kernel on the same step, and accuracy ----
+    if not args.no_extras and rank == 0:
+        if args.precision != "fp32":
+            nn32 = NN(GpuBackend("fp32"))
+            def step32():
+                for (name, xs, ks, st, r, p), (x, w, dy) in zip(LAYERS, dev_data):
+                    run_layer(nn32, x, w, dy, st, r, p)
+            step32()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(2):
+                step32()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms32 = a.elapsed_time(b) / 2
+            result["fp32_plain"] = {"value": flops_step / (ms32 / 1e3) / 1e12, "unit": "TFLOP/s",
+                                    "ms_per_step": ms32,
+                                    "speedup": (flops_step / (ms_per_step / 1e3)) /
+                                               (flops_step / (ms32 / 1e3))}
+        result["error_vs_f64"] = accuracy(nn, args.precision)
+
     # ---- end to end through the host drop-in C ABI ----
     if not args.no_e2e and rank == 0:
         host_nn = NN(GpuBackend(args.precision))
@@ -344,7 +395,7 @@ def main():
                          "steps": e_steps, "api": "owl_float32_ndarray_conv_* host drop-in"}
 
     if rank == 0 and world == 1 and not args.no_cpu:
-        cb = cpu_baseline()
+        cb = cpu_baseline(budget_s=15.0)
         result["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
     if rank == 0:
         print(json.dumps(result), flush=True)
