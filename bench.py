@@ -216,6 +216,59 @@ def accuracy(nn, precision, batch=2):
     return out
 
 
+def bench_pool(reps: int = 20):
+    """Config-3 pooling on [4;32;32;32;64] float32: max/avg pool3d 2x2x2
+    stride 2 forward and backward, plus config-1 max_pool2d with argmax.
+    Each call is timed alone with CUDA events after a 256 MB write that
+    evicts L2 (the inputs are smaller than L2).  GB/s counts the algorithmic
+    bytes: read input + write output (+ argmax) for forward; read X + dY and
+    write dX for max backward; read dY and write dX for avg backward."""
+    import torch
+
+    from owl_gb300.dense import NN, GpuBackend
+
+    nn = NN(GpuBackend("fp32"))
+    hbm, _, src = peaks()
+    rng = np.random.default_rng(9)
+    x = torch.from_numpy(rng.uniform(-1, 1, (4, 32, 32, 32, 64)).astype(np.float32)).cuda()
+    y = nn.max_pool3d(x, [2, 2, 2], [2, 2, 2], "SAME")
+    dy = torch.from_numpy(rng.standard_normal(tuple(y.shape)).astype(np.float32)).cuda()
+    x2 = torch.from_numpy(rng.uniform(-1, 1, (8, 32, 32, 32)).astype(np.float32)).cuda()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    xb, yb = x.numel() * 4, y.numel() * 4
+    cases = [
+        ("max_pool3d", lambda: nn.max_pool3d(x, [2, 2, 2], [2, 2, 2], "SAME"), xb + yb),
+        ("avg_pool3d", lambda: nn.avg_pool3d(x, [2, 2, 2], [2, 2, 2], "SAME"), xb + yb),
+        ("max_pool3d_backward",
+         lambda: nn.max_pool3d_backward("SAME", x, [2, 2, 2], [2, 2, 2], dy), 2 * xb + yb),
+        ("avg_pool3d_backward",
+         lambda: nn.avg_pool3d_backward("SAME", x, [2, 2, 2], [2, 2, 2], dy), xb + yb),
+        ("max_pool2d_argmax c1",
+         lambda: nn.max_pool2d_argmax(x2, [2, 2], [2, 2], "SAME"),
+         x2.numel() * 4 + x2.numel() // 4 * (4 + 8)),
+    ]
+    out = {}
+    stream = torch.cuda.current_stream()
+    for name, fn, nbytes in cases:
+        fn()
+        ts = []
+        for _ in range(reps):
+            flush.fill_(1.0)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        ms = statistics.median(ts)
+        gbs = nbytes / (ms / 1e3) / 1e9
+        out[name] = {"us": ms * 1e3, "GB/s": gbs, "frac_hbm": gbs / hbm, "bytes": nbytes}
+    out["peak_GB/s"] = hbm
+    out["peak_source"] = f"{src} copy bandwidth"
+    out["note"] = "median of %d calls, L2 evicted before each" % reps
+    return out
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -366,6 +419,7 @@ def main():
                                     "speedup": (flops_step / (ms_per_step / 1e3)) /
                                                (flops_step / (ms32 / 1e3))}
         result["error_vs_f64"] = accuracy(nn, args.precision)
+        result["pool"] = bench_pool()
 
     # ---- end to end through the host drop-in C ABI ----
     if not args.no_e2e and rank == 0:
