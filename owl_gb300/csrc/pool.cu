@@ -17,16 +17,27 @@
 // consecutive channels (16-byte loads and stores when the channel count
 // allows) and a warp covers a contiguous run of channels and pixels.
 //
-// The backward pass is written in gather form: one thread per input element
-// (vector) visits the windows that contain it, in the same output order in
-// which Owl's scatter loop adds their contributions, so the float result is
-// identical to Owl's `+=` sequence without atomics.  A window in which no
-// element beats -inf routes its gradient to flat element 0 in Owl; that case
-// is detected (device flag) and element 0 is then rebuilt by an ordered
-// fix-up pass.
+// Every thread walks its window in chunks of eight taps, issuing the eight
+// vector loads before reducing them in scan order, so each thread keeps
+// several loads in flight (a pooling kernel is bound by HBM latency x
+// parallelism, not by arithmetic).  The reduction axis is the window, not
+// the contiguous channel axis, so no cross-lane shuffle is needed: a warp's
+// loads of one tap are one contiguous run of channels.
+//
+// Backward has two forms, both equal to Owl's zero-initialised `+=` scatter
+// bit for bit and without atomics:
+//   * windows that do not overlap (stride >= kernel in every dimension):
+//     one thread per window recomputes its winner and writes each element
+//     of the window's cell once (read X and dY once, write dX once);
+//   * overlapping windows: one thread per input element visits the windows
+//     that contain it in output order, the order of Owl's `+=` sequence.
+// A max window in which no element beats -inf routes its gradient to flat
+// element 0 in Owl; such windows are detected on the device and element 0
+// is then rebuilt by an ordered fix-up pass.
 #include "common.cuh"
 
 #include <algorithm>
+#include <atomic>
 
 namespace owlgpu {
 namespace {
@@ -40,6 +51,37 @@ PG to_pg(const PoolGeom &g) {
   PG p{g.B, g.IC, g.IR, g.ID, g.Ch, g.KC, g.KR, g.KD, g.OC, g.OR, g.OD,
        g.sc, g.sr, g.sd, g.pc, g.pr, g.pd};
   return p;
+}
+
+// Unsigned 32-bit division by a divisor fixed for the whole launch, by one
+// multiply-high, an add and a shift (Granlund & Montgomery, "Division by
+// invariant integers using multiplication", PLDI 1994, round-up variant):
+// with l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1,
+// n / d = (umulhi(m, n) + n) >> l for every n < 2^31.
+struct FastDiv {
+  uint32_t d, m, l;
+};
+
+FastDiv make_fastdiv(uint32_t d) {
+  uint32_t l = 0;
+  while ((1ull << l) < d) ++l;
+  const uint64_t m = (((1ull << l) - d) << 32) / d + 1;
+  return FastDiv{d, (uint32_t)m, l};
+}
+
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) {
+  return (__umulhi(f.m, n) + n) >> f.l;
+}
+
+// Output index -> (b, oc, or, od, channel vector) with channel vectors
+// innermost; valid while the output has fewer than 2^31 vectors.
+struct OutDecode {
+  FastDiv cv, od, orr, oc;
+};
+
+OutDecode make_out_decode(const PG &g, int64_t cv) {
+  return OutDecode{make_fastdiv((uint32_t)cv), make_fastdiv((uint32_t)g.OD),
+                   make_fastdiv((uint32_t)g.OR), make_fastdiv((uint32_t)g.OC)};
 }
 
 template <typename T, int V>
@@ -74,6 +116,99 @@ __device__ __forceinline__ void store_vec(T *p, const T (&v)[V]) {
   *reinterpret_cast<VT *>(p) = t;
 }
 
+// ---- window walking ------------------------------------------------------
+
+// In-range part of one window: [c0,c1) x [r0,r1) x [d0,d1); n taps.
+struct Box {
+  int c0, c1, r0, r1, d0, d1, nr, nd, n;
+};
+
+__device__ __forceinline__ Box window_box(const PG &g, int oc, int orr, int od) {
+  Box w;
+  const int cs = oc * g.sc - g.pc, rs = orr * g.sr - g.pr, ds = od * g.sd - g.pd;
+  w.c0 = max(cs, 0); w.c1 = min(cs + (int)g.KC, (int)g.IC);
+  w.r0 = max(rs, 0); w.r1 = min(rs + (int)g.KR, (int)g.IR);
+  w.d0 = max(ds, 0); w.d1 = min(ds + (int)g.KD, (int)g.ID);
+  const int nc = max(w.c1 - w.c0, 0);
+  w.nr = max(w.r1 - w.r0, 0);
+  w.nd = max(w.d1 - w.d0, 0);
+  w.n = nc * w.nr * w.nd;
+  return w;
+}
+
+// Walks a window's taps in Owl's scan order (cols, rows, dpts) U at a time:
+// all U loads of a chunk are issued before any is used, so a thread keeps U
+// vector loads in flight instead of one.
+struct Cursor {
+  int a, b, c;
+};
+
+template <typename T, int V, int U>
+__device__ __forceinline__ void load_chunk(const T *__restrict__ x, int64_t base, const PG &g,
+                                           const Box &w, Cursor &cur, int left,
+                                           T (&v)[U][V]) {
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    if (u < left) {
+      load_vec<T, V>(x + base + (((int64_t)cur.a * g.IR + cur.b) * g.ID + cur.c) * g.Ch, v[u]);
+      if (++cur.c == w.d1) {
+        cur.c = w.d0;
+        if (++cur.b == w.r1) { cur.b = w.r0; ++cur.a; }
+      }
+    }
+  }
+}
+
+// Max over the window with Owl's strict `<` (first maximum wins, NaN never
+// selected); bt = tap index of the winner in scan order, -1 if none.
+template <typename T, int V, int U>
+__device__ __forceinline__ void window_max(const T *__restrict__ x, int64_t base, const PG &g,
+                                           const Box &w, T (&best)[V], int (&bt)[V]) {
+#pragma unroll
+  for (int i = 0; i < V; ++i) { best[i] = T(-INFINITY); bt[i] = -1; }
+  Cursor cur{w.c0, w.r0, w.d0};
+  for (int t0 = 0; t0 < w.n; t0 += U) {
+    T v[U][V];
+    load_chunk<T, V, U>(x, base, g, w, cur, w.n - t0, v);
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (u < w.n - t0) {
+#pragma unroll
+        for (int i = 0; i < V; ++i)
+          if (best[i] < v[u][i]) { best[i] = v[u][i]; bt[i] = t0 + u; }
+      }
+  }
+}
+
+// Sum over the window in scan order, in the element type.
+template <typename T, int V, int U>
+__device__ __forceinline__ void window_sum(const T *__restrict__ x, int64_t base, const PG &g,
+                                           const Box &w, T (&acc)[V]) {
+#pragma unroll
+  for (int i = 0; i < V; ++i) acc[i] = T(0);
+  Cursor cur{w.c0, w.r0, w.d0};
+  for (int t0 = 0; t0 < w.n; t0 += U) {
+    T v[U][V];
+    load_chunk<T, V, U>(x, base, g, w, cur, w.n - t0, v);
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (u < w.n - t0) {
+#pragma unroll
+        for (int i = 0; i < V; ++i) acc[i] += v[u][i];
+      }
+  }
+}
+
+// Flat input offset (without the channel) of tap t of window w.
+__device__ __forceinline__ int64_t tap_offset(const PG &g, int64_t xbase, const Box &w, int t) {
+  const int per_c = w.nr * w.nd;
+  const int a = w.c0 + t / per_c, rem = t % per_c;
+  const int b = w.r0 + rem / w.nd, c = w.d0 + rem % w.nd;
+  return xbase + (((int64_t)a * g.IR + b) * g.ID + c) * g.Ch;
+}
+
+constexpr int kChunk = 8;
+
 // ---- forward --------------------------------------------------------------
 
 template <typename T, int V, int MODE, bool ARG>
@@ -84,52 +219,256 @@ __global__ void __launch_bounds__(256) pool_fwd_kernel(PG g, const T *__restrict
   const int64_t total = g.B * g.OC * g.OR * g.OD * CV;
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
-    int64_t cv = idx % CV, p = idx / CV;
-    int64_t od = p % g.OD, t = p / g.OD;
-    int64_t orr = t % g.OR; t /= g.OR;
-    int64_t oc = t % g.OC, b = t / g.OC;
+    const int64_t cv = idx % CV, p = idx / CV;
+    const int od = (int)(p % g.OD);
+    int64_t t = p / g.OD;
+    const int orr = (int)(t % g.OR); t /= g.OR;
+    const int oc = (int)(t % g.OC);
+    const int64_t b = t / g.OC;
     const int64_t xbase = b * g.IC * g.IR * g.ID * g.Ch;
-    const int cs = (int)(oc * g.sc) - g.pc, rs = (int)(orr * g.sr) - g.pr,
-              ds = (int)(od * g.sd) - g.pd;
-    T acc[V];
-    int64_t mi[V];
-#pragma unroll
-    for (int i = 0; i < V; ++i) {
-      acc[i] = MODE == POOL_MAX ? T(-INFINITY) : T(0);
-      mi[i] = -1;
-    }
-    int cnt = 0;
-    const int c0 = max(cs, 0), c1 = min(cs + (int)g.KC, (int)g.IC);
-    const int r0 = max(rs, 0), r1 = min(rs + (int)g.KR, (int)g.IR);
-    const int d0 = max(ds, 0), d1 = min(ds + (int)g.KD, (int)g.ID);
-    for (int a = c0; a < c1; ++a)
-      for (int bb = r0; bb < r1; ++bb)
-        for (int c = d0; c < d1; ++c) {
-          const int64_t off = xbase + (((int64_t)a * g.IR + bb) * g.ID + c) * g.Ch + cv * V;
-          T v[V];
-          load_vec<T, V>(x + off, v);
-#pragma unroll
-          for (int i = 0; i < V; ++i) {
-            if (MODE == POOL_MAX) {
-              if (acc[i] < v[i]) { acc[i] = v[i]; mi[i] = off + i; }
-            } else {
-              acc[i] += v[i];
-            }
-          }
-          ++cnt;
-        }
+    const Box w = window_box(g, oc, orr, od);
     T out[V];
+    if (MODE == POOL_MAX) {
+      int bt[V];
+      window_max<T, V, kChunk>(x, xbase + cv * V, g, w, out, bt);
+      if (ARG) {
 #pragma unroll
-    for (int i = 0; i < V; ++i) out[i] = MODE == POOL_MAX ? acc[i] : acc[i] / (T)cnt;
-    store_vec<T, V>(y + p * g.Ch + cv * V, out);
-    if (ARG) {
+        for (int i = 0; i < V; ++i)
+          argmax[p * g.Ch + cv * V + i] =
+              bt[i] < 0 ? -1 : tap_offset(g, xbase, w, bt[i]) + cv * V + i;
+      }
+    } else {
+      window_sum<T, V, kChunk>(x, xbase + cv * V, g, w, out);
 #pragma unroll
-      for (int i = 0; i < V; ++i) argmax[p * g.Ch + cv * V + i] = mi[i];
+      for (int i = 0; i < V; ++i) out[i] = out[i] / (T)w.n;
     }
+    store_vec<T, V>(y + p * g.Ch + cv * V, out);
   }
 }
 
-// ---- backward (gather form) ---------------------------------------------
+// ---- degenerate max windows ------------------------------------------------
+
+// A max window in which no element beats -inf (all -inf/NaN, or no in-range
+// element) routes its gradient to flat element 0 in Owl.  Kernels that meet
+// one raise this device-wide mark to their call's ticket with atomicMax; the
+// fix-up kernel of a call runs when the mark is at or above its own ticket.
+// Tickets grow monotonically, so a call never misses its own mark; a later
+// call's mark can only make an earlier call redo the (always exact) ordered
+// rebuild of dX[0].  No per-call memory is needed.
+__device__ unsigned long long g_degenerate_mark = 0;
+std::atomic<unsigned long long> g_ticket{0};
+
+__device__ __forceinline__ void raise_mark(unsigned long long ticket) {
+  atomicMax(&g_degenerate_mark, ticket);
+}
+
+// ---- backward, non-overlapping windows (scatter form) ---------------------
+
+// Per-dimension part of the input owned by output position o when s >= k:
+// [o*s - p, (o+1)*s - p) clipped to [0, I), the last position taking the
+// tail up to I.  These ranges partition [0, I) and each contains its window.
+__device__ __forceinline__ void cell_range(int o, int s, int p, int64_t O, int64_t I, int &lo,
+                                           int &hi) {
+  lo = min(max(o * s - p, 0), (int)I);
+  hi = o == (int)O - 1 ? (int)I : min(max((o + 1) * s - p, 0), (int)I);
+}
+
+// One thread per (window, channel vector): recompute the window's maximum
+// (or its count), then write every element of the window's cell exactly
+// once: 0 + dY at the winner, 0 + dY/count for average, 0 elsewhere.  With
+// s >= k every input element lies in at most one window, so this equals
+// Owl's zero-initialised `+=` scatter bit for bit.
+template <typename T, int V, int MODE>
+__global__ void __launch_bounds__(256) pool_bwd_cell_kernel(PG g, const T *__restrict__ x,
+                                                            const T *__restrict__ dy,
+                                                            T *__restrict__ dx,
+                                                            unsigned long long ticket) {
+  asm volatile("griddepcontrol.launch_dependents;");
+  const int64_t CV = g.Ch / V;
+  const int64_t total = g.B * g.OC * g.OR * g.OD * CV;
+  bool degen = false;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t cv = idx % CV, p = idx / CV;
+    const int od = (int)(p % g.OD);
+    int64_t t = p / g.OD;
+    const int orr = (int)(t % g.OR); t /= g.OR;
+    const int oc = (int)(t % g.OC);
+    const int64_t b = t / g.OC;
+    const int64_t xbase = b * g.IC * g.IR * g.ID * g.Ch;
+    const Box w = window_box(g, oc, orr, od);
+    T gv[V];
+    load_vec<T, V>(dy + p * g.Ch + cv * V, gv);
+    int bt[V];
+    if (MODE == POOL_MAX) {
+      T best[V];
+      window_max<T, V, kChunk>(x, xbase + cv * V, g, w, best, bt);
+#pragma unroll
+      for (int i = 0; i < V; ++i) degen |= bt[i] < 0;
+    } else {
+#pragma unroll
+      for (int i = 0; i < V; ++i) gv[i] = gv[i] / (T)w.n;
+    }
+    int alo, ahi, blo, bhi, clo, chi;
+    cell_range(oc, g.sc, g.pc, g.OC, g.IC, alo, ahi);
+    cell_range(orr, g.sr, g.pr, g.OR, g.IR, blo, bhi);
+    cell_range(od, g.sd, g.pd, g.OD, g.ID, clo, chi);
+    for (int a = alo; a < ahi; ++a)
+      for (int bb = blo; bb < bhi; ++bb)
+        for (int c = clo; c < chi; ++c) {
+          const bool in = a >= w.c0 && a < w.c1 && bb >= w.r0 && bb < w.r1 && c >= w.d0 &&
+                          c < w.d1;
+          const int tap = ((a - w.c0) * w.nr + (bb - w.r0)) * w.nd + (c - w.d0);
+          T o[V];
+#pragma unroll
+          for (int i = 0; i < V; ++i) {
+            if (MODE == POOL_MAX) o[i] = in && tap == bt[i] ? T(0) + gv[i] : T(0);
+            else o[i] = in ? T(0) + gv[i] : T(0);
+          }
+          store_vec<T, V>(dx + xbase + (((int64_t)a * g.IR + bb) * g.ID + c) * g.Ch + cv * V, o);
+        }
+  }
+  if (MODE == POOL_MAX && degen) raise_mark(ticket);
+}
+
+// ---- fixed-window fast paths ----------------------------------------------
+
+// Windows of compile-time size KC x KR x KD that lie wholly inside the input
+// (no padding, (O-1)*s + k <= I in every dimension): the taps are constant
+// strides apart, every tap of a window is loaded before the reduction, and
+// nothing is clipped.  Same scan order and comparisons as the general path.
+template <typename T, int V, int KC, int KR, int KD, int MODE, bool ARG>
+__global__ void __launch_bounds__(256) pool_fwd_fixed_kernel(PG g, OutDecode dec,
+                                                             const T *__restrict__ x,
+                                                             T *__restrict__ y,
+                                                             int64_t *__restrict__ argmax) {
+  constexpr int N = KC * KR * KD;
+  const uint32_t total = (uint32_t)(g.B * g.OC * g.OR * g.OD * (g.Ch / V));
+  const int64_t sd = g.Ch, sr = g.ID * g.Ch, sc = g.IR * g.ID * g.Ch;
+  for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += gridDim.x * blockDim.x) {
+    const uint32_t p32 = fdiv(idx, dec.cv);
+    const int64_t cv = idx - p32 * dec.cv.d, p = p32;
+    const uint32_t t1 = fdiv(p32, dec.od);
+    const int od = (int)(p32 - t1 * dec.od.d);
+    const uint32_t t2 = fdiv(t1, dec.orr);
+    const int orr = (int)(t1 - t2 * dec.orr.d);
+    const uint32_t t3 = fdiv(t2, dec.oc);
+    const int oc = (int)(t2 - t3 * dec.oc.d);
+    const int64_t b = t3;
+    const int64_t base = b * g.IC * sc + (int64_t)oc * g.sc * sc + (int64_t)orr * g.sr * sr +
+                         (int64_t)od * g.sd * sd + cv * V;
+    T v[N][V];
+#pragma unroll
+    for (int a = 0; a < KC; ++a)
+#pragma unroll
+      for (int bb = 0; bb < KR; ++bb)
+#pragma unroll
+        for (int c = 0; c < KD; ++c)
+          load_vec<T, V>(x + base + a * sc + bb * sr + c * sd, v[(a * KR + bb) * KD + c]);
+    T out[V];
+    if (MODE == POOL_MAX) {
+      int bt[V];
+#pragma unroll
+      for (int i = 0; i < V; ++i) { out[i] = T(-INFINITY); bt[i] = -1; }
+#pragma unroll
+      for (int u = 0; u < N; ++u)
+#pragma unroll
+        for (int i = 0; i < V; ++i)
+          if (out[i] < v[u][i]) { out[i] = v[u][i]; bt[i] = u; }
+      if (ARG) {
+#pragma unroll
+        for (int i = 0; i < V; ++i) {
+          const int a = bt[i] / (KR * KD), bb = bt[i] / KD % KR, c = bt[i] % KD;
+          argmax[p * g.Ch + cv * V + i] = bt[i] < 0 ? -1 : base + a * sc + bb * sr + c * sd + i;
+        }
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < V; ++i) out[i] = T(0);
+#pragma unroll
+      for (int u = 0; u < N; ++u)
+#pragma unroll
+        for (int i = 0; i < V; ++i) out[i] += v[u][i];
+#pragma unroll
+      for (int i = 0; i < V; ++i) out[i] = out[i] / (T)N;
+    }
+    store_vec<T, V>(y + p * g.Ch + cv * V, out);
+  }
+}
+
+// Backward for windows that tile the input exactly (stride = kernel, no
+// padding, O*s = I): each window is its own cell.
+template <typename T, int V, int KC, int KR, int KD, int MODE>
+__global__ void __launch_bounds__(256) pool_bwd_tile_kernel(PG g, OutDecode dec,
+                                                            const T *__restrict__ x,
+                                                            const T *__restrict__ dy,
+                                                            T *__restrict__ dx,
+                                                            unsigned long long ticket) {
+  asm volatile("griddepcontrol.launch_dependents;");
+  constexpr int N = KC * KR * KD;
+  const uint32_t total = (uint32_t)(g.B * g.OC * g.OR * g.OD * (g.Ch / V));
+  const int64_t sd = g.Ch, sr = g.ID * g.Ch, sc = g.IR * g.ID * g.Ch;
+  bool degen = false;
+  for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += gridDim.x * blockDim.x) {
+    const uint32_t p32 = fdiv(idx, dec.cv);
+    const int64_t cv = idx - p32 * dec.cv.d, p = p32;
+    const uint32_t t1 = fdiv(p32, dec.od);
+    const int od = (int)(p32 - t1 * dec.od.d);
+    const uint32_t t2 = fdiv(t1, dec.orr);
+    const int orr = (int)(t1 - t2 * dec.orr.d);
+    const uint32_t t3 = fdiv(t2, dec.oc);
+    const int oc = (int)(t2 - t3 * dec.oc.d);
+    const int64_t b = t3;
+    const int64_t base = b * g.IC * sc + (int64_t)oc * KC * sc + (int64_t)orr * KR * sr +
+                         (int64_t)od * KD * sd + cv * V;
+    T gv[V];
+    load_vec<T, V>(dy + p * g.Ch + cv * V, gv);
+    int bt[V];
+    if (MODE == POOL_MAX) {
+      T v[N][V];
+#pragma unroll
+      for (int a = 0; a < KC; ++a)
+#pragma unroll
+        for (int bb = 0; bb < KR; ++bb)
+#pragma unroll
+          for (int c = 0; c < KD; ++c)
+            load_vec<T, V>(x + base + a * sc + bb * sr + c * sd, v[(a * KR + bb) * KD + c]);
+      T best[V];
+#pragma unroll
+      for (int i = 0; i < V; ++i) { best[i] = T(-INFINITY); bt[i] = -1; }
+#pragma unroll
+      for (int u = 0; u < N; ++u)
+#pragma unroll
+        for (int i = 0; i < V; ++i)
+          if (best[i] < v[u][i]) { best[i] = v[u][i]; bt[i] = u; }
+#pragma unroll
+      for (int i = 0; i < V; ++i) degen |= bt[i] < 0;
+    } else {
+#pragma unroll
+      for (int i = 0; i < V; ++i) gv[i] = gv[i] / (T)N;
+    }
+#pragma unroll
+    for (int a = 0; a < KC; ++a)
+#pragma unroll
+      for (int bb = 0; bb < KR; ++bb)
+#pragma unroll
+        for (int c = 0; c < KD; ++c) {
+          const int u = (a * KR + bb) * KD + c;
+          T o[V];
+#pragma unroll
+          for (int i = 0; i < V; ++i) {
+            if (MODE == POOL_MAX) o[i] = bt[i] == u ? T(0) + gv[i] : T(0);
+            else o[i] = T(0) + gv[i];
+          }
+          store_vec<T, V>(dx + base + a * sc + bb * sr + c * sd, o);
+        }
+  }
+  if (MODE == POOL_MAX && degen) raise_mark(ticket);
+}
+
+// ---- backward, overlapping windows (gather form) ---------------------------
 
 // Range of output positions o whose window [o*s - p, o*s - p + k) contains i.
 __device__ __forceinline__ void win_range(int i, int s, int p, int k, int64_t O, int &lo,
@@ -142,24 +481,28 @@ __device__ __forceinline__ void win_range(int i, int s, int p, int k, int64_t O,
   if (hi > (int)O - 1) hi = (int)O - 1;
 }
 
+// One thread per input element (vector): visit the windows that contain it
+// in output order, the order in which Owl's scatter loop adds their
+// contributions, so the float sum is Owl's `+=` sequence without atomics.
 template <typename T, int V, int MODE>
-__global__ void __launch_bounds__(256) pool_bwd_kernel(PG g, const T *__restrict__ x,
-                                                       const T *__restrict__ dy,
-                                                       T *__restrict__ dx,
-                                                       int *__restrict__ degenerate) {
+__global__ void __launch_bounds__(256) pool_bwd_gather_kernel(PG g, const T *__restrict__ x,
+                                                              const T *__restrict__ dy,
+                                                              T *__restrict__ dx,
+                                                              unsigned long long ticket) {
+  asm volatile("griddepcontrol.launch_dependents;");
   const int64_t CV = g.Ch / V;
   const int64_t total = g.B * g.IC * g.IR * g.ID * CV;
+  bool degen = false;
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
-    int64_t cv = idx % CV, p = idx / CV;
-    int id = (int)(p % g.ID);
+    const int64_t cv = idx % CV, p = idx / CV;
+    const int id = (int)(p % g.ID);
     int64_t t = p / g.ID;
-    int ir = (int)(t % g.IR); t /= g.IR;
-    int ic = (int)(t % g.IC);
-    int64_t b = t / g.IC;
+    const int ir = (int)(t % g.IR); t /= g.IR;
+    const int ic = (int)(t % g.IC);
+    const int64_t b = t / g.IC;
     const int64_t xbase = b * g.IC * g.IR * g.ID * g.Ch;
     const int64_t ybase = b * g.OC * g.OR * g.OD * g.Ch;
-    const int64_t my_off = xbase + (((int64_t)ic * g.IR + ir) * g.ID + id) * g.Ch + cv * V;
     int oc0, oc1, or0, or1, od0, od1;
     win_range(ic, g.sc, g.pc, (int)g.KC, g.OC, oc0, oc1);
     win_range(ir, g.sr, g.pr, (int)g.KR, g.OR, or0, or1);
@@ -167,59 +510,49 @@ __global__ void __launch_bounds__(256) pool_bwd_kernel(PG g, const T *__restrict
     T acc[V];
 #pragma unroll
     for (int i = 0; i < V; ++i) acc[i] = T(0);
-    bool degen = false;
     for (int oc = oc0; oc <= oc1; ++oc)
       for (int orr = or0; orr <= or1; ++orr)
         for (int od = od0; od <= od1; ++od) {
-          const int cs = oc * g.sc - g.pc, rs = orr * g.sr - g.pr, ds = od * g.sd - g.pd;
-          const int c0 = max(cs, 0), c1 = min(cs + (int)g.KC, (int)g.IC);
-          const int r0 = max(rs, 0), r1 = min(rs + (int)g.KR, (int)g.IR);
-          const int d0 = max(ds, 0), d1 = min(ds + (int)g.KD, (int)g.ID);
+          const Box w = window_box(g, oc, orr, od);
           T gv[V];
           load_vec<T, V>(dy + ybase + (((int64_t)oc * g.OR + orr) * g.OD + od) * g.Ch + cv * V,
                          gv);
           if (MODE == POOL_AVG) {
-            const int cnt = (c1 - c0) * (r1 - r0) * (d1 - d0);
 #pragma unroll
-            for (int i = 0; i < V; ++i) acc[i] += gv[i] / (T)cnt;
+            for (int i = 0; i < V; ++i) acc[i] += gv[i] / (T)w.n;
           } else {
             T best[V];
-            int64_t bi[V];
-#pragma unroll
-            for (int i = 0; i < V; ++i) { best[i] = T(-INFINITY); bi[i] = -1; }
-            for (int a = c0; a < c1; ++a)
-              for (int bb = r0; bb < r1; ++bb)
-                for (int c = d0; c < d1; ++c) {
-                  const int64_t off =
-                      xbase + (((int64_t)a * g.IR + bb) * g.ID + c) * g.Ch + cv * V;
-                  T v[V];
-                  load_vec<T, V>(x + off, v);
-#pragma unroll
-                  for (int i = 0; i < V; ++i)
-                    if (best[i] < v[i]) { best[i] = v[i]; bi[i] = off; }
-                }
+            int bt[V];
+            window_max<T, V, kChunk>(x, xbase + cv * V, g, w, best, bt);
+            const int mine = ((ic - w.c0) * w.nr + (ir - w.r0)) * w.nd + (id - w.d0);
 #pragma unroll
             for (int i = 0; i < V; ++i) {
-              if (bi[i] < 0) degen = true;
-              else if (bi[i] == my_off) acc[i] += gv[i];
+              if (bt[i] < 0) degen = true;
+              else if (bt[i] == mine) acc[i] += gv[i];
             }
           }
         }
-    store_vec<T, V>(dx + my_off, acc);
-    if (MODE == POOL_MAX && degen) atomicOr(degenerate, 1);
+    store_vec<T, V>(dx + xbase + (((int64_t)ic * g.IR + ir) * g.ID + id) * g.Ch + cv * V, acc);
   }
+  if (MODE == POOL_MAX && degen) raise_mark(ticket);
 }
 
 // Ordered rebuild of dX[0] for max-pool backward when some window selected
 // nothing (Owl routes those windows to flat element 0, owl_ndarray_pool_impl.h
 // :167).  One block walks all windows in Owl's loop order (b, oc, or, od,
 // ch), 1024 at a time; contributions are summed by one thread in order.
+// Runs only when this call's ticket is marked (or `force`: some window has
+// no in-range element, which the gather form never visits).
 template <typename T>
 __global__ void __launch_bounds__(1024) pool_max_fix0_kernel(PG g, const T *__restrict__ x,
                                                              const T *__restrict__ dy,
                                                              T *__restrict__ dx,
-                                                             const int *__restrict__ flag) {
-  if (*flag == 0) return;
+                                                             unsigned long long ticket,
+                                                             int force) {
+  // Launched as a programmatic dependent of the backward kernel: wait for
+  // that grid to finish and its writes to become visible.
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  if (!force && *(volatile unsigned long long *)&g_degenerate_mark < ticket) return;
   __shared__ T contrib[1024];
   __shared__ int hit[1024];
   const int64_t total = g.B * g.OC * g.OR * g.OD * g.Ch;
@@ -273,15 +606,70 @@ int vec_width(int64_t ch, const void *a, const void *b, const void *c) {
   return 1;
 }
 
+// Every window lies wholly inside the input: no padding and the last
+// window ends at or before the input's end, in every dimension.
+bool interior(const PG &g) {
+  auto ok = [](int64_t I, int64_t K, int64_t O, int s, int p) {
+    return p == 0 && (O - 1) * s + K <= I;
+  };
+  return ok(g.IC, g.KC, g.OC, g.sc, g.pc) && ok(g.IR, g.KR, g.OR, g.sr, g.pr) &&
+         ok(g.ID, g.KD, g.OD, g.sd, g.pd);
+}
+
+// Windows tile the input exactly: stride = kernel, no padding, O*s = I.
+bool exact_tiling(const PG &g) {
+  auto ok = [](int64_t I, int64_t K, int64_t O, int s, int p) {
+    return p == 0 && s == K && O * s == I;
+  };
+  return ok(g.IC, g.KC, g.OC, g.sc, g.pc) && ok(g.IR, g.KR, g.OR, g.sr, g.pr) &&
+         ok(g.ID, g.KD, g.OD, g.sd, g.pd);
+}
+
+bool window_is(const PG &g, int kc, int kr, int kd) {
+  return g.KC == kc && g.KR == kr && g.KD == kd;
+}
+
+template <typename T, int V, int KC, int KR, int KD>
+void fwd_fixed(const PG &g, PoolMode mode, const T *x, T *y, int64_t *arg, int grid,
+               cudaStream_t s) {
+  const OutDecode d = make_out_decode(g, g.Ch / V);
+  if (mode == POOL_AVG)
+    pool_fwd_fixed_kernel<T, V, KC, KR, KD, POOL_AVG, false>
+        <<<grid, 256, 0, s>>>(g, d, x, y, nullptr);
+  else if (arg)
+    pool_fwd_fixed_kernel<T, V, KC, KR, KD, POOL_MAX, true><<<grid, 256, 0, s>>>(g, d, x, y, arg);
+  else
+    pool_fwd_fixed_kernel<T, V, KC, KR, KD, POOL_MAX, false>
+        <<<grid, 256, 0, s>>>(g, d, x, y, nullptr);
+}
+
+// The fixed-window kernels index outputs with 32-bit fast division.
+bool small_output(const PG &g, int V) {
+  return g.B * g.OC * g.OR * g.OD * (g.Ch / V) < (int64_t(1) << 31);
+}
+
+// Fixed-window kernels exist for the widest vector of each type (16 bytes)
+// and the common window shapes 2x2, 3x3 and 2x2x2.
+template <typename T>
+constexpr int kWide = sizeof(T) == 4 ? 4 : 2;
+
 template <typename T, int V>
 int fwd_launch(const PG &g, PoolMode mode, const T *x, T *y, int64_t *arg, cudaStream_t s) {
   int grid = grid_for(g.B * g.OC * g.OR * g.OD * (g.Ch / V));
-  if (mode == POOL_AVG)
+  const bool fixed = V == kWide<T> && interior(g) && small_output(g, V);
+  if (fixed && window_is(g, 2, 2, 1)) {
+    fwd_fixed<T, V, 2, 2, 1>(g, mode, x, y, arg, grid, s);
+  } else if (fixed && window_is(g, 3, 3, 1)) {
+    fwd_fixed<T, V, 3, 3, 1>(g, mode, x, y, arg, grid, s);
+  } else if (fixed && window_is(g, 2, 2, 2)) {
+    fwd_fixed<T, V, 2, 2, 2>(g, mode, x, y, arg, grid, s);
+  } else if (mode == POOL_AVG) {
     pool_fwd_kernel<T, V, POOL_AVG, false><<<grid, 256, 0, s>>>(g, x, y, nullptr);
-  else if (arg)
+  } else if (arg) {
     pool_fwd_kernel<T, V, POOL_MAX, true><<<grid, 256, 0, s>>>(g, x, y, arg);
-  else
+  } else {
     pool_fwd_kernel<T, V, POOL_MAX, false><<<grid, 256, 0, s>>>(g, x, y, nullptr);
+  }
   OWL_CHECK_LAUNCH("pool_fwd_kernel");
   return kOk;
 }
@@ -291,20 +679,49 @@ int fwd_t(const PoolGeom &pg, PoolMode mode, const T *x, T *y, int64_t *arg, cud
   PG g = to_pg(pg);
   if (pg.y_elems() == 0) return kOk;
   int v = vec_width<T>(g.Ch, x, y, y);
-  if (v == 4) return fwd_launch<T, (sizeof(T) == 4 ? 4 : 1)>(g, mode, x, y, arg, s);
+  if (v == 4) return fwd_launch<T, kWide<T>>(g, mode, x, y, arg, s);
   if (v == 2) return fwd_launch<T, 2>(g, mode, x, y, arg, s);
   return fwd_launch<T, 1>(g, mode, x, y, arg, s);
 }
 
-template <typename T, int V>
-int bwd_launch(const PG &g, PoolMode mode, const T *x, const T *dy, T *dx, int *flag,
-               cudaStream_t s) {
-  int grid = grid_for(g.B * g.IC * g.IR * g.ID * (g.Ch / V));
+// Windows overlap in no dimension: every input element lies in at most one.
+bool non_overlapping(const PG &g) { return g.sc >= g.KC && g.sr >= g.KR && g.sd >= g.KD; }
+
+template <typename T, int V, int KC, int KR, int KD>
+void bwd_tile(const PG &g, PoolMode mode, const T *x, const T *dy, T *dx,
+              unsigned long long ticket, int grid, cudaStream_t s) {
+  const OutDecode d = make_out_decode(g, g.Ch / V);
   if (mode == POOL_AVG)
-    pool_bwd_kernel<T, V, POOL_AVG><<<grid, 256, 0, s>>>(g, x, dy, dx, flag);
+    pool_bwd_tile_kernel<T, V, KC, KR, KD, POOL_AVG>
+        <<<grid, 256, 0, s>>>(g, d, x, dy, dx, ticket);
   else
-    pool_bwd_kernel<T, V, POOL_MAX><<<grid, 256, 0, s>>>(g, x, dy, dx, flag);
-  OWL_CHECK_LAUNCH("pool_bwd_kernel");
+    pool_bwd_tile_kernel<T, V, KC, KR, KD, POOL_MAX>
+        <<<grid, 256, 0, s>>>(g, d, x, dy, dx, ticket);
+}
+
+template <typename T, int V>
+int bwd_launch(const PG &g, PoolMode mode, const T *x, const T *dy, T *dx,
+               unsigned long long ticket, cudaStream_t s) {
+  if (non_overlapping(g)) {
+    int grid = grid_for(g.B * g.OC * g.OR * g.OD * (g.Ch / V));
+    const bool tile = V == kWide<T> && exact_tiling(g) && small_output(g, V);
+    if (tile && window_is(g, 2, 2, 1))
+      bwd_tile<T, V, 2, 2, 1>(g, mode, x, dy, dx, ticket, grid, s);
+    else if (tile && window_is(g, 2, 2, 2))
+      bwd_tile<T, V, 2, 2, 2>(g, mode, x, dy, dx, ticket, grid, s);
+    else if (mode == POOL_AVG)
+      pool_bwd_cell_kernel<T, V, POOL_AVG><<<grid, 256, 0, s>>>(g, x, dy, dx, ticket);
+    else
+      pool_bwd_cell_kernel<T, V, POOL_MAX><<<grid, 256, 0, s>>>(g, x, dy, dx, ticket);
+    OWL_CHECK_LAUNCH("pool_bwd_cell_kernel");
+  } else {
+    int grid = grid_for(g.B * g.IC * g.IR * g.ID * (g.Ch / V));
+    if (mode == POOL_AVG)
+      pool_bwd_gather_kernel<T, V, POOL_AVG><<<grid, 256, 0, s>>>(g, x, dy, dx, ticket);
+    else
+      pool_bwd_gather_kernel<T, V, POOL_MAX><<<grid, 256, 0, s>>>(g, x, dy, dx, ticket);
+    OWL_CHECK_LAUNCH("pool_bwd_gather_kernel");
+  }
   return kOk;
 }
 
@@ -329,26 +746,29 @@ int bwd_t(const PoolGeom &pg, PoolMode mode, const T *x, const T *dy, T *dx, cud
     OWL_CUDA(cudaMemsetAsync(dx, 0, sizeof(T) * pg.x_elems(), s));
     return kOk;
   }
-  int *flag = nullptr;
-  if (mode == POOL_MAX) {
-    int rc = scratch_alloc((void **)&flag, sizeof(int), s);
-    if (rc) return rc;
-    int init = has_empty_window(g) ? 1 : 0;
-    cudaError_t e = cudaMemsetAsync(flag, init, sizeof(int), s);
-    if (e != cudaSuccess) { scratch_free(flag, s); return cuda_fail(e, "cudaMemsetAsync"); }
-  }
+  const unsigned long long ticket = ++g_ticket;
   int v = vec_width<T>(g.Ch, x ? (const void *)x : (const void *)dy, dy, dx);
   int rc;
-  if (v == 4) rc = bwd_launch<T, (sizeof(T) == 4 ? 4 : 1)>(g, mode, x, dy, dx, flag, s);
-  else if (v == 2) rc = bwd_launch<T, 2>(g, mode, x, dy, dx, flag, s);
-  else rc = bwd_launch<T, 1>(g, mode, x, dy, dx, flag, s);
+  if (v == 4) rc = bwd_launch<T, kWide<T>>(g, mode, x, dy, dx, ticket, s);
+  else if (v == 2) rc = bwd_launch<T, 2>(g, mode, x, dy, dx, ticket, s);
+  else rc = bwd_launch<T, 1>(g, mode, x, dy, dx, ticket, s);
   if (rc == kOk && mode == POOL_MAX) {
-    pool_max_fix0_kernel<T><<<1, 1024, 0, s>>>(g, x, dy, dx, flag);
-    cudaError_t e = cudaGetLastError();
+    const int force = has_empty_window(g) ? 1 : 0;
+    // Programmatic dependent launch: the fix-up grid is scheduled while the
+    // backward grid drains and waits on it with griddepcontrol.wait.
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(1);
+    cfg.blockDim = dim3(1024);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, pool_max_fix0_kernel<T>, g, x, dy, dx, ticket, force);
     note_launch();
     if (e != cudaSuccess) rc = cuda_fail(e, "pool_max_fix0_kernel");
   }
-  if (flag) scratch_free(flag, s);
   return rc;
 }
 

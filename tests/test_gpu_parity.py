@@ -106,7 +106,15 @@ def test_conv3d_family(gpu_nn, oracle_nn, dt, case):
 
 POOL2D = [((2, 7, 9, 5), (2, 3), (1, 2), SAME), ((2, 8, 8, 4), (2, 2), (2, 2), VALID),
           ((1, 5, 6, 3), (3, 3), (2, 2), SAME), ((1, 4, 4, 1), (4, 4), (1, 1), SAME),
-          ((3, 16, 12, 64), (3, 3), (1, 1), SAME), ((2, 9, 11, 6), (3, 2), (2, 3), VALID)]
+          ((3, 16, 12, 64), (3, 3), (1, 1), SAME), ((2, 9, 11, 6), (3, 2), (2, 3), VALID),
+          # non-overlapping windows: cells wider than windows, padded first
+          # cell, ragged tail, 16-byte channel vectors
+          ((2, 9, 10, 5), (2, 2), (3, 3), VALID), ((1, 4, 7, 3), (3, 3), (3, 3), SAME),
+          ((2, 10, 10, 64), (2, 2), (2, 2), SAME), ((1, 11, 5, 8), (1, 2), (3, 2), SAME),
+          # interior windows of the fixed-size kernels (2x2, 3x3), overlapping
+          # and not
+          ((2, 9, 11, 8), (3, 3), (2, 2), VALID), ((2, 7, 6, 12), (2, 2), (1, 1), VALID),
+          ((1, 12, 10, 16), (3, 3), (3, 3), VALID)]
 
 
 @pytest.mark.parametrize("dt", [np.float32, np.float64])
@@ -131,7 +139,8 @@ def test_pool2d_bit_exact(gpu_nn, oracle_nn, dt, case):
 
 
 POOL3D = [((2, 5, 4, 6, 3), (2, 2, 3), (1, 2, 1), SAME), ((1, 6, 6, 4, 2), (2, 2, 2), (2, 2, 2), VALID),
-          ((1, 5, 5, 5, 4), (3, 2, 2), (2, 1, 2), SAME), ((2, 8, 8, 8, 64), (2, 2, 2), (2, 2, 2), SAME)]
+          ((1, 5, 5, 5, 4), (3, 2, 2), (2, 1, 2), SAME), ((2, 8, 8, 8, 64), (2, 2, 2), (2, 2, 2), SAME),
+          ((1, 7, 5, 9, 6), (2, 2, 3), (3, 2, 3), VALID), ((1, 4, 7, 5, 2), (3, 3, 2), (3, 3, 2), SAME)]
 
 
 @pytest.mark.parametrize("dt", [np.float32, np.float64])
@@ -166,17 +175,42 @@ def test_config1_full_size(gpu_nn, oracle_nn):
     assert np.array_equal(p_g, p_o) and np.array_equal(i_g, i_o)
 
 
-def test_degenerate_windows_match_owl(gpu_nn, oracle_nn):
-    x = np.full((1, 4, 4, 2), -np.inf, dtype=np.float32)
+@pytest.mark.parametrize("ch", [2, 4])
+def test_degenerate_windows_match_owl(gpu_nn, oracle_nn, ch):
+    x = np.full((1, 4, 4, ch), -np.inf, dtype=np.float32)
     x[0, 0, 0, 0] = 1.0
     x[0, 3, 3, 1] = np.nan
-    g = np.arange(1, 9, dtype=np.float32).reshape(1, 2, 2, 2)
+    g = np.arange(1, 4 * ch + 1, dtype=np.float32).reshape(1, 2, 2, ch)
     a = oracle_nn.max_pool2d_backward("VALID", x, [2, 2], [2, 2], g)
     b = from_dev(gpu_nn.max_pool2d_backward("VALID", to_dev(x), [2, 2], [2, 2], to_dev(g)))
     assert np.array_equal(a, b)
     pa, ia = oracle_nn.max_pool2d_argmax(x, [2, 2], [2, 2], "VALID")
     pb, ib = gpu_nn.max_pool2d_argmax(x, [2, 2], [2, 2], "VALID")
     assert np.array_equal(pa, pb) and np.array_equal(ia, ib)
+
+
+@pytest.mark.parametrize("k,st", [((2, 2), (2, 2)), ((3, 3), (1, 1)), ((3, 2), (2, 3))])
+def test_degenerate_windows_ordered(gpu_nn, oracle_nn, k, st):
+    """Many windows that select nothing (all -inf or NaN), spread over the
+    tensor, in both backward forms: their gradients are summed into element
+    0 in Owl's window order."""
+    rng = np.random.default_rng(17)
+    x = rng.uniform(-1, 1, (2, 9, 8, 6)).astype(np.float32)
+    x[:, 2:7, 1:6, :] = -np.inf
+    x[1, 4:8, 3:5, 2:4] = np.nan
+    y = oracle_nn.max_pool2d(x, list(k), list(st), SAME)
+    g = rng.standard_normal(y.shape).astype(np.float32)
+    a = oracle_nn.max_pool2d_backward(SAME, x, list(k), list(st), g)
+    b = from_dev(gpu_nn.max_pool2d_backward(SAME, to_dev(x), list(k), list(st), to_dev(g)))
+    assert np.array_equal(a, b)
+    for c3 in (3, 4):
+        x3 = np.full((1, 4, 4, 4, c3), -np.inf, dtype=np.float64)
+        x3[0, 1, 2, 3, 1] = 0.5
+        g3 = np.arange(1, 8 * c3 + 1, dtype=np.float64).reshape(1, 2, 2, 2, c3)
+        a3 = oracle_nn.max_pool3d_backward("VALID", x3, [2, 2, 2], [2, 2, 2], g3)
+        b3 = from_dev(gpu_nn.max_pool3d_backward("VALID", to_dev(x3), [2, 2, 2], [2, 2, 2],
+                                                 to_dev(g3)))
+        assert np.array_equal(a3, b3)
 
 
 def test_repeat_calls_are_deterministic(gpu_nn):
