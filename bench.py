@@ -97,6 +97,24 @@ def layer_calls(nn, x, w, dy, stride, rate, pad):
             ("bwd_kernel", lambda: nn.conv2d_backward_kernel(x, w, st, dy))]
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
+# the BF16 kernel, from one ncu capture of `python bench.py --case ...`
+# (the summaries under profiles/ hold the commands and the other counters).
+# Output lines still in the write-back L2 when a kernel ends are not counted.
+NCU_TRAFFIC = {
+    "L1.fwd": (103_144_448 + 47_627_520, "profiles/conv2d_l1_fwd_bf16_ncu.md"),
+    "L1.bwd_kernel": (208_301_056 + 3_362_816, "profiles/conv2d_l1_bwdk_bf16_ncu.md"),
+    "L2.bwd_input": (42_216_448 + 3_456_000, "profiles/conv2d_l2_bwdi_bf16_ncu.md"),
+}
+# Algorithmic bytes of the same calls: float32 operands read once, result
+# written once.  L1: X and Y/dY [64;56;56;128] (102.8 MB each), W
+# [3;3;128;128] (0.59 MB).
+ALGO_BYTES = {
+    "L1.fwd": 2 * 64 * 56 * 56 * 128 * 4 + 3 * 3 * 128 * 128 * 4,
+    "L1.bwd_kernel": 2 * 64 * 56 * 56 * 128 * 4 + 3 * 3 * 128 * 128 * 4,
+}
+
+
 def peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -105,8 +123,72 @@ def peaks():
     return 6800.0, 1900.0, "fallback"
 
 
+class _Nvml:
+    """Read-only NVML queries through ctypes (libnvidia-ml ships with the
+    driver): SM clock, its maximum, and the active clock-event reasons."""
+
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, index: int, props=None):
+        import ctypes
+
+        self.c = ctypes
+        self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        bus = None
+        if props is not None:
+            bus = "%08x:%02x:%02x.0" % (props.pci_domain_id, props.pci_bus_id,
+                                         props.pci_device_id)
+        rc = (self.lib.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), ctypes.byref(self.h))
+              if bus else 1)
+        if rc != 0 and self.lib.nvmlDeviceGetHandleByIndex_v2(
+                index, ctypes.byref(self.h)) != 0:
+            raise OSError("no NVML handle for the device")
+        self.reasons_fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+
+    def sm_mhz(self) -> int:
+        v = self.c.c_uint()
+        self.lib.nvmlDeviceGetClockInfo(self.h, 1, self.c.byref(v))  # NVML_CLOCK_SM
+        return v.value
+
+    def sm_max_mhz(self) -> int:
+        v = self.c.c_uint()
+        self.lib.nvmlDeviceGetMaxClockInfo(self.h, 1, self.c.byref(v))
+        return v.value
+
+    def reasons(self) -> int:
+        v = self.c.c_ulonglong()
+        self.reasons_fn(self.h, self.c.byref(v))
+        return v.value
+
+
+def sample_clocks_child(bus: str, index: int, period_s: float):
+    """Child-process clock sampler: prints `ready`, then one line
+    `monotonic_s sm_mhz reasons_mask` per sample until killed.  Run in its
+    own process because NVML queries from the benchmarking process slow its
+    kernel launches."""
+    import time
+
+    class _P:
+        pci_domain_id, pci_bus_id, pci_device_id = (int(v, 16) for v in
+                                                    bus.replace(".", ":").split(":")[:3])
+
+    nv = _Nvml(index, props=_P if bus else None)
+    print("ready %d" % nv.sm_max_mhz(), flush=True)
+    while True:
+        print("%.6f %d %d" % (time.monotonic(), nv.sm_mhz(), nv.reasons()), flush=True)
+        time.sleep(period_s)
+
+
 class Clocks:
-    """Sample nvidia-smi clocks and throttle reasons during the timed region."""
+    """Sample the SM clock and clock-event reasons during the timed region:
+    a child process polls NVML every millisecond (timestamps on the shared
+    monotonic clock select the samples inside the region); nvidia-smi every
+    200 ms if NVML is unavailable."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -116,27 +198,89 @@ class Clocks:
         self.dev = device_index
         self.proc = None
         self.f = None
+        self.child = None
+        self.t0 = self.t1 = None
+
+    def _start_nvml_child(self) -> bool:
+        import time
+
+        bus = ""
+        try:
+            import torch
+
+            pr = torch.cuda.get_device_properties(self.dev)
+            bus = "%x:%x:%x" % (pr.pci_domain_id, pr.pci_bus_id, pr.pci_device_id)
+        except Exception:  # noqa: BLE001 - older torch: NVML index instead
+            pass
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".clk", delete=False)
+        self.child = subprocess.Popen(
+            [sys.executable, str(Path(__file__).resolve()), "--sample-clocks", bus or "-",
+             str(self.dev)], stdout=self.f, stderr=subprocess.DEVNULL)
+        deadline = time.monotonic() + 20
+        while time.monotonic() < deadline:
+            head = Path(self.f.name).read_text().split("\n", 1)[0]
+            if head.startswith("ready"):
+                self.max_mhz = int(head.split()[1])
+                return True
+            if self.child.poll() is not None:
+                break
+            time.sleep(0.02)
+        self.child.kill()
+        self.child = None
+        return False
 
     def __enter__(self):
+        import time
+
         try:
-            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
-                stdout=self.f, stderr=subprocess.DEVNULL)
-        except (OSError, FileNotFoundError):
-            self.proc = None
+            ok = self._start_nvml_child()
+        except OSError:
+            ok = False
+        if not ok:
+            try:
+                self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+                self.proc = subprocess.Popen(
+                    ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.Q}",
+                     "--format=csv,noheader,nounits", "-lms", "200"],
+                    stdout=self.f, stderr=subprocess.DEVNULL)
+            except (OSError, FileNotFoundError):
+                self.proc = None
+        self.t0 = time.monotonic()
         return self
 
     def __exit__(self, *exc):
-        if self.proc is not None:
-            self.proc.terminate()
+        import time
+
+        self.t1 = time.monotonic()
+        for pr in (self.child, self.proc):
+            if pr is None:
+                continue
+            if pr is self.child:
+                time.sleep(0.003)  # one more sample past the end
+            pr.terminate()
             try:
-                self.proc.wait(timeout=5)
+                pr.wait(timeout=5)
             except subprocess.TimeoutExpired:
-                self.proc.kill()
+                pr.kill()
 
     def summary(self):
+        if self.child is not None:
+            rows = Path(self.f.name).read_text().splitlines()[1:]
+            os.unlink(self.f.name)
+            sm, mask = [], 0
+            for ln in rows:
+                try:
+                    t, mhz, rs = ln.split()
+                    t, mhz, rs = float(t), int(mhz), int(rs)
+                except ValueError:
+                    continue
+                if self.t0 <= t <= self.t1:
+                    sm.append(mhz)
+                    mask |= rs
+            reasons = sorted(n for bit, n in _Nvml.REASONS.items() if mask & bit)
+            return {"sm_mhz": statistics.median(sm) if sm else None,
+                    "sm_max_mhz": self.max_mhz, "samples": len(sm),
+                    "source": "nvml (child process, 1 ms)", "reasons": reasons}
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.f.flush()
@@ -155,7 +299,7 @@ class Clocks:
                 continue
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "samples": len(sm),
-                "reasons": sorted(reasons)}
+                "source": "nvidia-smi", "reasons": sorted(reasons)}
 
 
 def cpu_baseline(budget_s: float = 12.0, batch: int = 2):
@@ -315,6 +459,45 @@ def bench_pool(reps: int = 20):
     return out
 
 
+PROFILE_CASES = ("conv_fwd_l1", "conv_bwdi_l1", "conv_bwdk_l1", "conv_fwd_l2", "conv_bwdi_l2",
+                 "conv_bwdk_l2", "pool3d_large")
+
+
+def profile_case(name: str, precision: str = "bf16"):
+    """One small, fixed invocation for an ncu capture: the named call runs
+    twice (the second launch is the warm one to capture).  conv_*: layer L1
+    or L2 of the conv2d workload; pool3d_large: max/avg pool3d 2x2x2 stride 2
+    forward and backward on [8;64;32;32;64] float32 (268 MB, above L2)."""
+    import torch
+
+    from owl_gb300.dense import NN, GpuBackend
+
+    if name.startswith("conv_"):
+        op, layer = name[5:].split("_")
+        i = {"l1": 0, "l2": 1}[layer]
+        lname, xs, ks, st, r, p = LAYERS[i]
+        nn = NN(GpuBackend(precision))
+        x, w, dy = (torch.from_numpy(a).cuda() for a in make_inputs(xs, ks, st, r, p, seed=100 + i))
+        fn = dict(layer_calls(nn, x, w, dy, st, r, p))[
+            {"fwd": "fwd", "bwdi": "bwd_input", "bwdk": "bwd_kernel"}[op]]
+        for _ in range(2):
+            fn()
+    elif name == "pool3d_large":
+        nn = NN(GpuBackend("fp32"))
+        rng = np.random.default_rng(3)
+        x = torch.from_numpy(rng.uniform(-1, 1, (8, 64, 32, 32, 64)).astype(np.float32)).cuda()
+        k, s_ = [2, 2, 2], [2, 2, 2]
+        y = nn.max_pool3d(x, k, s_, "SAME")
+        dy = torch.from_numpy(rng.standard_normal(tuple(y.shape)).astype(np.float32)).cuda()
+        nn.avg_pool3d(x, k, s_, "SAME")
+        nn.max_pool3d_backward("SAME", x, k, s_, dy)
+        nn.avg_pool3d_backward("SAME", x, k, s_, dy)
+    else:
+        raise SystemExit(f"unknown case {name}; one of {PROFILE_CASES}")
+    torch.cuda.synchronize()
+    print(json.dumps({"case": name, "precision": precision, "status": "ok"}))
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -334,6 +517,9 @@ def run_reference(args):
 
 
 def main():
+    if len(sys.argv) == 4 and sys.argv[1] == "--sample-clocks":
+        sample_clocks_child("" if sys.argv[2] == "-" else sys.argv[2], int(sys.argv[3]), 0.001)
+        return
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -345,8 +531,13 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the FP32-plain comparison and the float64 error check")
+    ap.add_argument("--case", choices=PROFILE_CASES,
+                    help="run one small fixed invocation for a profiler capture and exit")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.case:
+        profile_case(args.case, args.precision)
+        return
 
     if args.impl == "reference":
         run_reference(args)
@@ -420,8 +611,18 @@ def main():
             torch.cuda.synchronize()
             t = a.elapsed_time(b) / reps
             per.append({"layer": name, "op": op, "ms": t, "tflops": f / (t / 1e3) / 1e12})
-    dom = max(per, key=lambda d: d["ms"])
     hbm, bf16, src = peaks()
+    byk = {f"{d['layer']}.{d['op']}": d for d in per}
+
+    def roof(key, kernel):
+        d = byk[key]
+        tr = NCU_TRAFFIC.get(key) if args.precision == "bf16" else None
+        return {"bound": "tensor", "kernel": f"{kernel} ({key})", "achieved": d["tflops"],
+                "peak": bf16, "unit": "TFLOP/s", "frac": d["tflops"] / bf16,
+                "traffic": tr[0] if tr else None, "traffic_unit": "bytes per launch",
+                "traffic_source": tr[1] if tr else None,
+                "algorithmic_bytes": ALGO_BYTES.get(key),
+                "peak_source": f"{src} bf16 dense (cuBLAS, burst)"}
 
     result = {
         "metric": "conv2d fwd+bwd TFLOP/s (config 2: L1+L2+dilated)",
@@ -436,10 +637,10 @@ def main():
                    "l2": "no flush: per-step working set ~1.2 GB > 129 MB L2",
                    "parallelism": f"replicas x{world}"},
         "per_kernel": per,
-        "roofline": {"bound": "tensor", "kernel": f"{dom['layer']}.{dom['op']}",
-                     "achieved": dom["tflops"], "peak": bf16, "unit": "TFLOP/s",
-                     "frac": dom["tflops"] / bf16, "traffic": None,
-                     "peak_source": f"{src} bf16 dense (cuBLAS)"},
+        # conv_tc_kernel (forward and backward_input) holds the largest share
+        # of the step; wgrad_tc_kernel (backward_kernel) is the next.
+        "roofline": roof("L1.fwd", "conv_tc_kernel"),
+        "roofline_wgrad": roof("L1.bwd_kernel", "wgrad_tc_kernel"),
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
