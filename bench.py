@@ -459,6 +459,45 @@ def bench_pool(reps: int = 20):
     return out
 
 
+def bench_algodiff(precision: str, steps: int = 10):
+    """Config-4 training step through the Algodiff registrations: a CNN on
+    [256;28;28;1] uniform[0,1] images with random labels (conv 5x5x1x32,
+    ReLU, max_pool 2x2, conv 5x5x32x64, ReLU, max_pool 2x2, dense
+    3136->1024->10, softmax cross-entropy), He-initialised; one step = loss,
+    reverse sweep and SGD update, all on the device."""
+    import torch
+
+    from owl_gb300 import _lib
+    from owl_gb300.algodiff import Algodiff, init_mnist_cnn, sgd_step
+    from owl_gb300.dense import NN, GpuBackend
+
+    out = {}
+    for prec in dict.fromkeys([precision, "fp32"]):
+        ad = Algodiff(NN(GpuBackend(prec)))
+        params = {k: torch.from_numpy(v).cuda() for k, v in init_mnist_cnn(0).items()}
+        rng = np.random.default_rng(43)
+        x = torch.from_numpy(rng.uniform(0, 1, (256, 28, 28, 1)).astype(np.float32)).cuda()
+        onehot = torch.from_numpy(np.eye(10, dtype=np.float32)[rng.integers(0, 10, 256)]).cuda()
+        for _ in range(3):
+            sgd_step(ad, params, x, onehot, lr=0.01)
+        torch.cuda.synchronize()
+        n0 = _lib.launch_count()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(steps):
+            loss, _ = sgd_step(ad, params, x, onehot, lr=0.01)
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / steps
+        out[prec] = {"ms_per_step": ms, "images_per_s": 256 / (ms / 1e3),
+                     "loss_after": float(loss.item()),
+                     "owl_launches_per_step": (_lib.launch_count() - n0) / steps}
+    out["note"] = ("batch 256; conv/pool through libowlgpu, dense layers and softmax in torch "
+                   "(cuBLAS); gradients checked against float64 finite differences and the "
+                   "oracle in tests/test_gpu_algodiff.py")
+    return out
+
+
 PROFILE_CASES = ("conv_fwd_l1", "conv_bwdi_l1", "conv_bwdk_l1", "conv_fwd_l2", "conv_bwdi_l2",
                  "conv_bwdk_l2", "pool3d_large")
 
@@ -667,6 +706,7 @@ def main():
                                                (flops_step / (ms32 / 1e3))}
         result["error_vs_f64"] = accuracy(nn, args.precision)
         result["pool"] = bench_pool()
+        result["algodiff"] = bench_algodiff(args.precision)
 
     # ---- end to end through the host drop-in C ABI ----
     if not args.no_e2e and rank == 0:

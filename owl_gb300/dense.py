@@ -457,6 +457,56 @@ class NN:
                                   padding)
         return self.b.reshape(y, (B, self._shape(y)[2], Co))
 
+    def _as2d(self, input, kernel, output_):
+        """The [B;1;W;C] / [1;K;Ci;Co] views through which Owl runs 1-D
+        convolutions as 2-D ones (G:3402-3440)."""
+        _verify(self._dims(input) == 3 and self._dims(kernel) == 3 and
+                (output_ is None or self._dims(output_) == 3), "1-D conv: bad dimensions")
+        B, IC, Ci = self._shape(input)
+        KC, kci, Co = self._shape(kernel)
+        _verify(Ci == kci, "1-D conv: the 3rd dimension of input shape should be equal to "
+                "the 2nd dimension of kernel shape")
+        x = self.b.reshape(input, (B, 1, IC, Ci))
+        w = self.b.reshape(kernel, (1, KC, Ci, Co))
+        dy = None
+        if output_ is not None:
+            ob, OC, oco = self._shape(output_)
+            dy = self.b.reshape(output_, (ob, 1, OC, oco))
+        return x, w, dy
+
+    def transpose_conv1d_backward_input(self, input, kernel, stride, output_):
+        """G:6570 transpose_conv1d_backward_input."""
+        x, w, dy = self._as2d(input, kernel, output_)
+        dx = self.transpose_conv2d_backward_input(x, w, [1, stride[0]], dy)
+        return self.b.reshape(dx, self._shape(input))
+
+    def transpose_conv1d_backward_kernel(self, input, kernel, stride, output_):
+        """G:6732 transpose_conv1d_backward_kernel."""
+        x, w, dy = self._as2d(input, kernel, output_)
+        dw = self.transpose_conv2d_backward_kernel(x, w, [1, stride[0]], dy)
+        return self.b.reshape(dw, self._shape(kernel))
+
+    def dilated_conv1d(self, input, kernel, stride, rate, padding=SAME):
+        """G:4967 dilated_conv1d: the 2-D view with stride [1; s]; `rate` is
+        handed to dilated_conv2d unchanged, as Owl does (two entries)."""
+        _verify(len(stride) == 1, "dilated_conv1d: stride dimension should be 1")
+        x, w, _ = self._as2d(input, kernel, None)
+        y = self.dilated_conv2d(x, w, [1, stride[0]], list(rate), padding)
+        B, _, OC, Co = self._shape(y)
+        return self.b.reshape(y, (B, OC, Co))
+
+    def dilated_conv1d_backward_input(self, input, kernel, stride, rate, output_):
+        """G:5054 dilated_conv1d_backward_input."""
+        x, w, dy = self._as2d(input, kernel, output_)
+        dx = self.dilated_conv2d_backward_input(x, w, [1, stride[0]], list(rate), dy)
+        return self.b.reshape(dx, self._shape(input))
+
+    def dilated_conv1d_backward_kernel(self, input, kernel, stride, rate, output_):
+        """G:5210 dilated_conv1d_backward_kernel."""
+        x, w, dy = self._as2d(input, kernel, output_)
+        dw = self.dilated_conv2d_backward_kernel(x, w, [1, stride[0]], list(rate), dy)
+        return self.b.reshape(dw, self._shape(kernel))
+
     def transpose_conv3d(self, input, kernel, stride, padding=SAME):
         """G:5915 transpose_conv3d."""
         _verify(self._dims(input) == 5 and self._dims(kernel) == 5 and len(stride) == 3,
@@ -606,6 +656,24 @@ class NN:
         y = self.avg_pool2d(self.b.reshape(input, (B, 1, IC, C)), [1, kernel[0]],
                             [1, stride[0]], padding)
         return self.b.reshape(y, (B, self._shape(y)[2], C))
+
+    def _pool1d_backward(self, which, padding, input, kernel, stride, output_):
+        _verify(self._dims(input) == 3 and len(kernel) == 1 and len(stride) == 1,
+                f"{which}_pool1d_backward: bad dimensions")
+        B, IC, C = self._shape(input)
+        ob, OC, oc = self._shape(output_)
+        dx = self._pool2d_backward(which, padding, self.b.reshape(input, (B, 1, IC, C)),
+                                   [1, kernel[0]], [1, stride[0]],
+                                   self.b.reshape(output_, (ob, 1, OC, oc)))
+        return self.b.reshape(dx, (B, IC, C))
+
+    def max_pool1d_backward(self, padding, input, kernel, stride, output_):
+        """G:7840 max_pool1d_backward (the 2-D view [B;1;W;C], window [1;k])."""
+        return self._pool1d_backward("max", padding, input, kernel, stride, output_)
+
+    def avg_pool1d_backward(self, padding, input, kernel, stride, output_):
+        """G:8158 avg_pool1d_backward."""
+        return self._pool1d_backward("avg", padding, input, kernel, stride, output_)
 
 
 def _int64_like(a) -> Any:

@@ -221,3 +221,46 @@ def test_repeat_calls_are_deterministic(gpu_nn):
     a = from_dev(gpu_nn.conv2d_backward_kernel(x, w, [1, 1], dy))
     b = from_dev(gpu_nn.conv2d_backward_kernel(x, w, [1, 1], dy))
     assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_1d_family(gpu_nn, oracle_nn, dt):
+    """conv1d / dilated_conv1d / transpose_conv1d and pool1d, forward and
+    backward: Owl runs them as 2-D calls on [B;1;W;C] views (G:3402,
+    G:4967, G:6483, G:7027, G:7840)."""
+    rng = np.random.default_rng(15)
+    G, O = gpu_nn, oracle_nn
+    x = rng.uniform(-1, 1, (3, 17, 5)).astype(dt)
+    w = rng.uniform(-1, 1, (3, 5, 4)).astype(dt)
+    xd, wd = to_dev(x), to_dev(w)
+    for pad in (SAME, VALID):
+        y = O.conv1d(x, w, [2], pad)
+        assert rel(from_dev(G.conv1d(xd, wd, [2], pad)), y) <= TOL[dt]
+        dy = rng.standard_normal(y.shape).astype(dt)
+        assert rel(from_dev(G.conv1d_backward_input(xd, wd, [2], to_dev(dy))),
+                   O.conv1d_backward_input(x, w, [2], dy)) <= TOL[dt]
+        assert rel(from_dev(G.conv1d_backward_kernel(xd, wd, [2], to_dev(dy))),
+                   O.conv1d_backward_kernel(x, w, [2], dy)) <= TOL[dt]
+        y = O.dilated_conv1d(x, w, [1], [1, 2], pad)
+        assert rel(from_dev(G.dilated_conv1d(xd, wd, [1], [1, 2], pad)), y) <= TOL[dt]
+        dy = rng.standard_normal(y.shape).astype(dt)
+        assert rel(from_dev(G.dilated_conv1d_backward_input(xd, wd, [1], [1, 2], to_dev(dy))),
+                   O.dilated_conv1d_backward_input(x, w, [1], [1, 2], dy)) <= TOL[dt]
+        assert rel(from_dev(G.dilated_conv1d_backward_kernel(xd, wd, [1], [1, 2], to_dev(dy))),
+                   O.dilated_conv1d_backward_kernel(x, w, [1], [1, 2], dy)) <= TOL[dt]
+        wt = rng.uniform(-1, 1, (3, 5, 2)).astype(dt)
+        y = O.transpose_conv1d(x, wt, [2], pad)
+        assert rel(from_dev(G.transpose_conv1d(xd, to_dev(wt), [2], pad)), y) <= TOL[dt]
+        dy = rng.standard_normal(y.shape).astype(dt)
+        assert rel(from_dev(G.transpose_conv1d_backward_input(xd, to_dev(wt), [2], to_dev(dy))),
+                   O.transpose_conv1d_backward_input(x, wt, [2], dy)) <= TOL[dt]
+        assert rel(from_dev(G.transpose_conv1d_backward_kernel(xd, to_dev(wt), [2],
+                                                               to_dev(dy))),
+                   O.transpose_conv1d_backward_kernel(x, wt, [2], dy)) <= TOL[dt]
+        for f in ("max_pool1d", "avg_pool1d"):
+            a = getattr(O, f)(x, [3], [2], pad)
+            assert np.array_equal(from_dev(getattr(G, f)(xd, [3], [2], pad)), a)
+            g = rng.standard_normal(a.shape).astype(dt)
+            assert np.array_equal(
+                from_dev(getattr(G, f + "_backward")(pad, xd, [3], [2], to_dev(g))),
+                getattr(O, f + "_backward")(pad, x, [3], [2], g))
