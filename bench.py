@@ -498,6 +498,50 @@ def bench_algodiff(precision: str, steps: int = 10):
     return out
 
 
+def bench_serve(precision: str, n_requests: int = 600, rate: float = 2000.0):
+    """Config-5 serving: a seeded Poisson stream (mean `rate` req/s) of
+    requests, batch uniform in 1..64, side drawn from {14,28,56,112,224}, 3
+    channels, U[0,1] pixels, through the 21-conv residual stack (BF16 MMAs,
+    FP32 accumulation) by the continuous-batching scheduler.  The stream is
+    run once to capture the graph instances it needs, then timed; latency
+    = completion seen by the host - arrival."""
+    import torch
+
+    from owl_gb300.dense import NN, GpuBackend
+    from owl_gb300.serving import (GraphExecutor, ResidualStack, Scheduler, attach_pixels,
+                                   init_stack, poisson_stream, stack_flops)
+
+    w = {k: torch.from_numpy(v).cuda() for k, v in init_stack(0).items()}
+    stack = ResidualStack(w, NN(GpuBackend(precision)))
+    reqs = poisson_stream(n_requests, rate, seed=11)
+    attach_pixels(reqs, seed=12)
+    ex = GraphExecutor(stack, streams=8)
+    sch = Scheduler(ex, hbm_budget=64 << 30, max_group=128)
+    sch.run(reqs)  # captures the instances this stream needs
+    torch.cuda.synchronize()
+    for r in reqs:
+        r.output = None
+    st = sch.run(reqs)
+    out = st.summary()
+    flops = sum(stack_flops(r.side, r.batch) for r in reqs)
+    out["offered_req_per_s"] = rate
+    out["tflops"] = flops / st.wall_s / 1e12
+    out["gflop_per_request"] = flops / len(reqs) / 1e9
+    # error against the float64 path on a sample of requests
+    w64 = {k: torch.from_numpy(v.astype(np.float64)).cuda() for k, v in init_stack(0).items()}
+    s64 = ResidualStack(w64, NN(GpuBackend("fp32")))
+    errs = []
+    for r in reqs[:8]:
+        y64 = s64.forward(r.pixels.double().cuda()).cpu().numpy()
+        errs.append(float(np.abs(r.output - y64).max() / np.abs(y64).max()))
+    out["error_vs_f64"] = max(errs)
+    out["precision"] = precision
+    out["note"] = ("%d requests; graph instances captured in a first pass over the same "
+                   "stream; hbm budget 64 GiB; 8 streams" % n_requests)
+    sch.close()
+    return out
+
+
 PROFILE_CASES = ("conv_fwd_l1", "conv_bwdi_l1", "conv_bwdk_l1", "conv_fwd_l2", "conv_bwdi_l2",
                  "conv_bwdk_l2", "pool3d_large")
 
@@ -707,6 +751,7 @@ def main():
         result["error_vs_f64"] = accuracy(nn, args.precision)
         result["pool"] = bench_pool()
         result["algodiff"] = bench_algodiff(args.precision)
+        result["serve"] = bench_serve(args.precision)
 
     # ---- end to end through the host drop-in C ABI ----
     if not args.no_e2e and rank == 0:
