@@ -71,16 +71,19 @@ def make_inputs(xs, ks, stride, rate, pad, seed, batch=None):
     return x, w, dy
 
 
-def run_layer(nn, x, w, dy, stride, rate, pad):
+def run_layer(nn, x, w, dy, stride, rate, pad, outs=(None, None, None)):
+    """forward, backward_input, backward_kernel of one layer; `outs` are
+    optional result arrays (Owl's `_ ~out` variants)."""
     st = list(stride)
+    oy, odx, odw = outs
     if rate:
-        y = nn.dilated_conv2d(x, w, st, list(rate), pad)
-        dx = nn.dilated_conv2d_backward_input(x, w, st, list(rate), dy)
-        dw = nn.dilated_conv2d_backward_kernel(x, w, st, list(rate), dy)
+        y = nn.dilated_conv2d(x, w, st, list(rate), pad, out=oy)
+        dx = nn.dilated_conv2d_backward_input(x, w, st, list(rate), dy, out=odx)
+        dw = nn.dilated_conv2d_backward_kernel(x, w, st, list(rate), dy, out=odw)
     else:
-        y = nn.conv2d(x, w, st, pad)
-        dx = nn.conv2d_backward_input(x, w, st, dy)
-        dw = nn.conv2d_backward_kernel(x, w, st, dy)
+        y = nn.conv2d(x, w, st, pad, out=oy)
+        dx = nn.conv2d_backward_input(x, w, st, dy, out=odx)
+        dw = nn.conv2d_backward_kernel(x, w, st, dy, out=odw)
     return y, dx, dw
 
 
@@ -756,20 +759,24 @@ def main():
     # ---- end to end through the host drop-in C ABI ----
     if not args.no_e2e and rank == 0:
         host_nn = NN(GpuBackend(args.precision))
-        pinned = []
+        pinned, outs = [], []
         h2d = d2h = 0
+
+        def pin(shape):
+            return torch.empty(tuple(shape), dtype=torch.float32, pin_memory=True)
+
         for (name, xs, ks, st, r, p), (x, w, dy) in zip(LAYERS, dev_data):
-            hx = torch.empty(x.shape, dtype=torch.float32, pin_memory=True)
-            hw = torch.empty(w.shape, dtype=torch.float32, pin_memory=True)
-            hdy = torch.empty(dy.shape, dtype=torch.float32, pin_memory=True)
+            hx, hw, hdy = pin(x.shape), pin(w.shape), pin(dy.shape)
             hx.copy_(x.cpu()); hw.copy_(w.cpu()); hdy.copy_(dy.cpu())
             pinned.append((hx.numpy(), hw.numpy(), hdy.numpy()))
+            # results land in pinned arrays too (Owl's `_ ~out` variants)
+            outs.append((pin(dy.shape).numpy(), pin(x.shape).numpy(), pin(w.shape).numpy()))
             xb, wb, gb = hx.numel() * 4, hw.numel() * 4, hdy.numel() * 4
             h2d += (xb + wb) + (wb + gb) + (xb + gb)  # fwd, bwd_input, bwd_kernel inputs
             d2h += gb + xb + wb                        # y, dx, dw
         def host_step():
-            for (name, xs, ks, st, r, p), (x, w, dy) in zip(LAYERS, pinned):
-                run_layer(host_nn, x, w, dy, st, r, p)
+            for (name, xs, ks, st, r, p), (x, w, dy), o in zip(LAYERS, pinned, outs):
+                run_layer(host_nn, x, w, dy, st, r, p, o)
         host_step()
         e_steps = max(2, min(args.steps, 5))
         t0 = time.perf_counter()
@@ -778,7 +785,8 @@ def main():
         el = time.perf_counter() - t0
         result["e2e"] = {"value": flops_step / (el / e_steps) / 1e12, "unit": "TFLOP/s",
                          "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                         "steps": e_steps, "api": "owl_float32_ndarray_conv_* host drop-in"}
+                         "steps": e_steps, "api": "owl_float32_ndarray_conv_* host drop-in",
+                         "host_buffers": "pinned inputs and pinned result arrays (out=)"}
 
     if rank == 0 and world == 1 and not args.no_cpu:
         cb = cpu_baseline(budget_s=15.0)

@@ -190,14 +190,16 @@ static int default_precision() {
   return g_precision.load();
 }
 
+// Per host thread: a compute stream and two copy streams (host-to-device,
+// device-to-host), plus events to order them, reused across calls.
 struct HostStream {
-  cudaStream_t s = nullptr;
+  cudaStream_t s = nullptr, cin = nullptr, cout = nullptr;
   int device = -1;
-  ~HostStream() {}
+  std::vector<cudaEvent_t> ev;
 };
 static thread_local HostStream t_stream;
 
-static int host_stream(cudaStream_t *out) {
+static int host_stream(HostStream **out) {
   int dev = g_device.load();
   if (t_stream.s == nullptr || t_stream.device != dev) {
     OWL_CUDA(cudaSetDevice(dev));
@@ -207,14 +209,26 @@ static int host_stream(cudaStream_t *out) {
     OWL_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
     uint64_t keep = UINT64_MAX;
     OWL_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
-    cudaStream_t s;
-    OWL_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-    t_stream.s = s;
+    cudaStream_t st[3];
+    for (auto &x : st) OWL_CUDA(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+    t_stream.s = st[0];
+    t_stream.cin = st[1];
+    t_stream.cout = st[2];
+    t_stream.ev.clear();
     t_stream.device = dev;
   } else {
     OWL_CUDA(cudaSetDevice(dev));
   }
-  *out = t_stream.s;
+  *out = &t_stream;
+  return kOk;
+}
+
+static int host_events(HostStream &hs, size_t n) {
+  while (hs.ev.size() < n) {
+    cudaEvent_t e;
+    OWL_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    hs.ev.push_back(e);
+  }
   return kOk;
 }
 
@@ -222,45 +236,102 @@ struct Buf {
   const void *host;  // source (inputs) or destination (outputs)
   size_t bytes;
   bool in, out;
+  bool batched;      // leading axis is the batch: staged chunk by chunk
   void *dev = nullptr;
 };
 
-// Stage `bufs` to the device, run `body(dev pointers, stream)`, copy the
-// outputs back and wait.  Device memory comes from the stream-ordered pool,
-// so repeated calls of the same size reuse it.
+static bool page_locked(const void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+// Number of batch chunks for a staged call: about 24 MB of batched traffic
+// per chunk, at most 8, at most one sample per chunk.  Copies from or to
+// pageable host memory block the calling thread, which would serialise the
+// pipeline, so a call with any pageable batched buffer is staged whole.
+static int chunks_for(const std::vector<Buf> &bufs, int64_t batch) {
+  size_t moved = 0;
+  for (auto &b : bufs) {
+    if (!b.batched || b.bytes == 0) continue;
+    if (!page_locked(b.host)) return 1;
+    moved += b.bytes;
+  }
+  int64_t c = (int64_t)(moved / (24u << 20));
+  return (int)std::max<int64_t>(1, std::min<int64_t>({c, 8, batch}));
+}
+
+// Stage `bufs` to the device, run `body(dev pointers, b0, nb, stream)` over
+// the batch in `chunks` pieces, copy the outputs back and wait.  With more
+// than one chunk the host-to-device copy of chunk c+1, the compute of chunk
+// c and the device-to-host copy of chunk c-1 run concurrently on three
+// streams; only calls whose every batch sample is independent are chunked,
+// and they give the same results as one call.  Device memory comes from the
+// stream-ordered pool, so repeated calls of the same size reuse it.
 template <typename F>
-static int host_call(std::vector<Buf> bufs, F body) {
-  cudaStream_t s;
-  int rc = host_stream(&s);
+static int host_call(std::vector<Buf> bufs, int64_t batch, int chunks, F body) {
+  HostStream *hs;
+  int rc = host_stream(&hs);
+  if (rc) return rc;
+  if (batch <= 0) chunks = 1;
+  rc = host_events(*hs, 2 * (size_t)chunks);
   if (rc) return rc;
   for (auto &b : bufs) {
     if (b.bytes == 0) continue;
-    rc = scratch_alloc(&b.dev, b.bytes, s);
+    rc = scratch_alloc(&b.dev, b.bytes, hs->cin);
     if (rc) break;
-    if (b.in) {
-      cudaError_t e = cudaMemcpyAsync(b.dev, b.host, b.bytes, cudaMemcpyHostToDevice, s);
+    if (b.in && !b.batched) {
+      cudaError_t e = cudaMemcpyAsync(b.dev, b.host, b.bytes, cudaMemcpyHostToDevice, hs->cin);
       if (e != cudaSuccess) { rc = cuda_fail(e, "cudaMemcpyAsync(H2D)"); break; }
     }
   }
-  if (rc == kOk) {
-    std::vector<void *> ptrs;
-    for (auto &b : bufs) ptrs.push_back(b.dev);
-    rc = body(ptrs, s);
-  }
-  if (rc == kOk) {
+  std::vector<void *> ptrs;
+  for (auto &b : bufs) ptrs.push_back(b.dev);
+  for (int c = 0; rc == kOk && c < chunks; ++c) {
+    const int64_t b0 = batch * c / chunks, b1 = batch * (c + 1) / chunks;
+    cudaEvent_t ein = hs->ev[2 * c], ecomp = hs->ev[2 * c + 1];
     for (auto &b : bufs) {
-      if (!b.out || b.bytes == 0) continue;
-      cudaError_t e = cudaMemcpyAsync(const_cast<void *>(b.host), b.dev, b.bytes,
-                                      cudaMemcpyDeviceToHost, s);
+      if (!b.in || !b.batched || b.bytes == 0) continue;
+      const size_t per = b.bytes / (size_t)batch;
+      cudaError_t e = cudaMemcpyAsync((char *)b.dev + per * b0, (const char *)b.host + per * b0,
+                                      per * (b1 - b0), cudaMemcpyHostToDevice, hs->cin);
+      if (e != cudaSuccess) { rc = cuda_fail(e, "cudaMemcpyAsync(H2D)"); break; }
+    }
+    if (rc) break;
+    OWL_CUDA(cudaEventRecord(ein, hs->cin));
+    OWL_CUDA(cudaStreamWaitEvent(hs->s, ein, 0));
+    rc = body(ptrs, b0, b1 - b0, hs->s);
+    if (rc) break;
+    OWL_CUDA(cudaEventRecord(ecomp, hs->s));
+    OWL_CUDA(cudaStreamWaitEvent(hs->cout, ecomp, 0));
+    for (auto &b : bufs) {
+      if (!b.out || !b.batched || b.bytes == 0) continue;
+      const size_t per = b.bytes / (size_t)batch;
+      cudaError_t e = cudaMemcpyAsync((char *)b.host + per * b0, (char *)b.dev + per * b0,
+                                      per * (b1 - b0), cudaMemcpyDeviceToHost, hs->cout);
       if (e != cudaSuccess) { rc = cuda_fail(e, "cudaMemcpyAsync(D2H)"); break; }
     }
   }
-  for (auto &b : bufs) scratch_free(b.dev, s);
-  cudaError_t e = cudaStreamSynchronize(s);
+  if (rc == kOk) {
+    for (auto &b : bufs) {
+      if (!b.out || b.batched || b.bytes == 0) continue;
+      cudaError_t e = cudaMemcpyAsync(const_cast<void *>(b.host), b.dev, b.bytes,
+                                      cudaMemcpyDeviceToHost, hs->s);
+      if (e != cudaSuccess) { rc = cuda_fail(e, "cudaMemcpyAsync(D2H)"); break; }
+    }
+  }
+  cudaError_t e1 = cudaStreamSynchronize(hs->cin);
+  cudaError_t e2 = cudaStreamSynchronize(hs->s);
+  cudaError_t e3 = cudaStreamSynchronize(hs->cout);
+  for (auto &b : bufs) scratch_free(b.dev, hs->s);
+  cudaError_t e = e1 != cudaSuccess ? e1 : e2 != cudaSuccess ? e2 : e3;
   if (rc == kOk && e != cudaSuccess) rc = cuda_fail(e, "cudaStreamSynchronize");
   if (rc == kOk) {
     int st = 0;
-    rc = tc_read_status(&st, s);
+    rc = tc_read_status(&st, hs->s);
     if (rc == kOk && st) {
       set_error("a tensor-core kernel gave up waiting on one of its pipeline barriers");
       rc = kErrTimeout;
@@ -291,36 +362,70 @@ static int conv_device(ConvOp op, const ConvGeom &g, void *a, void *b, void *c, 
 template <typename T>
 static int conv_host(ConvOp op, const ConvGeom &g, const void *a, const void *b, const void *c) {
   size_t xb = sizeof(T) * g.x_elems(), wb = sizeof(T) * g.w_elems(), yb = sizeof(T) * g.y_elems();
+  // forward and backward_input are independent per batch sample: staged in
+  // chunks; backward_kernel sums over the batch: one piece.
+  const bool chunk = op != OP_BWDK;
   std::vector<Buf> bufs;
-  if (op == OP_FWD) bufs = {{a, xb, true, false}, {b, wb, true, false}, {c, yb, false, true}};
-  else if (op == OP_BWDI) bufs = {{a, xb, false, true}, {b, wb, true, false}, {c, yb, true, false}};
-  else bufs = {{a, xb, true, false}, {b, wb, false, true}, {c, yb, true, false}};
+  if (op == OP_FWD)
+    bufs = {{a, xb, true, false, chunk}, {b, wb, true, false, false}, {c, yb, false, true, chunk}};
+  else if (op == OP_BWDI)
+    bufs = {{a, xb, false, true, chunk}, {b, wb, true, false, false}, {c, yb, true, false, chunk}};
+  else
+    bufs = {{a, xb, true, false, false}, {b, wb, false, true, false}, {c, yb, true, false, false}};
   int prec = default_precision();
-  return host_call(bufs, [&](std::vector<void *> &p, cudaStream_t s) {
-    return conv_device<T>(op, g, p[0], p[1], p[2], prec, s);
+  const int chunks = chunk ? chunks_for(bufs, g.B) : 1;
+  const int64_t xs = g.x_elems() / std::max<int64_t>(g.B, 1);
+  const int64_t ys = g.y_elems() / std::max<int64_t>(g.B, 1);
+  return host_call(bufs, g.B, chunks,
+                   [&](std::vector<void *> &p, int64_t b0, int64_t nb, cudaStream_t s) {
+    ConvGeom gc = g;
+    gc.B = nb;
+    T *x = (T *)p[0] + (chunk ? b0 * xs : 0);
+    T *y = (T *)p[2] + (chunk ? b0 * ys : 0);
+    return conv_device<T>(op, gc, x, p[1], y, prec, s);
   });
 }
 
 template <typename T>
 static int pool_fwd_host(PoolMode mode, const PoolGeom &g, const void *x, void *y,
                          int64_t *arg) {
-  std::vector<Buf> bufs = {{x, sizeof(T) * g.x_elems(), true, false},
-                           {y, sizeof(T) * g.y_elems(), false, true}};
-  if (arg) bufs.push_back({arg, sizeof(int64_t) * g.y_elems(), false, true});
-  return host_call(bufs, [&](std::vector<void *> &p, cudaStream_t s) {
-    return pool_fwd(dtype_of<T>(), mode, g, p[0], p[1], arg ? (int64_t *)p[2] : nullptr, s);
+  // argmax holds flat indices into the whole input: staged in one piece.
+  const bool chunk = arg == nullptr;
+  std::vector<Buf> bufs = {{x, sizeof(T) * g.x_elems(), true, false, chunk},
+                           {y, sizeof(T) * g.y_elems(), false, true, chunk}};
+  if (arg) bufs.push_back({arg, sizeof(int64_t) * g.y_elems(), false, true, false});
+  const int chunks = chunk ? chunks_for(bufs, g.B) : 1;
+  const int64_t xs = g.x_elems() / std::max<int64_t>(g.B, 1);
+  const int64_t ys = g.y_elems() / std::max<int64_t>(g.B, 1);
+  return host_call(bufs, g.B, chunks,
+                   [&](std::vector<void *> &p, int64_t b0, int64_t nb, cudaStream_t s) {
+    PoolGeom gc = g;
+    gc.B = nb;
+    return pool_fwd(dtype_of<T>(), mode, gc, (T *)p[0] + b0 * xs, (T *)p[1] + b0 * ys,
+                    arg ? (int64_t *)p[2] : nullptr, s);
   });
 }
 
 template <typename T>
 static int pool_bwd_host(PoolMode mode, const PoolGeom &g, const void *x, const void *dy,
                          void *dx) {
-  // Average pooling never reads X (Owl passes a dummy there).
-  std::vector<Buf> bufs = {{x, mode == POOL_MAX ? sizeof(T) * g.x_elems() : 0, true, false},
-                           {dy, sizeof(T) * g.y_elems(), true, false},
-                           {dx, sizeof(T) * g.x_elems(), false, true}};
-  return host_call(bufs, [&](std::vector<void *> &p, cudaStream_t s) {
-    return pool_bwd(dtype_of<T>(), mode, g, p[0], p[1], p[2], s);
+  // Average pooling never reads X (Owl passes a dummy there) and is
+  // independent per sample; max pooling routes degenerate windows to flat
+  // element 0 of the whole input, so it is staged in one piece.
+  const bool chunk = mode == POOL_AVG;
+  std::vector<Buf> bufs = {
+      {x, mode == POOL_MAX ? sizeof(T) * g.x_elems() : 0, true, false, false},
+      {dy, sizeof(T) * g.y_elems(), true, false, chunk},
+      {dx, sizeof(T) * g.x_elems(), false, true, chunk}};
+  const int chunks = chunk ? chunks_for(bufs, g.B) : 1;
+  const int64_t xs = g.x_elems() / std::max<int64_t>(g.B, 1);
+  const int64_t ys = g.y_elems() / std::max<int64_t>(g.B, 1);
+  return host_call(bufs, g.B, chunks,
+                   [&](std::vector<void *> &p, int64_t b0, int64_t nb, cudaStream_t s) {
+    PoolGeom gc = g;
+    gc.B = nb;
+    const T *px = chunk ? nullptr : (const T *)p[0];
+    return pool_bwd(dtype_of<T>(), mode, gc, px, (T *)p[1] + b0 * ys, (T *)p[2] + b0 * xs, s);
   });
 }
 
@@ -350,11 +455,11 @@ int owlgpu_get_precision(void) { return default_precision(); }
 uint64_t owlgpu_launch_count(void) { return g_launches.load(); }
 int owlgpu_last_conv_path(void) { return t_last_path; }
 int owlgpu_device_status(void) {
-  cudaStream_t s;
-  int rc = host_stream(&s);
+  HostStream *hs;
+  int rc = host_stream(&hs);
   if (rc) return rc;
   int v = 0;
-  rc = tc_read_status(&v, s);
+  rc = tc_read_status(&v, hs->s);
   if (rc) return rc;
   if (v) {
     set_error("a tensor-core kernel gave up waiting on one of its pipeline barriers");

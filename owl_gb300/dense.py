@@ -198,6 +198,27 @@ class NN:
     def _dims(self, a):
         return len(self._shape(a))
 
+    def _out(self, out, like, shape, dtype=None):
+        """The `~out` argument of Owl's `_` variants (e.g. `conv2d_ ~out`,
+        G:2402): write into `out` when given (its shape must be the result's),
+        else allocate where `like` lives."""
+        if out is None:
+            return self.b.empty(like, shape, dtype)
+        _verify(tuple(self._shape(out)) == tuple(shape),
+                f"out: shape {list(self._shape(out))} should be {list(shape)}")
+        return out
+
+    def _ob(self, out):
+        """A 1-D result [B;W;C] seen as the 2-D [B;1;W;C] it is computed as."""
+        if out is None:
+            return None
+        sh = tuple(self._shape(out))
+        return self.b.reshape(out, (sh[0], 1) + sh[1:])
+
+    def _ok(self, out):
+        """A 1-D kernel [K;Ci;Co] seen as the 2-D [1;K;Ci;Co]."""
+        return None if out is None else self.b.reshape(out, (1,) + tuple(self._shape(out)))
+
     # ======================= conv2d (G:2324-2850) =======================
 
     def conv2d(self, input, kernel, stride: Sequence[int], padding=SAME, out=None):
@@ -213,7 +234,7 @@ class NN:
                 f"to the 3rd dimension of kernel shape.")
         cs, rs = stride
         OC, OR = calc_conv2d_output_shape(padding, IC, IR, KC, KR, rs, cs)
-        output = out if out is not None else self.b.empty(input, (B, OC, OR, Co))
+        output = self._out(out, input, (B, OC, OR, Co))
         self.b.stub(_kind(input), "conv_spatial", input, kernel, output, B, IC, IR, Ci, KC, KR,
                     OC, OR, Co, rs, cs, _pad_typ(padding), 1, 1)
         return output
@@ -230,29 +251,29 @@ class NN:
                 f"does not match input/kernel")
         return B, IC, IR, Ci, KC, KR, Co, OC, OR
 
-    def conv2d_backward_input(self, input, kernel, stride, output_):
+    def conv2d_backward_input(self, input, kernel, stride, output_, out=None):
         """G:2479 conv2d_backward_input."""
         B, IC, IR, Ci, KC, KR, Co, OC, OR = self._conv2d_bwd_check(
             "conv2d_backward_input", input, kernel, stride, output_)
         cs, rs = stride
-        input_ = self.b.empty(input, self._shape(input))
+        input_ = self._out(out, input, self._shape(input))
         self.b.stub(_kind(input), "conv_spatial_backward_input", input_, kernel, output_, B, IC,
                     IR, Ci, KC, KR, OC, OR, Co, rs, cs, 1, 1)
         return input_
 
-    def conv2d_backward_kernel(self, input, kernel, stride, output_):
+    def conv2d_backward_kernel(self, input, kernel, stride, output_, out=None):
         """G:2660 conv2d_backward_kernel."""
         B, IC, IR, Ci, KC, KR, Co, OC, OR = self._conv2d_bwd_check(
             "conv2d_backward_kernel", input, kernel, stride, output_)
         cs, rs = stride
-        kernel_ = self.b.empty(kernel, self._shape(kernel))
+        kernel_ = self._out(out, kernel, self._shape(kernel))
         self.b.stub(_kind(input), "conv_spatial_backward_kernel", input, kernel_, output_, B,
                     IC, IR, Ci, KC, KR, OC, OR, Co, rs, cs, 1, 1)
         return kernel_
 
     # ======================= conv1d (G:3402) =======================
 
-    def conv1d(self, input, kernel, stride, padding=SAME):
+    def conv1d(self, input, kernel, stride, padding=SAME, out=None):
         """G:3402 conv1d: reshape to conv2d [B;1;W;C] with stride [1;s]."""
         _verify(self._dims(input) == 3 and self._dims(kernel) == 3 and len(stride) == 1,
                 "conv1d: bad dimensions")
@@ -261,25 +282,27 @@ class NN:
         _verify(Ci == kci, "conv1d: channel mismatch")
         x = self.b.reshape(input, (B, 1, IC, Ci))
         w = self.b.reshape(kernel, (1, KC, Ci, Co))
-        y = self.conv2d(x, w, [1, stride[0]], padding)
+        y = self.conv2d(x, w, [1, stride[0]], padding, out=self._ob(out))
         return self.b.reshape(y, (B, self._shape(y)[2], Co))
 
-    def conv1d_backward_input(self, input, kernel, stride, output_):
+    def conv1d_backward_input(self, input, kernel, stride, output_, out=None):
         B, IC, Ci = self._shape(input)
         KC, _, Co = self._shape(kernel)
         OC = self._shape(output_)[1]
         dx = self.conv2d_backward_input(self.b.reshape(input, (B, 1, IC, Ci)),
                                         self.b.reshape(kernel, (1, KC, Ci, Co)),
-                                        [1, stride[0]], self.b.reshape(output_, (B, 1, OC, Co)))
+                                        [1, stride[0]], self.b.reshape(output_, (B, 1, OC, Co)),
+                                        out=self._ob(out))
         return self.b.reshape(dx, (B, IC, Ci))
 
-    def conv1d_backward_kernel(self, input, kernel, stride, output_):
+    def conv1d_backward_kernel(self, input, kernel, stride, output_, out=None):
         B, IC, Ci = self._shape(input)
         KC, _, Co = self._shape(kernel)
         OC = self._shape(output_)[1]
         dw = self.conv2d_backward_kernel(self.b.reshape(input, (B, 1, IC, Ci)),
                                          self.b.reshape(kernel, (1, KC, Ci, Co)),
-                                         [1, stride[0]], self.b.reshape(output_, (B, 1, OC, Co)))
+                                         [1, stride[0]], self.b.reshape(output_, (B, 1, OC, Co)),
+                                         out=self._ok(out))
         return self.b.reshape(dw, (KC, Ci, Co))
 
     # ======================= conv3d (G:2848-3400) =======================
@@ -294,7 +317,7 @@ class NN:
                 "4th dimension of kernel shape")
         cs, rs, ds = stride
         OC, OR, OD = calc_conv3d_output_shape(padding, IC, IR, ID, KC, KR, KD, rs, cs, ds)
-        output = out if out is not None else self.b.empty(input, (B, OC, OR, OD, Co))
+        output = self._out(out, input, (B, OC, OR, OD, Co))
         self.b.stub(_kind(input), "conv_cuboid_im2col", input, kernel, output, B, IC, IR, ID, Ci,
                     KC, KR, KD, OC, OR, OD, Co, ds, rs, cs, _pad_typ(padding))
         return output
@@ -309,22 +332,22 @@ class NN:
         _verify(B == ob and Co == oco, f"{name}: output' shape mismatch")
         return B, IC, IR, ID, Ci, KC, KR, KD, Co, OC, OR, OD
 
-    def conv3d_backward_input(self, input, kernel, stride, output_):
+    def conv3d_backward_input(self, input, kernel, stride, output_, out=None):
         """G:3017 conv3d_backward_input."""
         B, IC, IR, ID, Ci, KC, KR, KD, Co, OC, OR, OD = self._conv3d_bwd_check(
             "conv3d_backward_input", input, kernel, stride, output_)
         cs, rs, ds = stride
-        input_ = self.b.empty(input, self._shape(input))
+        input_ = self._out(out, input, self._shape(input))
         self.b.stub(_kind(input), "conv_cuboid_backward_input_im2col", input_, kernel, output_,
                     B, IC, IR, ID, Ci, KC, KR, KD, OC, OR, OD, Co, ds, rs, cs)
         return input_
 
-    def conv3d_backward_kernel(self, input, kernel, stride, output_):
+    def conv3d_backward_kernel(self, input, kernel, stride, output_, out=None):
         """G:3206 conv3d_backward_kernel."""
         B, IC, IR, ID, Ci, KC, KR, KD, Co, OC, OR, OD = self._conv3d_bwd_check(
             "conv3d_backward_kernel", input, kernel, stride, output_)
         cs, rs, ds = stride
-        kernel_ = self.b.empty(kernel, self._shape(kernel))
+        kernel_ = self._out(out, kernel, self._shape(kernel))
         self.b.stub(_kind(input), "conv_cuboid_backward_kernel_im2col", input, kernel_, output_,
                     B, IC, IR, ID, Ci, KC, KR, KD, OC, OR, OD, Co, ds, rs, cs)
         return kernel_
@@ -342,29 +365,29 @@ class NN:
         cr, rr = rate
         kcu, kru = KC + (KC - 1) * (cr - 1), KR + (KR - 1) * (rr - 1)
         OC, OR = calc_conv2d_output_shape(padding, IC, IR, kcu, kru, rs, cs)
-        output = out if out is not None else self.b.empty(input, (B, OC, OR, Co))
+        output = self._out(out, input, (B, OC, OR, Co))
         self.b.stub(_kind(input), "conv_dilated_spatial_im2col", input, kernel, output, B, IC,
                     IR, Ci, KC, KR, OC, OR, Co, rs, cs, _pad_typ(padding), rr, cr)
         return output
 
-    def dilated_conv2d_backward_input(self, input, kernel, stride, rate, output_):
+    def dilated_conv2d_backward_input(self, input, kernel, stride, rate, output_, out=None):
         """G:3960."""
         B, IC, IR, Ci, KC, KR, Co, OC, OR = self._conv2d_bwd_check(
             "dilated_conv2d_backward_input", input, kernel, stride, output_)
         cs, rs = stride
         cr, rr = rate
-        input_ = self.b.empty(input, self._shape(input))
+        input_ = self._out(out, input, self._shape(input))
         self.b.stub(_kind(input), "conv_dilated_spatial_backward_input_im2col", input_, kernel,
                     output_, B, IC, IR, Ci, KC, KR, OC, OR, Co, rs, cs, rr, cr)
         return input_
 
-    def dilated_conv2d_backward_kernel(self, input, kernel, stride, rate, output_):
+    def dilated_conv2d_backward_kernel(self, input, kernel, stride, rate, output_, out=None):
         """G:4151."""
         B, IC, IR, Ci, KC, KR, Co, OC, OR = self._conv2d_bwd_check(
             "dilated_conv2d_backward_kernel", input, kernel, stride, output_)
         cs, rs = stride
         cr, rr = rate
-        kernel_ = self.b.empty(kernel, self._shape(kernel))
+        kernel_ = self._out(out, kernel, self._shape(kernel))
         self.b.stub(_kind(input), "conv_dilated_spatial_backward_kernel_im2col", input, kernel_,
                     output_, B, IC, IR, Ci, KC, KR, OC, OR, Co, rs, cs, rr, cr)
         return kernel_
@@ -382,30 +405,30 @@ class NN:
         kru = KR + (KR - 1) * (rr - 1)
         kdu = KD + (KD - 1) * (dr - 1)
         OC, OR, OD = calc_conv3d_output_shape(padding, IC, IR, ID, kcu, kru, kdu, rs, cs, ds)
-        output = out if out is not None else self.b.empty(input, (B, OC, OR, OD, Co))
+        output = self._out(out, input, (B, OC, OR, OD, Co))
         self.b.stub(_kind(input), "conv_dilated_cuboid_im2col", input, kernel, output, B, IC, IR,
                     ID, Ci, KC, KR, KD, OC, OR, OD, Co, ds, rs, cs, dr, rr, cr,
                     _pad_typ(padding))
         return output
 
-    def dilated_conv3d_backward_input(self, input, kernel, stride, rate, output_):
+    def dilated_conv3d_backward_input(self, input, kernel, stride, rate, output_, out=None):
         """G:4539."""
         B, IC, IR, ID, Ci, KC, KR, KD, Co, OC, OR, OD = self._conv3d_bwd_check(
             "dilated_conv3d_backward_input", input, kernel, stride, output_)
         cs, rs, ds = stride
         cr, rr, dr = rate
-        input_ = self.b.empty(input, self._shape(input))
+        input_ = self._out(out, input, self._shape(input))
         self.b.stub(_kind(input), "conv_dilated_cuboid_backward_input_im2col", input_, kernel,
                     output_, B, IC, IR, ID, Ci, KC, KR, KD, OC, OR, OD, Co, ds, rs, cs, dr, rr, cr)
         return input_
 
-    def dilated_conv3d_backward_kernel(self, input, kernel, stride, rate, output_):
+    def dilated_conv3d_backward_kernel(self, input, kernel, stride, rate, output_, out=None):
         """G:4750."""
         B, IC, IR, ID, Ci, KC, KR, KD, Co, OC, OR, OD = self._conv3d_bwd_check(
             "dilated_conv3d_backward_kernel", input, kernel, stride, output_)
         cs, rs, ds = stride
         cr, rr, dr = rate
-        kernel_ = self.b.empty(kernel, self._shape(kernel))
+        kernel_ = self._out(out, kernel, self._shape(kernel))
         self.b.stub(_kind(input), "conv_dilated_cuboid_backward_kernel_im2col", input, kernel_,
                     output_, B, IC, IR, ID, Ci, KC, KR, KD, OC, OR, OD, Co, ds, rs, cs, dr, rr, cr)
         return kernel_
@@ -415,7 +438,7 @@ class NN:
     # roles; the kernel buffer [KC;KR;Cin;Cout] is then read as
     # [KC][KR][Cout][Cin] (a reinterpretation, not a transpose), G:5422-5439.
 
-    def transpose_conv2d(self, input, kernel, stride, padding=SAME):
+    def transpose_conv2d(self, input, kernel, stride, padding=SAME, out=None):
         """G:5371 transpose_conv2d."""
         _verify(self._dims(input) == 4 and self._dims(kernel) == 4 and len(stride) == 2,
                 "transpose_conv2d: bad dimensions")
@@ -424,37 +447,37 @@ class NN:
         _verify(Ci == kci, "transpose_conv2d: channel mismatch")
         cs, rs = stride
         OC, OR = calc_transpose_conv2d_output_shape(padding, IC, IR, KC, KR, rs, cs)
-        output = self.b.empty(input, (B, OC, OR, Co))
+        output = self._out(out, input, (B, OC, OR, Co))
         self.b.stub(_kind(input), "conv_spatial_backward_input", output, kernel, input, B, OC, OR,
                     Co, KC, KR, IC, IR, Ci, rs, cs, 1, 1)
         return output
 
-    def transpose_conv2d_backward_input(self, input, kernel, stride, output_):
+    def transpose_conv2d_backward_input(self, input, kernel, stride, output_, out=None):
         """G:5713: a forward conv of output' with the SAME padding rule."""
         B, IC, IR, Ci, KC, KR, Co, OC, OR = self._conv2d_bwd_check(
             "transpose_conv2d_backward_input", input, kernel, stride, output_)
         cs, rs = stride
-        input_ = self.b.empty(input, self._shape(input))
+        input_ = self._out(out, input, self._shape(input))
         self.b.stub(_kind(input), "conv_spatial", output_, kernel, input_, B, OC, OR, Co, KC, KR,
                     IC, IR, Ci, rs, cs, 0, 1, 1)
         return input_
 
-    def transpose_conv2d_backward_kernel(self, input, kernel, stride, output_):
+    def transpose_conv2d_backward_kernel(self, input, kernel, stride, output_, out=None):
         """G:5514."""
         B, IC, IR, Ci, KC, KR, Co, OC, OR = self._conv2d_bwd_check(
             "transpose_conv2d_backward_kernel", input, kernel, stride, output_)
         cs, rs = stride
-        kernel_ = self.b.empty(kernel, self._shape(kernel))
+        kernel_ = self._out(out, kernel, self._shape(kernel))
         self.b.stub(_kind(input), "conv_spatial_backward_kernel", output_, kernel_, input, B, OC,
                     OR, Co, KC, KR, IC, IR, Ci, rs, cs, 1, 1)
         return kernel_
 
-    def transpose_conv1d(self, input, kernel, stride, padding=SAME):
+    def transpose_conv1d(self, input, kernel, stride, padding=SAME, out=None):
         B, IC, Ci = self._shape(input)
         KC, _, Co = self._shape(kernel)
         y = self.transpose_conv2d(self.b.reshape(input, (B, 1, IC, Ci)),
                                   self.b.reshape(kernel, (1, KC, Ci, Co)), [1, stride[0]],
-                                  padding)
+                                  padding, out=self._ob(out))
         return self.b.reshape(y, (B, self._shape(y)[2], Co))
 
     def _as2d(self, input, kernel, output_):
@@ -474,40 +497,42 @@ class NN:
             dy = self.b.reshape(output_, (ob, 1, OC, oco))
         return x, w, dy
 
-    def transpose_conv1d_backward_input(self, input, kernel, stride, output_):
+    def transpose_conv1d_backward_input(self, input, kernel, stride, output_, out=None):
         """G:6570 transpose_conv1d_backward_input."""
         x, w, dy = self._as2d(input, kernel, output_)
-        dx = self.transpose_conv2d_backward_input(x, w, [1, stride[0]], dy)
+        dx = self.transpose_conv2d_backward_input(x, w, [1, stride[0]], dy, out=self._ob(out))
         return self.b.reshape(dx, self._shape(input))
 
-    def transpose_conv1d_backward_kernel(self, input, kernel, stride, output_):
+    def transpose_conv1d_backward_kernel(self, input, kernel, stride, output_, out=None):
         """G:6732 transpose_conv1d_backward_kernel."""
         x, w, dy = self._as2d(input, kernel, output_)
-        dw = self.transpose_conv2d_backward_kernel(x, w, [1, stride[0]], dy)
+        dw = self.transpose_conv2d_backward_kernel(x, w, [1, stride[0]], dy, out=self._ok(out))
         return self.b.reshape(dw, self._shape(kernel))
 
-    def dilated_conv1d(self, input, kernel, stride, rate, padding=SAME):
+    def dilated_conv1d(self, input, kernel, stride, rate, padding=SAME, out=None):
         """G:4967 dilated_conv1d: the 2-D view with stride [1; s]; `rate` is
         handed to dilated_conv2d unchanged, as Owl does (two entries)."""
         _verify(len(stride) == 1, "dilated_conv1d: stride dimension should be 1")
         x, w, _ = self._as2d(input, kernel, None)
-        y = self.dilated_conv2d(x, w, [1, stride[0]], list(rate), padding)
+        y = self.dilated_conv2d(x, w, [1, stride[0]], list(rate), padding, out=self._ob(out))
         B, _, OC, Co = self._shape(y)
         return self.b.reshape(y, (B, OC, Co))
 
-    def dilated_conv1d_backward_input(self, input, kernel, stride, rate, output_):
+    def dilated_conv1d_backward_input(self, input, kernel, stride, rate, output_, out=None):
         """G:5054 dilated_conv1d_backward_input."""
         x, w, dy = self._as2d(input, kernel, output_)
-        dx = self.dilated_conv2d_backward_input(x, w, [1, stride[0]], list(rate), dy)
+        dx = self.dilated_conv2d_backward_input(x, w, [1, stride[0]], list(rate), dy,
+                                                out=self._ob(out))
         return self.b.reshape(dx, self._shape(input))
 
-    def dilated_conv1d_backward_kernel(self, input, kernel, stride, rate, output_):
+    def dilated_conv1d_backward_kernel(self, input, kernel, stride, rate, output_, out=None):
         """G:5210 dilated_conv1d_backward_kernel."""
         x, w, dy = self._as2d(input, kernel, output_)
-        dw = self.dilated_conv2d_backward_kernel(x, w, [1, stride[0]], list(rate), dy)
+        dw = self.dilated_conv2d_backward_kernel(x, w, [1, stride[0]], list(rate), dy,
+                                                 out=self._ok(out))
         return self.b.reshape(dw, self._shape(kernel))
 
-    def transpose_conv3d(self, input, kernel, stride, padding=SAME):
+    def transpose_conv3d(self, input, kernel, stride, padding=SAME, out=None):
         """G:5915 transpose_conv3d."""
         _verify(self._dims(input) == 5 and self._dims(kernel) == 5 and len(stride) == 3,
                 "transpose_conv3d: bad dimensions")
@@ -517,54 +542,54 @@ class NN:
         cs, rs, ds = stride
         OC, OR, OD = calc_transpose_conv3d_output_shape(padding, IC, IR, ID, KC, KR, KD, rs, cs,
                                                         ds)
-        output = self.b.empty(input, (B, OC, OR, OD, Co))
+        output = self._out(out, input, (B, OC, OR, OD, Co))
         self.b.stub(_kind(input), "conv_cuboid_backward_input_im2col", output, kernel, input, B,
                     OC, OR, OD, Co, KC, KR, KD, IC, IR, ID, Ci, ds, rs, cs)
         return output
 
-    def transpose_conv3d_backward_input(self, input, kernel, stride, output_):
+    def transpose_conv3d_backward_input(self, input, kernel, stride, output_, out=None):
         """G:6072."""
         B, IC, IR, ID, Ci, KC, KR, KD, Co, OC, OR, OD = self._conv3d_bwd_check(
             "transpose_conv3d_backward_input", input, kernel, stride, output_)
         cs, rs, ds = stride
-        input_ = self.b.empty(input, self._shape(input))
+        input_ = self._out(out, input, self._shape(input))
         self.b.stub(_kind(input), "conv_cuboid_im2col", output_, kernel, input_, B, OC, OR, OD,
                     Co, KC, KR, KD, IC, IR, ID, Ci, ds, rs, cs, 0)
         return input_
 
-    def transpose_conv3d_backward_kernel(self, input, kernel, stride, output_):
+    def transpose_conv3d_backward_kernel(self, input, kernel, stride, output_, out=None):
         """G:6277."""
         B, IC, IR, ID, Ci, KC, KR, KD, Co, OC, OR, OD = self._conv3d_bwd_check(
             "transpose_conv3d_backward_kernel", input, kernel, stride, output_)
         cs, rs, ds = stride
-        kernel_ = self.b.empty(kernel, self._shape(kernel))
+        kernel_ = self._out(out, kernel, self._shape(kernel))
         self.b.stub(_kind(input), "conv_cuboid_backward_kernel_im2col", output_, kernel_, input,
                     B, OC, OR, OD, Co, KC, KR, KD, IC, IR, ID, Ci, ds, rs, cs)
         return kernel_
 
     # ======================= pooling (G:6905-8200) =======================
 
-    def _pool2d(self, which, padding, input, kernel, stride):
+    def _pool2d(self, which, padding, input, kernel, stride, out=None):
         _verify(self._dims(input) == 4 and len(kernel) == 2 and len(stride) == 2,
                 f"{which}_pool2d: bad dimensions")
         B, IC, IR, C = self._shape(input)
         KC, KR = kernel
         cs, rs = stride
         OC, OR = calc_conv2d_output_shape(padding, IC, IR, KC, KR, rs, cs)
-        output = self.b.empty(input, (B, OC, OR, C))
+        output = self._out(out, input, (B, OC, OR, C))
         self.b.stub(_kind(input), f"{which}pool_spatial", input, output, B, IC, IR, C, KC, KR, OC,
                     OR, rs, cs, _pad_typ(padding), 1, 1)
         return output
 
-    def max_pool2d(self, input, kernel, stride, padding=SAME):
+    def max_pool2d(self, input, kernel, stride, padding=SAME, out=None):
         """G:6905 max_pool2d ?padding input kernel stride."""
-        return self._pool2d("max", padding, input, kernel, stride)
+        return self._pool2d("max", padding, input, kernel, stride, out)
 
-    def avg_pool2d(self, input, kernel, stride, padding=SAME):
+    def avg_pool2d(self, input, kernel, stride, padding=SAME, out=None):
         """G:7080 avg_pool2d."""
-        return self._pool2d("avg", padding, input, kernel, stride)
+        return self._pool2d("avg", padding, input, kernel, stride, out)
 
-    def max_pool2d_argmax(self, input, kernel, stride, padding=SAME):
+    def max_pool2d_argmax(self, input, kernel, stride, padding=SAME, out=None, out_argmax=None):
         """G:7517 max_pool2d_argmax: (values, int64 flat indices)."""
         _verify(self._dims(input) == 4 and len(kernel) == 2 and len(stride) == 2,
                 "max_pool2d_argmax: bad dimensions")
@@ -573,13 +598,13 @@ class NN:
         cs, rs = stride
         OC, OR = calc_conv2d_output_shape(padding, IC, IR, KC, KR, rs, cs)
         pt, pl, _, _ = calc_conv2d_padding(IC, IR, KC, KR, OC, OR, rs, cs)
-        output = self.b.empty(input, (B, OC, OR, C))
-        argmax = self.b.empty(input, (B, OC, OR, C), dtype=_int64_like(input))
+        output = self._out(out, input, (B, OC, OR, C))
+        argmax = self._out(out_argmax, input, (B, OC, OR, C), _int64_like(input))
         self.b.stub(_kind(input), "maxpool_argmax_spatial", input, output, argmax, B, IC, IR, C,
                     KC, KR, OC, OR, rs, cs, pt, pl)
         return output, argmax
 
-    def _pool2d_backward(self, which, padding, input, kernel, stride, output_):
+    def _pool2d_backward(self, which, padding, input, kernel, stride, output_, out=None):
         _verify(self._dims(input) == 4 and len(kernel) == 2 and len(stride) == 2,
                 f"{which}_pool2d_backward: bad dimensions")
         B, IC, IR, C = self._shape(input)
@@ -587,7 +612,7 @@ class NN:
         cs, rs = stride
         OC, OR = calc_conv2d_output_shape(padding, IC, IR, KC, KR, rs, cs)
         pt, pl, _, _ = calc_conv2d_padding(IC, IR, KC, KR, OC, OR, rs, cs)
-        input_ = self.b.empty(input, self._shape(input))
+        input_ = self._out(out, input, self._shape(input))
         # avg: Owl's OCaml wrapper passes input' as the dummy first argument
         # (owl_ndarray_pool.ml:85-118); the stub never reads it.
         first = input if which == "max" else input_
@@ -595,85 +620,85 @@ class NN:
                     IR, C, KC, KR, OC, OR, rs, cs, pt, pl)
         return input_
 
-    def max_pool2d_backward(self, padding, input, kernel, stride, output_):
+    def max_pool2d_backward(self, padding, input, kernel, stride, output_, out=None):
         """G:7715 max_pool2d_backward padding input kernel stride output'."""
-        return self._pool2d_backward("max", padding, input, kernel, stride, output_)
+        return self._pool2d_backward("max", padding, input, kernel, stride, output_, out)
 
-    def avg_pool2d_backward(self, padding, input, kernel, stride, output_):
+    def avg_pool2d_backward(self, padding, input, kernel, stride, output_, out=None):
         """G:8035 avg_pool2d_backward."""
-        return self._pool2d_backward("avg", padding, input, kernel, stride, output_)
+        return self._pool2d_backward("avg", padding, input, kernel, stride, output_, out)
 
-    def _pool3d(self, which, padding, input, kernel, stride):
+    def _pool3d(self, which, padding, input, kernel, stride, out=None):
         _verify(self._dims(input) == 5 and len(kernel) == 3 and len(stride) == 3,
                 f"{which}_pool3d: bad dimensions")
         B, IC, IR, ID, C = self._shape(input)
         KC, KR, KD = kernel
         cs, rs, ds = stride
         OC, OR, OD = calc_conv3d_output_shape(padding, IC, IR, ID, KC, KR, KD, rs, cs, ds)
-        output = self.b.empty(input, (B, OC, OR, OD, C))
+        output = self._out(out, input, (B, OC, OR, OD, C))
         self.b.stub(_kind(input), f"{which}pool_cuboid", input, output, B, IC, IR, ID, C, KC, KR,
                     KD, OC, OR, OD, ds, rs, cs, _pad_typ(padding))
         return output
 
-    def max_pool3d(self, input, kernel, stride, padding=SAME):
+    def max_pool3d(self, input, kernel, stride, padding=SAME, out=None):
         """G:7255 max_pool3d."""
-        return self._pool3d("max", padding, input, kernel, stride)
+        return self._pool3d("max", padding, input, kernel, stride, out)
 
-    def avg_pool3d(self, input, kernel, stride, padding=SAME):
+    def avg_pool3d(self, input, kernel, stride, padding=SAME, out=None):
         """G:7386 avg_pool3d."""
-        return self._pool3d("avg", padding, input, kernel, stride)
+        return self._pool3d("avg", padding, input, kernel, stride, out)
 
-    def _pool3d_backward(self, which, padding, input, kernel, stride, output_):
+    def _pool3d_backward(self, which, padding, input, kernel, stride, output_, out=None):
         _verify(self._dims(input) == 5 and len(kernel) == 3 and len(stride) == 3,
                 f"{which}_pool3d_backward: bad dimensions")
         B, IC, IR, ID, C = self._shape(input)
         KC, KR, KD = kernel
         cs, rs, ds = stride
         OC, OR, OD = calc_conv3d_output_shape(padding, IC, IR, ID, KC, KR, KD, rs, cs, ds)
-        input_ = self.b.empty(input, self._shape(input))
+        input_ = self._out(out, input, self._shape(input))
         first = input if which == "max" else input_
         # Stride order col, row, dpt (G:7627-7647, owl_ndarray_pool_impl.h:324-331).
         self.b.stub(_kind(input), f"{which}pool_cuboid_backward", first, output_, input_, B, IC,
                     IR, ID, C, KC, KR, KD, OC, OR, OD, cs, rs, ds, _pad_typ(padding))
         return input_
 
-    def max_pool3d_backward(self, padding, input, kernel, stride, output_):
+    def max_pool3d_backward(self, padding, input, kernel, stride, output_, out=None):
         """G:7584 max_pool3d_backward."""
-        return self._pool3d_backward("max", padding, input, kernel, stride, output_)
+        return self._pool3d_backward("max", padding, input, kernel, stride, output_, out)
 
-    def avg_pool3d_backward(self, padding, input, kernel, stride, output_):
+    def avg_pool3d_backward(self, padding, input, kernel, stride, output_, out=None):
         """G:7906 avg_pool3d_backward."""
-        return self._pool3d_backward("avg", padding, input, kernel, stride, output_)
+        return self._pool3d_backward("avg", padding, input, kernel, stride, output_, out)
 
-    def max_pool1d(self, input, kernel, stride, padding=SAME):
+    def max_pool1d(self, input, kernel, stride, padding=SAME, out=None):
         B, IC, C = self._shape(input)
         y = self.max_pool2d(self.b.reshape(input, (B, 1, IC, C)), [1, kernel[0]],
-                            [1, stride[0]], padding)
+                            [1, stride[0]], padding, out=self._ob(out))
         return self.b.reshape(y, (B, self._shape(y)[2], C))
 
-    def avg_pool1d(self, input, kernel, stride, padding=SAME):
+    def avg_pool1d(self, input, kernel, stride, padding=SAME, out=None):
         B, IC, C = self._shape(input)
         y = self.avg_pool2d(self.b.reshape(input, (B, 1, IC, C)), [1, kernel[0]],
-                            [1, stride[0]], padding)
+                            [1, stride[0]], padding, out=self._ob(out))
         return self.b.reshape(y, (B, self._shape(y)[2], C))
 
-    def _pool1d_backward(self, which, padding, input, kernel, stride, output_):
+    def _pool1d_backward(self, which, padding, input, kernel, stride, output_, out=None):
         _verify(self._dims(input) == 3 and len(kernel) == 1 and len(stride) == 1,
                 f"{which}_pool1d_backward: bad dimensions")
         B, IC, C = self._shape(input)
         ob, OC, oc = self._shape(output_)
         dx = self._pool2d_backward(which, padding, self.b.reshape(input, (B, 1, IC, C)),
                                    [1, kernel[0]], [1, stride[0]],
-                                   self.b.reshape(output_, (ob, 1, OC, oc)))
+                                   self.b.reshape(output_, (ob, 1, OC, oc)), self._ob(out))
         return self.b.reshape(dx, (B, IC, C))
 
-    def max_pool1d_backward(self, padding, input, kernel, stride, output_):
+    def max_pool1d_backward(self, padding, input, kernel, stride, output_, out=None):
         """G:7840 max_pool1d_backward (the 2-D view [B;1;W;C], window [1;k])."""
-        return self._pool1d_backward("max", padding, input, kernel, stride, output_)
+        return self._pool1d_backward("max", padding, input, kernel, stride, output_, out)
 
-    def avg_pool1d_backward(self, padding, input, kernel, stride, output_):
+    def avg_pool1d_backward(self, padding, input, kernel, stride, output_, out=None):
         """G:8158 avg_pool1d_backward."""
-        return self._pool1d_backward("avg", padding, input, kernel, stride, output_)
+        return self._pool1d_backward("avg", padding, input, kernel, stride, output_, out)
 
 
 def _int64_like(a) -> Any:
