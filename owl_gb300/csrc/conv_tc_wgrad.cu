@@ -31,18 +31,18 @@ namespace {
 
 using namespace ptx;
 
-// Warp roles as in the forward kernel: MMA warp 0 keeps scheduler 0 nearly
-// to itself (warps 4 and 8 idle, epilogue warp 12), nine producer warps on
-// schedulers 1-3, epilogue warps 12-15 on TMEM lane quadrants 0-3.
+// Warp roles.  The accumulator is drained once per CTA, after the last
+// pixel tile, so every warp but the MMA issuer (warp 0) stages operands;
+// warps 12-15, one per TMEM lane quadrant, then drain the accumulator.
+// (Measured on GB300: 15 producer warps beat 9 or 12 here even though three
+// of them share the MMA warp's scheduler.)
 constexpr int kWarps = 16;
 constexpr int kThreads = kWarps * 32;
 constexpr int kMmaWarp = 0;
 constexpr int kEpiWarp0 = 12;
-constexpr int kProducerWarps = 9;
+constexpr int kProducerWarps = kWarps - 1;
 constexpr int kProducerThreads = kProducerWarps * 32;
-__device__ __forceinline__ int producer_index(int warp) {
-  return (warp & 3) != 0 && warp < 12 ? (warp >> 2) * 3 + (warp & 3) - 1 : -1;
-}
+__device__ __forceinline__ int producer_index(int warp) { return warp - 1; }
 constexpr int kSmemMax = 232448;
 constexpr long long kSpinLimit = 4000000000LL;
 
@@ -56,6 +56,8 @@ struct WgParams {
   long long xsb, xsw, xsu, xsv, ysb, ysw, ysu, ysv;
   int Ci, Co, T, TG, n_tg, BN, n_nb, n_mb, R;
   int TU, TP;             // reduction tile: TU output rows (u) x 8 columns (v) = TP pixels
+  int YPS;                // dY plane stride in pixels: TP + 1, so that the 16-byte chunks
+                          // of one pixel fall in different shared-memory banks
   int u_tiles, v_tiles;
   long long total_tiles, tiles_per_range;
   int PS;                 // X halo plane stride in pixels (max over groups)
@@ -79,39 +81,6 @@ __device__ __forceinline__ bool wait_bar(uint32_t bar, uint32_t parity, volatile
       atomicExch(status, 1);
       return false;
     }
-  }
-}
-
-__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
-  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-  return *reinterpret_cast<uint32_t *>(&h);
-}
-__device__ __forceinline__ float bf16_round(float a) {
-  return __bfloat162float(__float2bfloat16_rn(a));
-}
-__device__ __forceinline__ uint32_t to_tf32(float a) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(a));
-  return r;
-}
-
-// Convert EPC floats and store one 16-byte chunk (plus its lo part).
-template <int KIND, int EPC>
-__device__ __forceinline__ void put_chunk(uint8_t *dst, uint32_t lo_off, const float (&v)[EPC]) {
-  uint4 hi;
-  if (KIND == K_TF32) {
-    hi = make_uint4(to_tf32(v[0]), to_tf32(v[1]), to_tf32(v[2]), to_tf32(v[3]));
-  } else {
-    hi = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]),
-                    pack_bf16(v[6], v[7]));
-  }
-  *reinterpret_cast<uint4 *>(dst) = hi;
-  if (KIND == K_BF16X3) {
-    float r[8];
-#pragma unroll
-    for (int e = 0; e < 8; ++e) r[e] = v[e] - bf16_round(v[e]);
-    *reinterpret_cast<uint4 *>(dst + lo_off) = make_uint4(
-        pack_bf16(r[0], r[1]), pack_bf16(r[2], r[3]), pack_bf16(r[4], r[5]), pack_bf16(r[6], r[7]));
   }
 }
 
@@ -152,7 +121,6 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
   // 8 consecutive output columns are 8 consecutive stored pixels.
   const int HW = maxw - minw + 1, HU = (p.TU - 1) * p.su + (maxu - minu) + 1;
   const int HVR = 8 + (maxv - minv) / p.sv, HV = p.sv * HVR;
-  const int HP = HW * HU * HV;
 
   uint8_t *xs = smem;
   uint8_t *ys = smem + (size_t)p.NS * PARTS * p.x_bytes;
@@ -193,8 +161,9 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
   const uint32_t tmem_base = *tmem_slot;
 
   const int pidx = producer_index(warp);
-  if (pidx >= 0) {
+  if (warp != kMmaWarp) {
     // ===================== producers: X halo + dY tile =====================
+    bool staged = true;
     long long k = 0;
     for (long long t = t_begin; t < t_end; ++t, ++k) {
       long long q = t;
@@ -204,8 +173,10 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
       const int b = (int)(q / p.OW);
       const int st = (int)(k % p.NS);
       if (!wait_bar(smem_u32(&empty[st]), (uint32_t)(((k / p.NS) & 1) ^ 1), abort_flag,
-                    p.status))
-        goto done;
+                    p.status)) {
+        staged = false;
+        break;
+      }
       uint8_t *xd = xs + (size_t)st * PARTS * p.x_bytes;
       uint8_t *yd = ys + (size_t)st * PARTS * p.y_bytes;
       // X halo: rows (w, u, residue class) of HVR pixels x 128 channels of ci block mb
@@ -233,7 +204,7 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
       {
         const int cb0 = nb * p.BN;
         stage::stage_rows<KIND, EPC, 4>(
-            yd, p.y_bytes, (uint32_t)p.TP * 16, p.TU, 8, YPL, p.Co - cb0, p.vec_y != 0, pidx,
+            yd, p.y_bytes, (uint32_t)p.YPS * 16, p.TU, 8, YPL, p.Co - cb0, p.vec_y != 0, pidx,
             kProducerWarps, lane, [&](int r) {
               const int ou = u0 + r;
               stage::Row row;
@@ -250,12 +221,45 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
       fence_proxy_async();
       mbar_arrive(smem_u32(&full[st]));
     }
-  } else if (warp == kMmaWarp) {
+    if (staged && warp >= kEpiWarp0) {
+      // ===================== epilogue: TMEM -> partial dW =====================
+      const int q = warp & 3;
+      const int ci = mb * 128 + q * 32 + lane;
+      if (wait_bar(smem_u32(acc_full), 0, abort_flag, p.status)) {
+        tc_fence_after();
+        for (int i = 0; i < ntap; ++i) {
+          const int tt = tap0 + i;
+          float *out = p.out + (((long long)r * p.T + tt) * p.Ci + ci) * p.Co + nb * p.BN;
+          const uint32_t tcol = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(i * p.BN);
+          for (int c0 = 0; c0 < p.BN; c0 += 16) {
+            uint32_t rr[16];
+            tmem_ld16(tcol + (uint32_t)c0, rr);
+            tmem_ld_wait();
+            if (ci < p.Ci) {
+              const int n0 = nb * p.BN + c0;
+              if (p.vec_y && n0 + 16 <= p.Co && ((uintptr_t)(out + c0) % 16 == 0)) {
+#pragma unroll
+                for (int e = 0; e < 16; e += 4)
+                  *reinterpret_cast<float4 *>(out + c0 + e) =
+                      make_float4(__uint_as_float(rr[e]), __uint_as_float(rr[e + 1]),
+                                  __uint_as_float(rr[e + 2]), __uint_as_float(rr[e + 3]));
+              } else {
+#pragma unroll
+                for (int e = 0; e < 16; ++e)
+                  if (n0 + e < p.Co) out[c0 + e] = __uint_as_float(rr[e]);
+              }
+            }
+          }
+        }
+        tc_fence_before();
+      }
+    }
+  } else {
     // ===================== MMA issuer =====================
     if (lane == 0) {
       const uint32_t x0 = smem_u32(xs), y0 = smem_u32(ys);
       const uint32_t a_lbo = (uint32_t)(p.su * HV) * 16, a_sbo = (uint32_t)p.PS * 16;
-      const uint32_t b_lbo = 128, b_sbo = (uint32_t)p.TP * 16;
+      const uint32_t b_lbo = 128, b_sbo = (uint32_t)p.YPS * 16;
       const uint32_t xlo16 = p.x_bytes >> 4, ylo16 = p.y_bytes >> 4;
       long long k = 0;
       uint32_t acc = 0;
@@ -299,40 +303,7 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
       while (!mbar_try_wait(smem_u32(drain), 0) && clock64() - t0 < kSpinLimit) {
       }
     }
-  } else if (warp >= kEpiWarp0) {
-    // ===================== epilogue: TMEM -> partial dW =====================
-    const int q = warp & 3;
-    const int ci = mb * 128 + q * 32 + lane;
-    if (wait_bar(smem_u32(acc_full), 0, abort_flag, p.status)) {
-      tc_fence_after();
-      for (int i = 0; i < ntap; ++i) {
-        const int tt = tap0 + i;
-        float *out = p.out + (((long long)r * p.T + tt) * p.Ci + ci) * p.Co + nb * p.BN;
-        const uint32_t tcol = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(i * p.BN);
-        for (int c0 = 0; c0 < p.BN; c0 += 16) {
-          uint32_t rr[16];
-          tmem_ld16(tcol + (uint32_t)c0, rr);
-          tmem_ld_wait();
-          if (ci < p.Ci) {
-            const int n0 = nb * p.BN + c0;
-            if (p.vec_y && n0 + 16 <= p.Co && ((uintptr_t)(out + c0) % 16 == 0)) {
-#pragma unroll
-              for (int e = 0; e < 16; e += 4)
-                *reinterpret_cast<float4 *>(out + c0 + e) =
-                    make_float4(__uint_as_float(rr[e]), __uint_as_float(rr[e + 1]),
-                                __uint_as_float(rr[e + 2]), __uint_as_float(rr[e + 3]));
-            } else {
-#pragma unroll
-              for (int e = 0; e < 16; ++e)
-                if (n0 + e < p.Co) out[c0 + e] = __uint_as_float(rr[e]);
-            }
-          }
-        }
-      }
-      tc_fence_before();
-    }
   }
-done:
   tc_fence_before();
   __syncthreads();
   if (warp == kMmaWarp) {
@@ -442,16 +413,21 @@ int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, c
   if (planned) break;
   p.TU = tu;
   p.TP = tu * 8;
+  p.YPS = p.TP + 1;
   for (int bn : {256, 128, 64, 32, 16}) {
     p.BN = std::min(bn, (p.Co + 15) / 16 * 16);
-    for (int tg = std::min(p.T, 16); tg >= 1 && !planned; --tg) {
-      if (p.T % tg != 0 || tg * p.BN > 512) continue;
+    // fewest tap groups whose accumulators fit TMEM (TG * BN <= 512 columns),
+    // taps spread evenly over them (the last group may be smaller)
+    const int tg_max = std::min(p.T, std::min(16, 512 / p.BN));
+    for (int n_tg = (p.T + tg_max - 1) / tg_max; n_tg <= p.T && !planned; ++n_tg) {
+      const int tg = (p.T + n_tg - 1) / n_tg;
+      if ((p.T + tg - 1) / tg != n_tg) continue;
       p.TG = tg;
-      p.n_tg = p.T / tg;
+      p.n_tg = n_tg;
       int maxHP = 0;
       for (int gi = 0; gi < p.n_tg; ++gi) {
         int mnw = 1 << 30, mnu = 1 << 30, mnv = 1 << 30, mxw = -1, mxu = -1, mxv = -1;
-        for (int i = 0; i < tg; ++i) {
+        for (int i = 0; i < tg && gi * tg + i < p.T; ++i) {
           const int t = gi * tg + i;
           const int kv = t % p.KV, ku = (t / p.KV) % p.KU, kw = t / (p.KV * p.KU);
           mnw = std::min(mnw, kw * p.dw); mxw = std::max(mxw, kw * p.dw);
@@ -464,7 +440,7 @@ int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, c
       p.PS = maxHP + (((1 - maxHP) % 8) + 8) % 8;
       if (p.PS >= 16384) continue;
       p.x_bytes = (unsigned)(128 * EB / 16) * (unsigned)p.PS * 16u;
-      p.y_bytes = (unsigned)(p.BN * EB / 16) * (unsigned)p.TP * 16u;
+      p.y_bytes = (unsigned)(p.BN * EB / 16) * (unsigned)p.YPS * 16u;
       p.NS = 2;
       const size_t need = (size_t)p.NS * parts * (p.x_bytes + p.y_bytes) + 256;
       if (need <= (size_t)kSmemMax) planned = true;
