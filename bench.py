@@ -663,16 +663,27 @@ def main():
         step()
     barrier()
     stream = torch.cuda.current_stream()
-    n0 = _lib.launch_count()
+    # The step runs as one CUDA graph (its 9 conv calls and their helper
+    # kernels captured once): the host issues one launch per step instead of
+    # ~20, as a training loop on this GPU would.  Every kernel of the step
+    # still runs on every replay.
+    graph = torch.cuda.CUDAGraph()
+    n_cap = _lib.launch_count()
+    with torch.cuda.graph(graph):
+        step()
+    launches_per_step = _lib.launch_count() - n_cap
+    for _ in range(args.warmup):
+        graph.replay()
+    barrier()
     with Clocks(local) as clk:
         barrier()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(args.steps):
-            step()
+            graph.replay()
         e1.record(stream)
         barrier()
-    launches = _lib.launch_count() - n0
+    launches = launches_per_step * args.steps
     ms = e0.elapsed_time(e1)
     if world > 1:
         t = torch.tensor([ms], device="cuda")
@@ -680,22 +691,39 @@ def main():
         ms = float(t.item())
     ms_per_step = ms / args.steps
     value = flops_step * world / (ms_per_step / 1e3) / 1e12
+    del graph
 
-    # ---- per-kernel timing for the roofline (dominant conv call) ----
+    # the same step issued call by call from Python (no graph), for reference
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    barrier()
+    eager_ms = e0.elapsed_time(e1) / args.steps
+
+    # ---- per-kernel device time (each call captured 5 times in a graph) ----
     per = []
     for (name, xs, ks, st, r, p), (x, w, dy) in zip(LAYERS, dev_data):
         f = layer_flops(xs, ks, st, r, p)
         for op, fn in layer_calls(nn, x, w, dy, st, r, p):
             fn()
             torch.cuda.synchronize()
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             reps = 5
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                for _ in range(reps):
+                    fn()
+            g.replay()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
-            for _ in range(reps):
-                fn()
+            g.replay()
             b.record(stream)
             torch.cuda.synchronize()
             t = a.elapsed_time(b) / reps
+            del g
             per.append({"layer": name, "op": op, "ms": t, "tflops": f / (t / 1e3) / 1e12})
     hbm, bf16, src = peaks()
     byk = {f"{d['layer']}.{d['op']}": d for d in per}
@@ -714,6 +742,9 @@ def main():
         "metric": "conv2d fwd+bwd TFLOP/s (config 2: L1+L2+dilated)",
         "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "eager": {"ms_per_step": eager_ms,
+                  "value": flops_step * world / (eager_ms / 1e3) / 1e12,
+                  "note": "the same step issued call by call from Python, no CUDA graph"},
         "scaling": "weak", "vs_baseline": None, "dtype": PREC_DTYPE[args.precision],
         "data": "synthetic (seeded uniform[-1,1] inputs, N(0,2/fan_in) kernels, N(0,1) grads)",
         "config": {"workload": "owl conv2d c2: L1 [64;56;56;128]x[3;3;128;128] s1 SAME, "
@@ -728,6 +759,8 @@ def main():
         "roofline": roof("L1.fwd", "conv_tc_kernel"),
         "roofline_wgrad": roof("L1.bwd_kernel", "wgrad_tc_kernel"),
         "gpu_launches": launches,
+        "timing": "step captured once as a CUDA graph and replayed; CUDA events on the "
+                  "replaying stream; per_kernel: 5 calls of one op in a graph",
         "clocks": clk.summary(),
     }
 
@@ -740,13 +773,19 @@ def main():
                     run_layer(nn32, x, w, dy, st, r, p)
             step32()
             torch.cuda.synchronize()
+            g32 = torch.cuda.CUDAGraph()  # timed like the main step
+            with torch.cuda.graph(g32):
+                step32()
+            g32.replay()
+            torch.cuda.synchronize()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
             for _ in range(2):
-                step32()
+                g32.replay()
             b.record(stream)
             torch.cuda.synchronize()
             ms32 = a.elapsed_time(b) / 2
+            del g32
             result["fp32_plain"] = {"value": flops_step / (ms32 / 1e3) / 1e12, "unit": "TFLOP/s",
                                     "ms_per_step": ms32,
                                     "speedup": (flops_step / (ms_per_step / 1e3)) /
