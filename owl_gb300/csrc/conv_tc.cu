@@ -30,6 +30,8 @@
 // Backward-input with stride 1 is the same computation on dY with the kernel
 // flipped in every spatial axis and its channel axes exchanged:
 //   dX[i] = sum_t dY[i + p - t*d] W[t]^T = sum_t' dY[i - ((K-1)d - p) + t'd] W[K-1-t']^T.
+// With stride s it splits into s^d residue classes of dX, each such a
+// stride-1 correlation over the taps that reach it (run_bwd_input_strided).
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -77,6 +79,7 @@ struct TcParams {
   int sw, su, sv;          // strides along w, u, v
   int HW, HU, HV, HVR, HP, PS;  // halo rows along w, u; pixels per u-row (= sv * HVR)
   int n_tiles, u_tiles, v_tiles;
+  int NCT, n_groups;  // output-channel tiles per CTA tile (1 or 2), and tile groups
   long long total_tiles;
   unsigned halo_bytes, b_bytes;  // one halo stage / one weight slot (TPS taps), per part
   unsigned tile_bytes;           // one tap's weight tile (BN x CB)
@@ -110,8 +113,8 @@ struct Tile {
 
 __device__ __forceinline__ Tile decode_tile(const TcParams &p, long long t) {
   Tile r;
-  r.nt = (int)(t % p.n_tiles);
-  t /= p.n_tiles;
+  r.nt = (int)(t % p.n_groups);  // co-tile group: tiles nt*NCT .. nt*NCT+NCT-1
+  t /= p.n_groups;
   r.v0 = (int)(t % p.v_tiles) * 8;
   t /= p.v_tiles;
   r.u0 = (int)(t % p.u_tiles) * 16 * p.MH;
@@ -344,7 +347,8 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
         const uint32_t aph = (uint32_t)((tc >> 1) & 1);
         if (!wait_bar(smem_u32(&acc_empty[abuf]), aph ^ 1, abort_flag, p.status)) break;
         tc_fence_after();
-        const uint32_t d0 = tmem_base + (uint32_t)(abuf * p.MH * 128);
+        const uint32_t d0 = tmem_base + (uint32_t)(abuf * p.NCT * p.MH * 128);
+        const int nct = min(p.NCT, p.n_tiles - decode_tile(p, t).nt * p.NCT);
         uint32_t acc = 0;
         bool ok = true;
         for (int cb = 0; cb < p.NCB && ok; ++cb, ++kh) {
@@ -366,20 +370,47 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
             for (int tap = t0; tap < t1; ++tap) {
               const uint64_t wd0 = wslot + (uint64_t)((tap - t0) * tile16);
               const uint64_t xd0 = xd_stage + (uint64_t)tap_off[tap];
+              if (nct == 1) {
 #pragma unroll 4
-              for (int s = 0; s < ksteps; ++s) {
-                const uint64_t wd = wd0 + (uint64_t)(s * wstep16);  // A: 128 output channels
-                const uint64_t xd = xd0 + (uint64_t)(s * xstep16);  // B: 16*MH pixel groups
-                if (KIND == K_TF32) {
-                  mma_tf32(d0, wd, xd, p.idesc, acc);
-                } else {
-                  mma_bf16(d0, wd, xd, p.idesc, acc);
-                  if (KIND == K_BF16X3) {
-                    mma_bf16(d0, wd + (uint64_t)wlo16, xd, p.idesc, 1);
-                    mma_bf16(d0, wd, xd + (uint64_t)xlo16, p.idesc, 1);
+                for (int s = 0; s < ksteps; ++s) {
+                  const uint64_t wd = wd0 + (uint64_t)(s * wstep16);  // A: 128 output channels
+                  const uint64_t xd = xd0 + (uint64_t)(s * xstep16);  // B: 16*MH pixel groups
+                  if (KIND == K_TF32) {
+                    mma_tf32(d0, wd, xd, p.idesc, acc);
+                  } else {
+                    mma_bf16(d0, wd, xd, p.idesc, acc);
+                    if (KIND == K_BF16X3) {
+                      mma_bf16(d0, wd + (uint64_t)wlo16, xd, p.idesc, 1);
+                      mma_bf16(d0, wd, xd + (uint64_t)xlo16, p.idesc, 1);
+                    }
                   }
+                  acc = 1;
                 }
-                acc = 1;
+              } else {
+                // two co tiles share the pixel operand; alternating between
+                // their accumulators keeps N = 128 MMAs at full rate
+                const uint32_t d1 = d0 + (uint32_t)(p.MH * 128);
+                const uint64_t wd1 = wd0 + (uint64_t)(p.TPS * tile16);
+#pragma unroll 2
+                for (int s = 0; s < ksteps; ++s) {
+                  const uint64_t xd = xd0 + (uint64_t)(s * xstep16);
+                  const uint64_t wa = wd0 + (uint64_t)(s * wstep16);
+                  const uint64_t wb = wd1 + (uint64_t)(s * wstep16);
+                  if (KIND == K_TF32) {
+                    mma_tf32(d0, wa, xd, p.idesc, acc);
+                    mma_tf32(d1, wb, xd, p.idesc, acc);
+                  } else {
+                    mma_bf16(d0, wa, xd, p.idesc, acc);
+                    mma_bf16(d1, wb, xd, p.idesc, acc);
+                    if (KIND == K_BF16X3) {
+                      mma_bf16(d0, wa + (uint64_t)wlo16, xd, p.idesc, 1);
+                      mma_bf16(d1, wb + (uint64_t)wlo16, xd, p.idesc, 1);
+                      mma_bf16(d0, wa, xd + (uint64_t)xlo16, p.idesc, 1);
+                      mma_bf16(d1, wb, xd + (uint64_t)xlo16, p.idesc, 1);
+                    }
+                  }
+                  acc = 1;
+                }
               }
             }
             mma_commit(smem_u32(&b_empty[bs]));
@@ -411,14 +442,20 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
               goto loader_done;
             const int t0 = sl * p.TPS, nt_ = min(p.T - t0, p.TPS);
             const uint32_t bytes = (uint32_t)nt_ * p.tile_bytes;
+            const int nct = min(p.NCT, p.n_tiles - tl.nt * p.NCT);
             const uint32_t bar = smem_u32(&b_full[bs]);
-            mbar_arrive_expect_tx(bar, PARTS * bytes);
-            const size_t src = ((size_t)(tl.nt * p.NCB + cb) * p.T + t0) * p.tile_bytes;
-            const uint32_t dst = b0 + (uint32_t)bs * PARTS * p.b_bytes;
-            for (uint32_t o = 0; o < bytes; o += 32768u) {
-              const uint32_t n = min(32768u, bytes - o);
-              bulk_g2s(dst + o, p.wt_hi + src + o, n, bar);
-              if (PARTS == 2) bulk_g2s(dst + p.b_bytes + o, p.wt_lo + src + o, n, bar);
+            mbar_arrive_expect_tx(bar, PARTS * bytes * (uint32_t)nct);
+            // slot layout: [co tile c][tap][...], co tile c at c * TPS tiles
+            for (int c = 0; c < nct; ++c) {
+              const size_t src =
+                  ((size_t)((tl.nt * p.NCT + c) * p.NCB + cb) * p.T + t0) * p.tile_bytes;
+              const uint32_t dst = b0 + (uint32_t)bs * PARTS * p.b_bytes +
+                                   (uint32_t)(c * p.TPS) * p.tile_bytes;
+              for (uint32_t o = 0; o < bytes; o += 32768u) {
+                const uint32_t n = min(32768u, bytes - o);
+                bulk_g2s(dst + o, p.wt_hi + src + o, n, bar);
+                if (PARTS == 2) bulk_g2s(dst + p.b_bytes + o, p.wt_lo + src + o, n, bar);
+              }
             }
           }
       }
@@ -446,20 +483,25 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
         break;
       tc_fence_after();
       // TMEM lane = output channel, column = pixel (group g = col / 8, v = col % 8)
-      const int co = tl.nt * 128 + q * 32 + lane;
-      const bool co_ok = co < p.Cout;
-      const uint32_t tcol = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(abuf * p.MH * 128);
-      float *ybase = p.y + ((long long)tl.b * p.ysb + (long long)tl.ow * p.ysw) * p.Cout + co;
-      for (int c0 = 0; c0 < p.MH * 128; c0 += 16) {
-        uint32_t r[16];
-        tmem_ld16(tcol + (uint32_t)c0, r);
-        tmem_ld_wait();
+      const int nct = min(p.NCT, p.n_tiles - tl.nt * p.NCT);
+      for (int ct = 0; ct < nct; ++ct) {
+        const int co = (tl.nt * p.NCT + ct) * 128 + q * 32 + lane;
+        const bool co_ok = co < p.Cout;
+        const uint32_t tcol = tmem_base + ((uint32_t)(q * 32) << 16) +
+                              (uint32_t)((abuf * p.NCT + ct) * p.MH * 128);
+        float *ybase = p.y + ((long long)tl.b * p.ysb + (long long)tl.ow * p.ysw) * p.Cout + co;
+        for (int c0 = 0; c0 < p.MH * 128; c0 += 16) {
+          uint32_t r[16];
+          tmem_ld16(tcol + (uint32_t)c0, r);
+          tmem_ld_wait();
 #pragma unroll
-        for (int e = 0; e < 16; ++e) {
-          const int c = c0 + e;
-          const int u = tl.u0 + (c >> 3), v = tl.v0 + (c & 7);
-          if (co_ok && u < p.OU && v < p.OV)
-            ybase[((long long)u * p.ysu + (long long)v * p.ysv) * p.Cout] = __uint_as_float(r[e]);
+          for (int e = 0; e < 16; ++e) {
+            const int c = c0 + e;
+            const int u = tl.u0 + (c >> 3), v = tl.v0 + (c & 7);
+            if (co_ok && u < p.OU && v < p.OV)
+              ybase[((long long)u * p.ysu + (long long)v * p.ysv) * p.Cout] =
+                  __uint_as_float(r[e]);
+          }
         }
       }
       tc_fence_before();
@@ -475,14 +517,23 @@ done:
   }
 }
 
+// Which kernel taps a convolution uses, per view axis (w, u, v): tap t' of
+// the K[a] used along axis a is original tap base[a] + mul[a] * t' of the
+// KO[a] the kernel tensor has.  Forward: base 0, mul 1.  Backward-input
+// (flipped kernel): base K-1, mul -1.  One residue class of a strided
+// backward-input: the taps that reach it, largest first.
+struct TapMap {
+  int K[3], base[3], mul[3], KO[3];
+};
+
 // Re-lay the kernel tensor into B-tile images: [ntile][cblock][tap][chunk j]
 // [n < BN][16 B], element (n, k) with k = cb*CPB + j*EPC + e.  FWD reads
-// W[tap][k][n]; BWDI reads the flipped, channel-exchanged kernel
-// W[T-1-tap][n][k] (kernel layout [tap][Ci][Co]).
+// W[tap][k][n]; BWDI reads the channel-exchanged kernel W[tap][n][k] (kernel
+// layout [tap][Ci][Co]), taps chosen by `tm`.
 template <int KIND>
 __global__ void prep_weights(const float *__restrict__ w, uint8_t *__restrict__ hi,
                              uint8_t *__restrict__ lo, int T, int Ci, int Co, int K, int N,
-                             int BN, int CPB, int NCB, int n_tiles, int bwd_input) {
+                             int BN, int CPB, int NCB, int n_tiles, int bwd_input, TapMap tm) {
   constexpr int EPC = (KIND == K_TF32) ? 4 : 8;
   const int NCH = CPB / EPC;
   const long long total = (long long)n_tiles * NCB * T * NCH * BN;
@@ -495,14 +546,17 @@ __global__ void prep_weights(const float *__restrict__ w, uint8_t *__restrict__ 
     const int cb = (int)(r % NCB);
     const int nt = (int)(r / NCB);
     const int ng = nt * BN + n;
+    const int ta = tap / (tm.K[1] * tm.K[2]), tb = tap / tm.K[2] % tm.K[1], tc = tap % tm.K[2];
+    const long long orig =
+        ((long long)(tm.base[0] + tm.mul[0] * ta) * tm.KO[1] + (tm.base[1] + tm.mul[1] * tb)) *
+            tm.KO[2] + (tm.base[2] + tm.mul[2] * tc);
     float v[EPC];
 #pragma unroll
     for (int e = 0; e < EPC; ++e) {
       const int k = cb * CPB + j * EPC + e;
       float val = 0.f;
       if (k < K && ng < N) {
-        val = bwd_input ? w[((long long)(T - 1 - tap) * Ci + ng) * Co + k]
-                        : w[((long long)tap * Ci + k) * Co + ng];
+        val = bwd_input ? w[(orig * Ci + ng) * Co + k] : w[(orig * Ci + k) * Co + ng];
       }
       v[e] = val;
     }
@@ -525,21 +579,6 @@ __global__ void prep_weights(const float *__restrict__ w, uint8_t *__restrict__ 
     const long long off = tile * (long long)NCH * BN * 16 + ((long long)j * BN + n) * 16;
     *reinterpret_cast<uint4 *>(hi + off) = h4;
     if (KIND == K_BF16X3) *reinterpret_cast<uint4 *>(lo + off) = l4;
-  }
-}
-
-// dY [B][OC][OR][OD][Co] -> zero-filled dilated copy with dY[o] at o*stride.
-__global__ void dilate_dy(const float *__restrict__ dy, float *__restrict__ out, long long B,
-                          long long OC, long long OR, long long OD, long long Co, int sc, int sr,
-                          int sd, long long DC, long long DR, long long DD) {
-  const long long n = B * OC * OR * OD * Co;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    long long c = i % Co, t = i / Co;
-    long long od = t % OD; t /= OD;
-    long long orr = t % OR; t /= OR;
-    long long oc = t % OC, b = t / OC;
-    out[((((b * DC) + oc * sc) * DR + orr * sr) * DD + od * sd) * Co + c] = dy[i];
   }
 }
 
@@ -639,6 +678,10 @@ bool plan(TcParams &p, const View &v, int kind) {
       if (cb != cb0 && cb % 64 != 0 && cb != 32) continue;  // try cb0, then 64, 32
       TcParams q = p;
       q.MH = mh;
+      // 128-pixel tiles take two co tiles when there are two: the halo is
+      // staged once for both and their MMAs alternate accumulators
+      q.NCT = (mh == 1 && p.n_tiles >= 2) ? 2 : 1;
+      q.n_groups = (p.n_tiles + q.NCT - 1) / q.NCT;
       q.CB = cb;
       q.CPB = q.CB / EB;
       q.NCH = q.CB / 16;
@@ -656,16 +699,17 @@ bool plan(TcParams &p, const View &v, int kind) {
       const long long room = kSmemMax - fixed;
       if (room <= 0) continue;
       // at least two weight slots
-      const long long tps = std::min<long long>(q.T, room / (2LL * parts * q.tile_bytes));
+      const long long tps =
+          std::min<long long>(q.T, room / (2LL * parts * q.NCT * q.tile_bytes));
       if (tps < 1) continue;
       q.TPS = (int)tps;
       q.NSL = (q.T + q.TPS - 1) / q.TPS;
       q.TPS = (q.T + q.NSL - 1) / q.NSL;  // balance the slots
-      q.b_bytes = (unsigned)q.TPS * q.tile_bytes;
+      q.b_bytes = (unsigned)(q.NCT * q.TPS) * q.tile_bytes;
       q.NB = (int)std::min<long long>(4, room / ((long long)parts * q.b_bytes));
       if (q.NB < 2) continue;
       q.tmem_cols = 32;
-      while (q.tmem_cols < (unsigned)(2 * q.MH * 128)) q.tmem_cols <<= 1;
+      while (q.tmem_cols < (unsigned)(2 * q.NCT * q.MH * 128)) q.tmem_cols <<= 1;
       if (q.tmem_cols > 512) continue;
       const long long score = (long long)q.CB * 1000 + (long long)q.TPS * (q.NCH / 2);
       if (score > best_score) {
@@ -696,14 +740,11 @@ int launch(const TcParams &p, size_t smem, cudaStream_t s) {
   return kOk;
 }
 
-int run(int prec, const ConvGeom &g, bool bwd_input, const float *x, const float *w, float *y,
-        cudaStream_t s) {
-  // backward-input reads dY; with stride > 1 the caller passes dY dilated
-  // with zeros to a stride-1 geometry (dilate_dy), so strides are 1 here.
-  if (bwd_input && (g.sc != 1 || g.sr != 1 || g.sd != 1)) return kErrUnsupported;
-  if (g.sc > 8 || g.sr > 8 || g.sd > 8) return kErrUnsupported;
+// One launch over a view: `x` is read, `y` written, `tm` picks the taps of
+// the kernel tensor `w` ([taps][Ci][Co]); bwd_input exchanges its channels.
+int run_view(int prec, const View &v, const TapMap &tm, bool bwd_input, int Ci, int Co,
+             const float *x, const float *w, float *y, cudaStream_t s) {
   const int kind = prec == OWLGPU_PREC_TF32 ? K_TF32 : (prec == OWLGPU_PREC_BF16X3 ? K_BF16X3 : K_BF16);
-  const View v = make_view(g, bwd_input);
   if (v.OW * (long long)v.OU * v.OV * v.B == 0 || v.Cout == 0) return kOk;
   TcParams p{};
   if (v.Cin == 0 || !plan(p, v, kind)) return kErrUnsupported;
@@ -717,7 +758,7 @@ int run(int prec, const ConvGeom &g, bool bwd_input, const float *x, const float
   p.Cin = v.Cin; p.Cout = v.Cout;
   p.u_tiles = (v.OU + 16 * p.MH - 1) / (16 * p.MH);
   p.v_tiles = (v.OV + 7) / 8;
-  p.total_tiles = (long long)v.B * v.OW * p.u_tiles * p.v_tiles * p.n_tiles;
+  p.total_tiles = (long long)v.B * v.OW * p.u_tiles * p.v_tiles * p.n_groups;
   p.idesc = instr_desc(kind == K_TF32 ? 2u : 1u, (uint32_t)(128 * p.MH));
   p.vec_in = ((uintptr_t)x % 16 == 0) && (v.Cin % 4 == 0);
   p.vec_out = ((uintptr_t)y % 16 == 0) && (v.Cout % 4 == 0);
@@ -737,17 +778,16 @@ int run(int prec, const ConvGeom &g, bool bwd_input, const float *x, const float
     const long long n = (long long)p.n_tiles * p.NCB * p.T * p.NCH * p.BN;
     const int blocks = (int)std::min<long long>((n + 255) / 256, 4096);
     const int K = v.Cin, N = v.Cout;
-    const int Ci = (int)g.Ci, Co = (int)g.Co;
     if (kind == K_TF32)
       prep_weights<K_TF32><<<blocks, 256, 0, s>>>(w, (uint8_t *)wt, nullptr, p.T, Ci, Co, K, N,
-                                                  p.BN, p.CPB, p.NCB, p.n_tiles, bwd_input);
+                                                  p.BN, p.CPB, p.NCB, p.n_tiles, bwd_input, tm);
     else if (kind == K_BF16X3)
       prep_weights<K_BF16X3><<<blocks, 256, 0, s>>>(w, (uint8_t *)wt, (uint8_t *)wt + wt_bytes,
                                                     p.T, Ci, Co, K, N, p.BN, p.CPB, p.NCB,
-                                                    p.n_tiles, bwd_input);
+                                                    p.n_tiles, bwd_input, tm);
     else
       prep_weights<K_BF16><<<blocks, 256, 0, s>>>(w, (uint8_t *)wt, nullptr, p.T, Ci, Co, K, N,
-                                                  p.BN, p.CPB, p.NCB, p.n_tiles, bwd_input);
+                                                  p.BN, p.CPB, p.NCB, p.n_tiles, bwd_input, tm);
     cudaError_t e = cudaGetLastError();
     note_launch();
     if (e != cudaSuccess) {
@@ -764,6 +804,107 @@ int run(int prec, const ConvGeom &g, bool bwd_input, const float *x, const float
   return rc;
 }
 
+// The whole kernel over a geometry: forward, or stride-1 backward-input
+// (a forward convolution of dY with the flipped, channel-exchanged kernel).
+int run(int prec, const ConvGeom &g, bool bwd_input, const float *x, const float *w, float *y,
+        cudaStream_t s) {
+  if (bwd_input && (g.sc != 1 || g.sr != 1 || g.sd != 1)) return kErrUnsupported;
+  if (g.sc > 8 || g.sr > 8 || g.sd > 8) return kErrUnsupported;
+  const View v = make_view(g, bwd_input);
+  TapMap tm;
+  const int KO[3] = {v.KW, v.KU, v.KV};
+  for (int a = 0; a < 3; ++a) {
+    tm.K[a] = KO[a];
+    tm.KO[a] = KO[a];
+    tm.base[a] = bwd_input ? KO[a] - 1 : 0;
+    tm.mul[a] = bwd_input ? -1 : 1;
+  }
+  return run_view(prec, v, tm, bwd_input, (int)g.Ci, (int)g.Co, x, w, y, s);
+}
+
+// Strided backward-input by residue classes.  With forward x index
+// s*o - p + t*d, output element i = s*a + r of dX receives dY[o] W[t] for
+// the taps with (r + p - t*d) divisible by s, at o = a + (r + p - t*d)/s.
+// Those taps, largest first, form a stride-1 correlation of dY with
+// dilation d/g (g = gcd(s, d)) and pad -min((r + p - t*d)/s); its output
+// is the sub-grid i = s*a + r of dX.  The classes together do exactly the
+// multiply-adds of the backward pass (no zero-stuffed dY).  Classes that no
+// tap reaches are zero; dX is cleared first when there are any.
+int run_bwd_input_strided(int prec, const ConvGeom &g, float *dx, const float *w,
+                          const float *dy, cudaStream_t s) {
+  const View full = make_view(g, true);  // dY -> dX extents and strides
+  const bool flat = (g.ID == 1 && g.OD == 1 && g.KD == 1);
+  // per view axis (w, u, v): stride, dilation, forward pad, kernel size
+  int S[3], D[3], P[3], KO[3];
+  if (flat) {
+    S[0] = 1; D[0] = 1; P[0] = 0; KO[0] = 1;
+    S[1] = g.sc; D[1] = g.dc; P[1] = g.pc; KO[1] = (int)g.KC;
+    S[2] = g.sr; D[2] = g.dr; P[2] = g.pr; KO[2] = (int)g.KR;
+  } else {
+    S[0] = g.sc; D[0] = g.dc; P[0] = g.pc; KO[0] = (int)g.KC;
+    S[1] = g.sr; D[1] = g.dr; P[1] = g.pr; KO[1] = (int)g.KR;
+    S[2] = g.sd; D[2] = g.dd; P[2] = g.pd; KO[2] = (int)g.KD;
+  }
+  const int I[3] = {full.OW, full.OU, full.OV};  // dX extents
+  const long long YS[3] = {full.ysw, full.ysu, full.ysv};
+  struct Axis {
+    int K, base, mul, dil, pad, out;
+  };
+  // classes of one axis
+  auto axis_class = [&](int a, int r, Axis &ax) {
+    int tmax = -1, n = 0;
+    for (int t = 0; t < KO[a]; ++t)
+      if ((((r + P[a] - t * D[a]) % S[a]) + S[a]) % S[a] == 0) {
+        tmax = t > tmax ? t : tmax;
+        ++n;
+      }
+    int gg = S[a], dd = D[a];
+    while (dd) { const int t = gg % dd; gg = dd; dd = t; }  // gcd(s, d)
+    ax.K = n;
+    ax.base = tmax;
+    ax.mul = -(S[a] / gg);
+    ax.dil = D[a] / gg;
+    ax.pad = n ? -((r + P[a] - tmax * D[a]) / S[a]) : 0;
+    ax.out = I[a] > r ? (I[a] - r + S[a] - 1) / S[a] : 0;
+    return n > 0;
+  };
+  bool any_empty = false;
+  for (int a = 0; a < 3; ++a)
+    for (int r = 0; r < S[a]; ++r) {
+      Axis ax;
+      if (!axis_class(a, r, ax) && ax.out > 0) any_empty = true;
+    }
+  if (any_empty)
+    OWL_CUDA(cudaMemsetAsync(dx, 0, sizeof(float) * (size_t)g.x_elems(), s));
+  for (int r0 = 0; r0 < S[0]; ++r0)
+    for (int r1 = 0; r1 < S[1]; ++r1)
+      for (int r2 = 0; r2 < S[2]; ++r2) {
+        Axis ax[3];
+        const int rr[3] = {r0, r1, r2};
+        bool ok = true;
+        for (int a = 0; a < 3; ++a) ok = axis_class(a, rr[a], ax[a]) && ok;
+        if (!ok || ax[0].out * ax[1].out * ax[2].out == 0) continue;
+        View v = full;
+        v.OW = ax[0].out; v.OU = ax[1].out; v.OV = ax[2].out;
+        v.KW = ax[0].K; v.KU = ax[1].K; v.KV = ax[2].K;
+        v.dw = ax[0].dil; v.du = ax[1].dil; v.dv = ax[2].dil;
+        v.pw = ax[0].pad; v.pu = ax[1].pad; v.pv = ax[2].pad;
+        v.sw = v.su = v.sv = 1;
+        v.ysw = YS[0] * S[0]; v.ysu = YS[1] * S[1]; v.ysv = YS[2] * S[2];
+        float *y = dx + (r0 * YS[0] + r1 * YS[1] + r2 * YS[2]) * (long long)g.Ci;
+        TapMap tm;
+        for (int a = 0; a < 3; ++a) {
+          tm.K[a] = ax[a].K;
+          tm.base[a] = ax[a].base;
+          tm.mul[a] = ax[a].mul;
+          tm.KO[a] = KO[a];
+        }
+        const int rc = run_view(prec, v, tm, true, (int)g.Ci, (int)g.Co, dy, w, y, s);
+        if (rc) return rc;
+      }
+  return kOk;
+}
+
 }  // namespace
 
 int tc_conv_fwd(int prec, const ConvGeom &g, const float *x, const float *w, float *y,
@@ -774,38 +915,8 @@ int tc_conv_fwd(int prec, const ConvGeom &g, const float *x, const float *w, flo
 int tc_conv_bwd_input(int prec, const ConvGeom &g, float *dx, const float *w, const float *dy,
                       cudaStream_t s) {
   if (g.sc == 1 && g.sr == 1 && g.sd == 1) return run(prec, g, true, dy, w, dx, s);
-  // Strided: dX = stride-1 backward-input of dY dilated by the stride
-  // (dY[o] placed at o*s, zeros between); the padding rule is unchanged
-  // because (s*(O-1) + k_eff - I)/2 = (1*(O'-1) + k_eff - I)/2 with O' = s*(O-1)+1.
-  ConvGeom d = g;
-  d.OC = g.OC > 0 ? (g.OC - 1) * g.sc + 1 : 0;
-  d.OR = g.OR > 0 ? (g.OR - 1) * g.sr + 1 : 0;
-  d.OD = g.OD > 0 ? (g.OD - 1) * g.sd + 1 : 0;
-  d.sc = d.sr = d.sd = 1;
-  const long long n = d.B * d.OC * d.OR * d.OD * d.Co;
-  float *dyd = nullptr;
-  int rc = scratch_alloc((void **)&dyd, sizeof(float) * (size_t)std::max<long long>(n, 1), s);
-  if (rc) return rc;
-  cudaError_t e = cudaMemsetAsync(dyd, 0, sizeof(float) * (size_t)n, s);
-  if (e != cudaSuccess) {
-    scratch_free(dyd, s);
-    return cuda_fail(e, "cudaMemsetAsync(dilated dY)");
-  }
-  const long long m = g.y_elems();
-  if (m > 0) {
-    const int blocks = (int)std::min<long long>((m + 255) / 256, 152 * 16);
-    dilate_dy<<<blocks, 256, 0, s>>>(dy, dyd, g.B, g.OC, g.OR, g.OD, g.Co, g.sc, g.sr, g.sd, d.OC,
-                                     d.OR, d.OD);
-    e = cudaGetLastError();
-    note_launch();
-    if (e != cudaSuccess) {
-      scratch_free(dyd, s);
-      return cuda_fail(e, "dilate_dy");
-    }
-  }
-  rc = run(prec, d, true, dyd, w, dx, s);
-  scratch_free(dyd, s);
-  return rc;
+  if (g.sc > 8 || g.sr > 8 || g.sd > 8) return kErrUnsupported;
+  return run_bwd_input_strided(prec, g, dx, w, dy, s);
 }
 
 int tc_read_status(int *out, cudaStream_t s) {

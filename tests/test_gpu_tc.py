@@ -32,6 +32,10 @@ CASES2D = [
     ((3, 14, 14, 33), (1, 1, 33, 129), None, SAME),
     ((2, 16, 24, 128), (3, 3, 128, 128), None, SAME),
     ((1, 23, 21, 200), (3, 3, 200, 72), (1, 3), SAME),
+    # short outputs (128-pixel tiles) with several 128-channel output tiles:
+    # two co tiles per CTA tile, the last group holding one
+    ((2, 13, 11, 64), (3, 3, 64, 384), None, SAME),
+    ((1, 7, 7, 256), (3, 3, 256, 512), None, SAME),
 ]
 CASES3D = [
     ((2, 6, 7, 9, 8), (3, 3, 3, 8, 16), None, SAME),
@@ -158,6 +162,9 @@ STRIDED = [
     ((2, 17, 13, 24), (3, 2, 24, 40), (2, 3), (1, 2), SAME),
     ((1, 20, 22, 32), (5, 5, 32, 48), (3, 2), (2, 1), SAME),
     ((2, 16, 16, 64), (1, 1, 64, 128), (2, 2), (1, 1), SAME),
+    # stride and dilation sharing a factor (residue classes with dilation d/g)
+    ((1, 14, 12, 16), (3, 3, 16, 32), (2, 2), (2, 2), SAME),
+    ((2, 13, 13, 32), (3, 3, 32, 64), (2, 2), (1, 1), VALID),
 ]
 
 
@@ -165,8 +172,9 @@ STRIDED = [
 @pytest.mark.parametrize("case", STRIDED)
 def test_strided_conv2d_tc(gpu_lib, f64_nn, prec, case):
     """Strided geometries: forward stages the halo in stride residue classes,
-    backward_input runs on dY dilated by the stride, backward_kernel stages X
-    in residue classes -- all on tcgen05."""
+    backward_input runs as one stride-1 correlation per residue class of dX
+    (the 1x1 case has classes no tap reaches, which stay zero),
+    backward_kernel stages X in residue classes -- all on tcgen05."""
     xs, ks, st, rate, pad = case
     rng = np.random.default_rng(25)
     x = rng.uniform(-1, 1, xs).astype(np.float32)
