@@ -121,6 +121,11 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
   // 8 consecutive output columns are 8 consecutive stored pixels.
   const int HW = maxw - minw + 1, HU = (p.TU - 1) * p.su + (maxu - minu) + 1;
   const int HVR = 8 + (maxv - minv) / p.sv, HV = p.sv * HVR;
+  // X halo rows; when both operand tiles have at most one row per producer
+  // warp, each warp stages its X row and dY row together in a single pass
+  const int xrows = HW * HU * p.sv;
+  const bool paired = xrows <= kProducerWarps && p.TU <= kProducerWarps &&
+                      HVR * XPL <= 32 * 5 && 8 * YPL <= 32 * 4;
 
   uint8_t *xs = smem;
   uint8_t *ys = smem + (size_t)p.NS * PARTS * p.x_bytes;
@@ -179,44 +184,50 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
       }
       uint8_t *xd = xs + (size_t)st * PARTS * p.x_bytes;
       uint8_t *yd = ys + (size_t)st * PARTS * p.y_bytes;
-      // X halo: rows (w, u, residue class) of HVR pixels x 128 channels of ci block mb
-      {
-        const int cb0 = mb * 128;
-        stage::stage_rows<KIND, EPC, 6>(
-            xd, p.x_bytes, (uint32_t)p.PS * 16, HW * HU * p.sv, HVR, XPL, p.Ci - cb0,
-            p.vec_x != 0, pidx, kProducerWarps, lane, [&](int r) {
-              const int hr = r % p.sv, t3 = r / p.sv;
-              const int hu = t3 % HU, hw = t3 / HU;
-              const int iw = ow * p.sw - p.pw + minw + hw, iu = u0 * p.su - p.pu + minu + hu;
-              const int ivs = v0 * p.sv - p.pv + minv + hr;
-              stage::Row row;
-              row.ok = iw >= 0 && iw < p.IW && iu >= 0 && iu < p.IU;
-              row.rowp = p.x + ((long long)b * p.xsb + (long long)iw * p.xsw +
-                                (long long)iu * p.xsu + (long long)ivs * p.xsv) * p.Ci + cb0;
-              row.pstep = (long long)p.sv * p.xsv * p.Ci;
-              row.vfirst = ivs;
-              row.vstride = p.sv;
-              row.vlim = p.IV;
-              return row;
-            });
-      }
-      // dY tile: TU rows (u) of 8 output pixels x BN channels of co block nb
-      {
-        const int cb0 = nb * p.BN;
-        stage::stage_rows<KIND, EPC, 4>(
-            yd, p.y_bytes, (uint32_t)p.YPS * 16, p.TU, 8, YPL, p.Co - cb0, p.vec_y != 0, pidx,
-            kProducerWarps, lane, [&](int r) {
-              const int ou = u0 + r;
-              stage::Row row;
-              row.ok = ou < p.OU;
-              row.rowp = p.dy + ((long long)b * p.ysb + (long long)ow * p.ysw +
-                                 (long long)ou * p.ysu + (long long)v0 * p.ysv) * p.Co + cb0;
-              row.pstep = p.ysv * p.Co;
-              row.vfirst = v0;
-              row.vstride = 1;
-              row.vlim = p.OV;
-              return row;
-            });
+      // X halo: rows (w, u, residue class) of HVR pixels x 128 channels of
+      // ci block mb; dY tile: TU rows (u) of 8 output pixels x BN channels
+      // of co block nb.
+      const int xcb = mb * 128, ycb = nb * p.BN;
+      auto xrow = [&](int r) {
+        const int hr = r % p.sv, t3 = r / p.sv;
+        const int hu = t3 % HU, hw = t3 / HU;
+        const int iw = ow * p.sw - p.pw + minw + hw, iu = u0 * p.su - p.pu + minu + hu;
+        const int ivs = v0 * p.sv - p.pv + minv + hr;
+        stage::Row row;
+        row.ok = iw >= 0 && iw < p.IW && iu >= 0 && iu < p.IU;
+        row.rowp = p.x + ((long long)b * p.xsb + (long long)iw * p.xsw + (long long)iu * p.xsu +
+                          (long long)ivs * p.xsv) * p.Ci + xcb;
+        row.pstep = (long long)p.sv * p.xsv * p.Ci;
+        row.vfirst = ivs;
+        row.vstride = p.sv;
+        row.vlim = p.IV;
+        return row;
+      };
+      auto yrow = [&](int r) {
+        const int ou = u0 + r;
+        stage::Row row;
+        row.ok = ou < p.OU;
+        row.rowp = p.dy + ((long long)b * p.ysb + (long long)ow * p.ysw + (long long)ou * p.ysu +
+                           (long long)v0 * p.ysv) * p.Co + ycb;
+        row.pstep = p.ysv * p.Co;
+        row.vfirst = v0;
+        row.vstride = 1;
+        row.vlim = p.OV;
+        return row;
+      };
+      if (paired) {
+        // at most one row of each per warp: both rows in one pass
+        stage::RowSet sx{xd, p.x_bytes, (uint32_t)p.PS * 16, xrows, HVR, XPL, p.Ci - xcb};
+        stage::RowSet sy{yd, p.y_bytes, (uint32_t)p.YPS * 16, p.TU, 8, YPL, p.Co - ycb};
+        stage::stage_rows2<KIND, EPC, 5, 4>(sx, xrow, sy, yrow, p.vec_x != 0 && p.vec_y != 0,
+                                            pidx, kProducerWarps, lane);
+      } else {
+        stage::stage_rows<KIND, EPC, 6>(xd, p.x_bytes, (uint32_t)p.PS * 16, xrows, HVR, XPL,
+                                        p.Ci - xcb, p.vec_x != 0, pidx, kProducerWarps, lane,
+                                        xrow);
+        stage::stage_rows<KIND, EPC, 4>(yd, p.y_bytes, (uint32_t)p.YPS * 16, p.TU, 8, YPL,
+                                        p.Co - ycb, p.vec_y != 0, pidx, kProducerWarps, lane,
+                                        yrow);
       }
       fence_proxy_async();
       mbar_arrive(smem_u32(&full[st]));
@@ -408,45 +419,70 @@ int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, c
   // Plan: BN (co block), TG (taps per CTA, TG*BN <= 512 TMEM columns), NS = 2.
   // Prefer wide co blocks and many taps per CTA; shrink until the two stages
   // of X halo + dY tile fit in shared memory.
-  bool planned = false;
-  for (int tu : {16, 8, 4, 2}) {
-  if (planned) break;
-  p.TU = tu;
-  p.TP = tu * 8;
-  p.YPS = p.TP + 1;
-  for (int bn : {256, 128, 64, 32, 16}) {
-    p.BN = std::min(bn, (p.Co + 15) / 16 * 16);
-    // fewest tap groups whose accumulators fit TMEM (TG * BN <= 512 columns),
-    // taps spread evenly over them (the last group may be smaller)
-    const int tg_max = std::min(p.T, std::min(16, 512 / p.BN));
-    for (int n_tg = (p.T + tg_max - 1) / tg_max; n_tg <= p.T && !planned; ++n_tg) {
-      const int tg = (p.T + n_tg - 1) / n_tg;
-      if ((p.T + tg - 1) / tg != n_tg) continue;
-      p.TG = tg;
-      p.n_tg = n_tg;
-      int maxHP = 0;
-      for (int gi = 0; gi < p.n_tg; ++gi) {
-        int mnw = 1 << 30, mnu = 1 << 30, mnv = 1 << 30, mxw = -1, mxu = -1, mxv = -1;
-        for (int i = 0; i < tg && gi * tg + i < p.T; ++i) {
-          const int t = gi * tg + i;
-          const int kv = t % p.KV, ku = (t / p.KV) % p.KU, kw = t / (p.KV * p.KU);
-          mnw = std::min(mnw, kw * p.dw); mxw = std::max(mxw, kw * p.dw);
-          mnu = std::min(mnu, ku * p.du); mxu = std::max(mxu, ku * p.du);
-          mnv = std::min(mnv, kv * p.dv); mxv = std::max(mxv, kv * p.dv);
-        }
-        maxHP = std::max(maxHP, (mxw - mnw + 1) * ((tu - 1) * p.su + mxu - mnu + 1) *
-                                    (p.sv * (8 + (mxv - mnv) / p.sv)));
-      }
-      p.PS = maxHP + (((1 - maxHP) % 8) + 8) % 8;
-      if (p.PS >= 16384) continue;
-      p.x_bytes = (unsigned)(128 * EB / 16) * (unsigned)p.PS * 16u;
-      p.y_bytes = (unsigned)(p.BN * EB / 16) * (unsigned)p.YPS * 16u;
-      p.NS = 2;
-      const size_t need = (size_t)p.NS * parts * (p.x_bytes + p.y_bytes) + 256;
-      if (need <= (size_t)kSmemMax) planned = true;
+  // Tile height TU (even, so that TU*8 pixels fill whole 16-pixel K steps),
+  // tried in order of estimated cost: rows staged including padding plus a
+  // fixed per-tile cost of about four rows; a tile taller than the number of
+  // producer warps needs a second staging pass and ranks last.
+  int tus[8], ntu = 0;
+  {
+    int cand[8] = {14, 12, 10, 16, 8, 6, 4, 2}, waste[8];
+    for (int i = 0; i < 8; ++i) {
+      waste[i] = (p.OU + cand[i] - 1) / cand[i] * (cand[i] + 4);
+      if (cand[i] > kProducerWarps) waste[i] += 1 << 20;
     }
-    if (planned) break;
+    bool used[8] = {false};
+    for (int k = 0; k < 8; ++k) {
+      int best = -1;
+      for (int i = 0; i < 8; ++i)
+        if (!used[i] && (best < 0 || waste[i] < waste[best] ||
+                         (waste[i] == waste[best] && cand[i] > cand[best])))
+          best = i;
+      used[best] = true;
+      tus[ntu++] = cand[best];
+    }
   }
+  // Widest output-channel block first (it is the MMA's N: narrow blocks waste
+  // the tensor core), then the cheapest tile height, then the fewest tap
+  // groups that fit shared memory.
+  bool planned = false;
+  for (int bn : {256, 128, 64, 32, 16}) {
+    if (planned) break;
+    p.BN = std::min(bn, (p.Co + 15) / 16 * 16);
+    const int tg_max = std::min(p.T, std::min(16, 512 / p.BN));
+    for (int ti = 0; ti < ntu && !planned; ++ti) {
+      const int tu = tus[ti];
+      p.TU = tu;
+      p.TP = tu * 8;
+      p.YPS = p.TP + 1;
+      // fewest tap groups whose accumulators fit TMEM (TG * BN <= 512
+      // columns), taps spread evenly over them (the last may be smaller)
+      for (int n_tg = (p.T + tg_max - 1) / tg_max; n_tg <= p.T && !planned; ++n_tg) {
+        const int tg = (p.T + n_tg - 1) / n_tg;
+        if ((p.T + tg - 1) / tg != n_tg) continue;
+        p.TG = tg;
+        p.n_tg = n_tg;
+        int maxHP = 0;
+        for (int gi = 0; gi < p.n_tg; ++gi) {
+          int mnw = 1 << 30, mnu = 1 << 30, mnv = 1 << 30, mxw = -1, mxu = -1, mxv = -1;
+          for (int i = 0; i < tg && gi * tg + i < p.T; ++i) {
+            const int t = gi * tg + i;
+            const int kv = t % p.KV, ku = (t / p.KV) % p.KU, kw = t / (p.KV * p.KU);
+            mnw = std::min(mnw, kw * p.dw); mxw = std::max(mxw, kw * p.dw);
+            mnu = std::min(mnu, ku * p.du); mxu = std::max(mxu, ku * p.du);
+            mnv = std::min(mnv, kv * p.dv); mxv = std::max(mxv, kv * p.dv);
+          }
+          maxHP = std::max(maxHP, (mxw - mnw + 1) * ((tu - 1) * p.su + mxu - mnu + 1) *
+                                      (p.sv * (8 + (mxv - mnv) / p.sv)));
+        }
+        p.PS = maxHP + (((1 - maxHP) % 8) + 8) % 8;
+        if (p.PS >= 16384) continue;
+        p.x_bytes = (unsigned)(128 * EB / 16) * (unsigned)p.PS * 16u;
+        p.y_bytes = (unsigned)(p.BN * EB / 16) * (unsigned)p.YPS * 16u;
+        p.NS = 2;
+        const size_t need = (size_t)p.NS * parts * (p.x_bytes + p.y_bytes) + 256;
+        if (need <= (size_t)kSmemMax) planned = true;
+      }
+    }
   }
   if (!planned) return kErrUnsupported;
   p.u_tiles = (p.OU + p.TU - 1) / p.TU;

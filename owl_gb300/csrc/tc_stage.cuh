@@ -107,3 +107,104 @@ __device__ __forceinline__ void stage_rows(uint8_t *dst, uint32_t lo_off, uint32
 
 }  // namespace stage
 }  // namespace owlgpu
+
+namespace owlgpu {
+namespace stage {
+
+// One operand tile for stage_rows2: nrows rows of npix pixels x nch chunks,
+// chunk j of row r pixel i at dst + j*plane_bytes + (r*npix + i)*16.
+struct RowSet {
+  uint8_t *dst;
+  uint32_t lo_off, plane_bytes;
+  int nrows, npix, nch, clim;
+};
+
+// Stage two row sets in the same passes: warp w takes row w (+ k*nwarps)
+// of each set and issues the loads of both rows before converting either,
+// so a tile whose two sets have at most nwarps rows each costs every warp a
+// single round trip to memory.
+template <int KIND, int EPC, int BA, int BB, class FnA, class FnB>
+__device__ __forceinline__ void stage_rows2(const RowSet &A, FnA rowa, const RowSet &Bs,
+                                            FnB rowb, bool vec, int warp, int nwarps,
+                                            int lane) {
+  const int SA = A.npix * A.nch, SB = Bs.npix * Bs.nch;
+  const int nshA = (A.nch & (A.nch - 1)) == 0 ? __ffs(A.nch) - 1 : -1;
+  const int nshB = (Bs.nch & (Bs.nch - 1)) == 0 ? __ffs(Bs.nch) - 1 : -1;
+  const int nr = max(A.nrows, Bs.nrows);
+  for (int r = warp; r < nr; r += nwarps) {
+    const bool hasA = r < A.nrows, hasB = r < Bs.nrows;
+    Row ra, rb;
+    ra.ok = rb.ok = false;
+    if (hasA) ra = rowa(r);
+    if (hasB) rb = rowb(r);
+    const int passes = max(hasA ? (SA + 32 * BA - 1) / (32 * BA) : 0,
+                           hasB ? (SB + 32 * BB - 1) / (32 * BB) : 0);
+    for (int ps = 0; ps < passes; ++ps) {
+      float va[BA][EPC], vb[BB][EPC];
+      int oa[BA], ob[BB];
+#pragma unroll
+      for (int q = 0; q < BA; ++q) {
+        const int sl = ps * 32 * BA + lane + 32 * q;
+#pragma unroll
+        for (int e = 0; e < EPC; ++e) va[q][e] = 0.f;
+        oa[q] = -1;
+        if (hasA && sl < SA) {
+          const int i = nshA >= 0 ? (sl >> nshA) : sl / A.nch;
+          const int j = sl - i * A.nch;
+          oa[q] = (int)(j * A.plane_bytes) + (r * A.npix + i) * 16;
+          const int vv = ra.vfirst + i * ra.vstride, c = j * EPC;
+          if (ra.ok && vv >= 0 && vv < ra.vlim && c < A.clim) {
+            const float *src = ra.rowp + (long long)i * ra.pstep + c;
+            if (vec && c + EPC <= A.clim) {
+#pragma unroll
+              for (int e = 0; e < EPC; e += 4) {
+                float4 f = __ldg(reinterpret_cast<const float4 *>(src + e));
+                va[q][e] = f.x; va[q][e + 1] = f.y; va[q][e + 2] = f.z; va[q][e + 3] = f.w;
+              }
+            } else {
+#pragma unroll
+              for (int e = 0; e < EPC; ++e)
+                if (c + e < A.clim) va[q][e] = __ldg(src + e);
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < BB; ++q) {
+        const int sl = ps * 32 * BB + lane + 32 * q;
+#pragma unroll
+        for (int e = 0; e < EPC; ++e) vb[q][e] = 0.f;
+        ob[q] = -1;
+        if (hasB && sl < SB) {
+          const int i = nshB >= 0 ? (sl >> nshB) : sl / Bs.nch;
+          const int j = sl - i * Bs.nch;
+          ob[q] = (int)(j * Bs.plane_bytes) + (r * Bs.npix + i) * 16;
+          const int vv = rb.vfirst + i * rb.vstride, c = j * EPC;
+          if (rb.ok && vv >= 0 && vv < rb.vlim && c < Bs.clim) {
+            const float *src = rb.rowp + (long long)i * rb.pstep + c;
+            if (vec && c + EPC <= Bs.clim) {
+#pragma unroll
+              for (int e = 0; e < EPC; e += 4) {
+                float4 f = __ldg(reinterpret_cast<const float4 *>(src + e));
+                vb[q][e] = f.x; vb[q][e + 1] = f.y; vb[q][e + 2] = f.z; vb[q][e + 3] = f.w;
+              }
+            } else {
+#pragma unroll
+              for (int e = 0; e < EPC; ++e)
+                if (c + e < Bs.clim) vb[q][e] = __ldg(src + e);
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < BA; ++q)
+        if (oa[q] >= 0) put_chunk<KIND, EPC>(A.dst + oa[q], A.lo_off, va[q]);
+#pragma unroll
+      for (int q = 0; q < BB; ++q)
+        if (ob[q] >= 0) put_chunk<KIND, EPC>(Bs.dst + ob[q], Bs.lo_off, vb[q]);
+    }
+  }
+}
+
+}  // namespace stage
+}  // namespace owlgpu
