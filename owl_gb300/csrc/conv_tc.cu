@@ -430,6 +430,9 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
   } else if (warp == kLoadWarp) {
     // ===================== B (kernel) loader =====================
     if (lane == 0) {
+      // The kernel is a programmatic dependent of prep_weights: wait for that
+      // grid to finish (and its weight images to be visible) before copying.
+      asm volatile("griddepcontrol.wait;" ::: "memory");
       long long kb = 0;
       const uint32_t b0 = smem_u32(bring);
       for (long long t = blockIdx.x; t < p.total_tiles; t += gridDim.x) {
@@ -534,6 +537,9 @@ template <int KIND>
 __global__ void prep_weights(const float *__restrict__ w, uint8_t *__restrict__ hi,
                              uint8_t *__restrict__ lo, int T, int Ci, int Co, int K, int N,
                              int BN, int CPB, int NCB, int n_tiles, int bwd_input, TapMap tm) {
+  // the convolution launched next may start its prologue and halo staging
+  // now; its weight loader waits for this grid (griddepcontrol.wait)
+  asm volatile("griddepcontrol.launch_dependents;");
   constexpr int EPC = (KIND == K_TF32) ? 4 : 8;
   const int NCH = CPB / EPC;
   const long long total = (long long)n_tiles * NCB * T * NCH * BN;
@@ -735,8 +741,20 @@ int launch(const TcParams &p, size_t smem, cudaStream_t s) {
     attr_set[dev] = true;
   }
   int grid = (int)std::min<long long>(p.total_tiles, num_sms());
-  conv_tc_kernel<KIND><<<grid, kThreads, smem, s>>>(p);
-  OWL_CHECK_LAUNCH("conv_tc_kernel");
+  // programmatic dependent launch on prep_weights (launched just before)
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaError_t e = cudaLaunchKernelEx(&cfg, conv_tc_kernel<KIND>, p);
+  note_launch();
+  if (e != cudaSuccess) return cuda_fail(e, "conv_tc_kernel");
   return kOk;
 }
 

@@ -323,10 +323,35 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
   }
 }
 
-// out[i] = sum_r part[r][i] in increasing r (deterministic).
+// out[i] = sum_r part[r][i] in increasing r (deterministic).  Each thread
+// sums four consecutive elements and issues the loads of 16 partials before
+// adding them, in order, so the sum is the same as one add at a time while
+// 16 loads are in flight.
 __global__ void wgrad_reduce(const float *__restrict__ part, float *__restrict__ out, long long n,
-                             int R) {
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+                             int R, int vec) {
+  // vec: n % 4 == 0 and `out` 16-byte aligned (the partials always are)
+  const long long n4 = vec ? n / 4 : 0;
+  const float4 *p4 = reinterpret_cast<const float4 *>(part);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n4;
+       i += (long long)gridDim.x * blockDim.x) {
+    float4 s = __ldg(p4 + i);
+    int r = 1;
+    for (; r + 16 <= R; r += 16) {
+      float4 v[16];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) v[q] = __ldg(p4 + (long long)(r + q) * n4 + i);
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        s.x += v[q].x; s.y += v[q].y; s.z += v[q].z; s.w += v[q].w;
+      }
+    }
+    for (; r < R; ++r) {
+      const float4 v = __ldg(p4 + (long long)r * n4 + i);
+      s.x += v.x; s.y += v.y; s.z += v.z; s.w += v.w;
+    }
+    reinterpret_cast<float4 *>(out)[i] = s;
+  }
+  for (long long i = n4 * 4 + (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     float s = part[i];
     for (int r = 1; r < R; ++r) s += part[(long long)r * n + i];
@@ -525,8 +550,11 @@ int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, c
   if (kind == K_BF16X3) rc = launch<K_BF16X3>(p, smem, grid, s);
   else rc = launch<K_BF16>(p, smem, grid, s);
   if (rc == kOk && p.R > 1) {
-    const int blocks = (int)std::min<long long>((welems + 255) / 256, 4 * 152);
-    wgrad_reduce<<<blocks, 256, 0, s>>>(part, dw, welems, p.R);
+    // float4 path needs 16-byte aligned rows: welems % 4 == 0 and dw aligned
+    const bool v4 = welems % 4 == 0 && (uintptr_t)dw % 16 == 0;
+    const long long work = v4 ? welems / 4 : welems;
+    const int blocks = (int)std::max<long long>(1, std::min<long long>((work + 127) / 128, 8 * 152));
+    wgrad_reduce<<<blocks, 128, 0, s>>>(part, dw, welems, p.R, v4 ? 1 : 0);
     cudaError_t e = cudaGetLastError();
     note_launch();
     if (e != cudaSuccess) rc = cuda_fail(e, "wgrad_reduce");
