@@ -493,17 +493,26 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
         const uint32_t tcol = tmem_base + ((uint32_t)(q * 32) << 16) +
                               (uint32_t)((abuf * p.NCT + ct) * p.MH * 128);
         float *ybase = p.y + ((long long)tl.b * p.ysb + (long long)tl.ow * p.ysw) * p.Cout + co;
-        for (int c0 = 0; c0 < p.MH * 128; c0 += 16) {
-          uint32_t r[16];
-          tmem_ld16(tcol + (uint32_t)c0, r);
+        // 64 columns (8 u-rows of 8 pixels) per TMEM round trip: four loads
+        // in flight, one wait
+        for (int c0 = 0; c0 < p.MH * 128; c0 += 64) {
+          uint32_t r[4][16];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) tmem_ld16(tcol + (uint32_t)(c0 + 16 * k), r[k]);
           tmem_ld_wait();
 #pragma unroll
-          for (int e = 0; e < 16; ++e) {
-            const int c = c0 + e;
-            const int u = tl.u0 + (c >> 3), v = tl.v0 + (c & 7);
-            if (co_ok && u < p.OU && v < p.OV)
-              ybase[((long long)u * p.ysu + (long long)v * p.ysv) * p.Cout] =
-                  __uint_as_float(r[e]);
+          for (int k = 0; k < 4; ++k) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              const int u = tl.u0 + ((c0 + 16 * k + 8 * h) >> 3);
+              if (!co_ok || u >= p.OU) continue;
+              float *row = ybase + (long long)u * p.ysu * p.Cout;
+#pragma unroll
+              for (int e = 0; e < 8; ++e) {
+                const int v = tl.v0 + e;
+                if (v < p.OV) row[(long long)v * p.ysv * p.Cout] = __uint_as_float(r[k][8 * h + e]);
+              }
+            }
           }
         }
       }
