@@ -462,6 +462,140 @@ def bench_pool(reps: int = 20):
     return out
 
 
+def graph_ms(fn, reps: int = 5) -> float:
+    """Device time of one call: `reps` calls captured in a CUDA graph,
+    replayed, timed with CUDA events on the current stream."""
+    import torch
+
+    fn()
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        for _ in range(reps):
+            fn()
+    g.replay()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    g.replay()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def bench_conv3d(precision: str):
+    """Config 3, convolutions: conv3d X [4;32;32;32;32] * W [3;3;3;32;64]
+    stride 1 SAME, forward + backward_input + backward_kernel (43.49 GFLOP),
+    and transpose_conv3d W [2;2;2;64;32] stride 2 SAME on the conv3d output
+    [4;32;32;32;64] -> [4;64;64;64;32] with its two backward passes
+    (12.88 GFLOP); float32 at `precision` and plain FP32, float64 on the D
+    path.  Inputs uniform[-1,1], seeded.  Error: max|y - y64| / max|y64|
+    against the float64 oracle on batch 1."""
+    import torch
+
+    import oracle
+    from owl_gb300.dense import NN, GpuBackend
+
+    rng = np.random.default_rng(31)
+    x = rng.uniform(-1, 1, (4, 32, 32, 32, 32)).astype(np.float32)
+    w = rng.uniform(-1, 1, (3, 3, 3, 32, 64)).astype(np.float32) * np.float32(0.05)
+    wt = rng.uniform(-1, 1, (2, 2, 2, 64, 32)).astype(np.float32) * np.float32(0.1)
+    f_conv = 2.0 * 4 * 32 ** 3 * 64 * 27 * 32
+    f_tconv = 2.0 * 4 * 32 ** 3 * 64 * 8 * 32
+    out = {"gflop": {"conv3d_step": 3 * f_conv / 1e9, "transpose_conv3d_step": 3 * f_tconv / 1e9}}
+    O = NN(oracle.OracleBackend(threads=os.cpu_count() or 1))
+    ref = {}
+    x1, w64, wt64 = x[:1].astype(np.float64), w.astype(np.float64), wt.astype(np.float64)
+    y64 = O.conv3d(x1, w64, [1, 1, 1], "SAME")
+    dy1 = rng.standard_normal(y64.shape)
+    ref["conv3d"] = (y64, O.conv3d_backward_input(x1, w64, [1, 1, 1], dy1),
+                     O.conv3d_backward_kernel(x1, w64, [1, 1, 1], dy1))
+    t64 = O.transpose_conv3d(y64, wt64, [2, 2, 2], "SAME")
+    dt1 = rng.standard_normal(t64.shape)
+    ref["transpose_conv3d"] = (t64, O.transpose_conv3d_backward_input(y64, wt64, [2, 2, 2], dt1),
+                               O.transpose_conv3d_backward_kernel(y64, wt64, [2, 2, 2], dt1))
+    for prec, dt in ((precision, torch.float32), ("fp32", torch.float32), ("fp64", torch.float64)):
+        if prec in out:
+            continue
+        nn = NN(GpuBackend("fp32" if prec == "fp64" else prec))
+        X = torch.from_numpy(x).to("cuda", dt)
+        W = torch.from_numpy(w).to("cuda", dt)
+        WT = torch.from_numpy(wt).to("cuda", dt)
+        Y = nn.conv3d(X, W, [1, 1, 1], "SAME")
+        DY = torch.randn_like(Y)
+        T = nn.transpose_conv3d(Y, WT, [2, 2, 2], "SAME")
+        DT = torch.randn_like(T)
+
+        def step3():
+            nn.conv3d(X, W, [1, 1, 1], "SAME")
+            nn.conv3d_backward_input(X, W, [1, 1, 1], DY)
+            nn.conv3d_backward_kernel(X, W, [1, 1, 1], DY)
+
+        def stept():
+            nn.transpose_conv3d(Y, WT, [2, 2, 2], "SAME")
+            nn.transpose_conv3d_backward_input(Y, WT, [2, 2, 2], DT)
+            nn.transpose_conv3d_backward_kernel(Y, WT, [2, 2, 2], DT)
+
+        ms3, mst = graph_ms(step3, 3), graph_ms(stept, 3)
+        # accuracy on batch 1, same values as the oracle
+        X1 = torch.from_numpy(x[:1]).to("cuda", dt)
+        D1 = torch.from_numpy(dy1).to("cuda", dt)
+        Y1 = torch.from_numpy(y64).to("cuda", dt)
+        T1 = torch.from_numpy(dt1).to("cuda", dt)
+        got = {"conv3d": (nn.conv3d(X1, W, [1, 1, 1], "SAME"),
+                          nn.conv3d_backward_input(X1, W, [1, 1, 1], D1),
+                          nn.conv3d_backward_kernel(X1, W, [1, 1, 1], D1)),
+               "transpose_conv3d": (nn.transpose_conv3d(Y1, WT, [2, 2, 2], "SAME"),
+                                    nn.transpose_conv3d_backward_input(Y1, WT, [2, 2, 2], T1),
+                                    nn.transpose_conv3d_backward_kernel(Y1, WT, [2, 2, 2], T1))}
+        err = 0.0
+        for k in got:
+            for a, b in zip(got[k], ref[k]):
+                a = a.double().cpu().numpy()
+                err = max(err, float(np.abs(a - b).max() / np.abs(b).max()))
+        out[prec] = {"conv3d_ms": ms3, "conv3d_tflops": 3 * f_conv / (ms3 / 1e3) / 1e12,
+                     "transpose_conv3d_ms": mst,
+                     "transpose_conv3d_tflops": 3 * f_tconv / (mst / 1e3) / 1e12,
+                     "error_vs_f64": err}
+    out["note"] = ("fwd + backward_input + backward_kernel per step; device time of the calls "
+                   "replayed from a CUDA graph; error on batch 1 against the float64 oracle")
+    return out
+
+
+def bench_c1():
+    """Config 1: plain float32 conv2d [8;32;32;16] * [3;3;16;32] stride 1 SAME
+    followed by max_pool2d 2x2 stride 2 with argmax -- the device time of the
+    pair, and the same pair through the host drop-in (Owl's stubs' calling
+    convention, host arrays in and out)."""
+    import time
+
+    import torch
+
+    from owl_gb300.dense import NN, GpuBackend
+
+    nn = NN(GpuBackend("fp32"))
+    rng = np.random.default_rng(2024)
+    x = rng.uniform(-1, 1, (8, 32, 32, 16)).astype(np.float32)
+    w = rng.uniform(-1, 1, (3, 3, 16, 32)).astype(np.float32)
+    X, W = torch.from_numpy(x).cuda(), torch.from_numpy(w).cuda()
+
+    def dev():
+        y = nn.conv2d(X, W, [1, 1], "SAME")
+        nn.max_pool2d_argmax(y, [2, 2], [2, 2], "SAME")
+
+    ms = graph_ms(dev, 10)
+    nn.conv2d(x, w, [1, 1], "SAME")
+    t0 = time.perf_counter()
+    for _ in range(20):
+        y = nn.conv2d(x, w, [1, 1], "SAME")
+        nn.max_pool2d_argmax(y, [2, 2], [2, 2], "SAME")
+    host_ms = (time.perf_counter() - t0) / 20 * 1e3
+    return {"device_us": ms * 1e3, "host_dropin_us": host_ms * 1e3,
+            "conv_gflop": 2.0 * 8 * 32 * 32 * 32 * 9 * 16 / 1e9,
+            "note": "device: conv + pool/argmax replayed from a CUDA graph; host: two drop-in "
+                    "calls from numpy arrays (copies and synchronisation included)"}
+
+
 def bench_algodiff(precision: str, steps: int = 10):
     """Config-4 training step through the Algodiff registrations: a CNN on
     [256;28;28;1] uniform[0,1] images with random labels (conv 5x5x1x32,
@@ -794,6 +928,8 @@ def main():
         result["pool"] = bench_pool()
         result["algodiff"] = bench_algodiff(args.precision)
         result["serve"] = bench_serve(args.precision)
+        result["conv3d"] = bench_conv3d(args.precision)
+        result["c1"] = bench_c1()
 
     # ---- end to end through the host drop-in C ABI ----
     if not args.no_e2e and rank == 0:
