@@ -331,7 +331,10 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
   } else if (warp == kMmaWarp) {
     // ===================== MMA issuer =====================
     if (lane == 0) {
-      long long kh = 0, kb = 0;
+      // ring positions and phases advance by counting (no division in the
+      // issue loop: this thread's own work is on the critical path)
+      int hs = 0, bs = 0;
+      uint32_t hph = 0, bph = 0;
       int tc = 0;
       const uint32_t halo0 = smem_u32(halo), b0 = smem_u32(bring);
       const uint32_t a_lbo = (uint32_t)p.PS * 16, a_sbo = (uint32_t)(p.su * p.HV) * 16;
@@ -348,22 +351,24 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
         if (!wait_bar(smem_u32(&acc_empty[abuf]), aph ^ 1, abort_flag, p.status)) break;
         tc_fence_after();
         const uint32_t d0 = tmem_base + (uint32_t)(abuf * p.NCT * p.MH * 128);
-        const int nct = min(p.NCT, p.n_tiles - decode_tile(p, t).nt * p.NCT);
+        const int nct = min(p.NCT, p.n_tiles - (int)(t % p.n_groups) * p.NCT);
         uint32_t acc = 0;
         bool ok = true;
-        for (int cb = 0; cb < p.NCB && ok; ++cb, ++kh) {
-          const int hs = (int)(kh % p.NH);
-          if (!wait_bar(smem_u32(&halo_full[hs]), (uint32_t)((kh / p.NH) & 1), abort_flag,
-                        p.status)) { ok = false; break; }
+        for (int cb = 0; cb < p.NCB && ok; ++cb) {
+          if (!wait_bar(smem_u32(&halo_full[hs]), hph, abort_flag, p.status)) {
+            ok = false;
+            break;
+          }
           tc_fence_after();
           // Descriptors advance by plain adds: the start-address field is the
           // low 14 bits (16-byte units) and never carries out of them here.
           const uint64_t xd_stage =
               smem_desc(halo0 + (uint32_t)hs * PARTS * p.halo_bytes, a_lbo, a_sbo);
-          for (int sl = 0; sl < p.NSL; ++sl, ++kb) {
-            const int bs = (int)(kb % p.NB);
-            if (!wait_bar(smem_u32(&b_full[bs]), (uint32_t)((kb / p.NB) & 1), abort_flag,
-                          p.status)) { ok = false; break; }
+          for (int sl = 0; sl < p.NSL; ++sl) {
+            if (!wait_bar(smem_u32(&b_full[bs]), bph, abort_flag, p.status)) {
+              ok = false;
+              break;
+            }
             tc_fence_after();
             const int t0 = sl * p.TPS, t1 = min(p.T, t0 + p.TPS);
             const uint64_t wslot = wd_ring + (uint64_t)(bs * wslot16);
@@ -414,9 +419,11 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
               }
             }
             mma_commit(smem_u32(&b_empty[bs]));
+            if (++bs == p.NB) { bs = 0; bph ^= 1; }
           }
           if (!ok) break;
           mma_commit(smem_u32(&halo_empty[hs]));
+          if (++hs == p.NH) { hs = 0; hph ^= 1; }
         }
         if (!ok) break;
         mma_commit(smem_u32(&acc_full[abuf]));
@@ -492,25 +499,36 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
         const bool co_ok = co < p.Cout;
         const uint32_t tcol = tmem_base + ((uint32_t)(q * 32) << 16) +
                               (uint32_t)((abuf * p.NCT + ct) * p.MH * 128);
-        float *ybase = p.y + ((long long)tl.b * p.ysb + (long long)tl.ow * p.ysw) * p.Cout + co;
-        // 64 columns (8 u-rows of 8 pixels) per TMEM round trip: four loads
-        // in flight, one wait
+        // Few instructions per store: this warp (quadrant 0) shares a
+        // scheduler with the MMA issuer.  Element (u, v) of the tile is at
+        // ytile + (u - u0) * du + (v - v0) * dv.
+        float *ytile = p.y + ((long long)tl.b * p.ysb + (long long)tl.ow * p.ysw +
+                              (long long)tl.u0 * p.ysu + (long long)tl.v0 * p.ysv) * p.Cout + co;
+        const long long du = p.ysu * (long long)p.Cout, dv = p.ysv * (long long)p.Cout;
+        const int urows = min(p.MH * 16, p.OU - tl.u0), vcols = min(8, p.OV - tl.v0);
         for (int c0 = 0; c0 < p.MH * 128; c0 += 64) {
           uint32_t r[4][16];
 #pragma unroll
           for (int k = 0; k < 4; ++k) tmem_ld16(tcol + (uint32_t)(c0 + 16 * k), r[k]);
           tmem_ld_wait();
+          // (the next tcgen05.ld is warp-collective: no lane leaves the loop)
+          if (co_ok) {
 #pragma unroll
-          for (int k = 0; k < 4; ++k) {
+            for (int k = 0; k < 4; ++k) {
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-              const int u = tl.u0 + ((c0 + 16 * k + 8 * h) >> 3);
-              if (!co_ok || u >= p.OU) continue;
-              float *row = ybase + (long long)u * p.ysu * p.Cout;
+              for (int h = 0; h < 2; ++h) {
+                const int ur = (c0 + 16 * k + 8 * h) >> 3;  // u row within the tile
+                if (ur < urows) {
+                  float *row = ytile + ur * du;
+                  if (vcols == 8) {
 #pragma unroll
-              for (int e = 0; e < 8; ++e) {
-                const int v = tl.v0 + e;
-                if (v < p.OV) row[(long long)v * p.ysv * p.Cout] = __uint_as_float(r[k][8 * h + e]);
+                    for (int e = 0; e < 8; ++e) row[e * dv] = __uint_as_float(r[k][8 * h + e]);
+                  } else {
+#pragma unroll
+                    for (int e = 0; e < 8; ++e)
+                      if (e < vcols) row[e * dv] = __uint_as_float(r[k][8 * h + e]);
+                  }
+                }
               }
             }
           }
