@@ -272,12 +272,24 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
       const uint32_t a_lbo = (uint32_t)(p.su * HV) * 16, a_sbo = (uint32_t)p.PS * 16;
       const uint32_t b_lbo = 128, b_sbo = (uint32_t)p.YPS * 16;
       const uint32_t xlo16 = p.x_bytes >> 4, ylo16 = p.y_bytes >> 4;
-      long long k = 0;
+      // per K step: 16 pixels = two 8-pixel u-groups further into the X
+      // halo, 16 pixels further into the dY tile (16-byte units)
+      const uint32_t xk16 = (uint32_t)(KSTEP_PIX / 8) * (uint32_t)(p.su * HV);
+      const int nks = p.TP / KSTEP_PIX;
+      // up to four taps' A offsets in registers (the common tap groups)
+      const bool few = ntap <= 4;
+      uint32_t to[4], dc[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        to[i] = i < ntap ? tap_off[i] : 0u;
+        dc[i] = tmem_base + (uint32_t)(i * p.BN);
+      }
+      int st = 0;
+      uint32_t ph = 0;
       uint32_t acc = 0;
       bool ok = true;
-      for (long long t = t_begin; t < t_end; ++t, ++k) {
-        const int st = (int)(k % p.NS);
-        if (!wait_bar(smem_u32(&full[st]), (uint32_t)((k / p.NS) & 1), abort_flag, p.status)) {
+      for (long long t = t_begin; t < t_end; ++t) {
+        if (!wait_bar(smem_u32(&full[st]), ph, abort_flag, p.status)) {
           ok = false;
           break;
         }
@@ -285,28 +297,44 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
         // descriptors advance by adds of 16-byte units (start-address field)
         const uint64_t xd_st = smem_desc(x0 + (uint32_t)st * PARTS * p.x_bytes, a_lbo, a_sbo);
         const uint64_t yd_st = smem_desc(y0 + (uint32_t)st * PARTS * p.y_bytes, b_lbo, b_sbo);
-        const int nks = p.TP / KSTEP_PIX;
         for (int s = 0; s < nks; ++s) {
-          // K step s covers output pixels [s*KSTEP_PIX, +KSTEP_PIX): u-groups from g0
-          const int g0 = (s * KSTEP_PIX) >> 3;
           const uint64_t bd = yd_st + (uint64_t)(s * KSTEP_PIX);
-          const uint64_t xs_ = xd_st + (uint64_t)(g0 * p.su * HV);
-          for (int i = 0; i < ntap; ++i) {
-            const uint64_t ad = xs_ + (uint64_t)tap_off[i];
-            const uint32_t d = tmem_base + (uint32_t)(i * p.BN);
-            if (KIND == K_TF32) {
-              mma_tf32(d, ad, bd, p.idesc, acc);
-            } else {
-              mma_bf16(d, ad, bd, p.idesc, acc);
-              if (KIND == K_BF16X3) {
-                mma_bf16(d, ad, bd + (uint64_t)ylo16, p.idesc, 1);
-                mma_bf16(d, ad + (uint64_t)xlo16, bd, p.idesc, 1);
+          const uint64_t xs_ = xd_st + (uint64_t)(s * xk16);
+          if (few) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+              if (i < ntap) {
+                const uint64_t ad = xs_ + (uint64_t)to[i];
+                if (KIND == K_TF32) {
+                  mma_tf32(dc[i], ad, bd, p.idesc, acc);
+                } else {
+                  mma_bf16(dc[i], ad, bd, p.idesc, acc);
+                  if (KIND == K_BF16X3) {
+                    mma_bf16(dc[i], ad, bd + (uint64_t)ylo16, p.idesc, 1);
+                    mma_bf16(dc[i], ad + (uint64_t)xlo16, bd, p.idesc, 1);
+                  }
+                }
+              }
+            }
+          } else {
+            for (int i = 0; i < ntap; ++i) {
+              const uint64_t ad = xs_ + (uint64_t)tap_off[i];
+              const uint32_t d = tmem_base + (uint32_t)(i * p.BN);
+              if (KIND == K_TF32) {
+                mma_tf32(d, ad, bd, p.idesc, acc);
+              } else {
+                mma_bf16(d, ad, bd, p.idesc, acc);
+                if (KIND == K_BF16X3) {
+                  mma_bf16(d, ad, bd + (uint64_t)ylo16, p.idesc, 1);
+                  mma_bf16(d, ad + (uint64_t)xlo16, bd, p.idesc, 1);
+                }
               }
             }
           }
           acc = 1;
         }
         mma_commit(smem_u32(&empty[st]));
+        if (++st == p.NS) { st = 0; ph ^= 1; }
       }
       if (ok) mma_commit(smem_u32(acc_full));
       mma_commit(smem_u32(drain));
