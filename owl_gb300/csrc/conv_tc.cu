@@ -501,7 +501,9 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
                               (uint32_t)((abuf * p.NCT + ct) * p.MH * 128);
         // Few instructions per store: this warp (quadrant 0) shares a
         // scheduler with the MMA issuer.  Element (u, v) of the tile is at
-        // ytile + (u - u0) * du + (v - v0) * dv.
+        // ytile + (u - u0) * du + (v - v0) * dv.  Streaming stores: the
+        // output is not read again here, so it should not displace the
+        // input halo lines the producers still read from L2.
         float *ytile = p.y + ((long long)tl.b * p.ysb + (long long)tl.ow * p.ysw +
                               (long long)tl.u0 * p.ysu + (long long)tl.v0 * p.ysv) * p.Cout + co;
         const long long du = p.ysu * (long long)p.Cout, dv = p.ysv * (long long)p.Cout;
@@ -522,11 +524,11 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
                   float *row = ytile + ur * du;
                   if (vcols == 8) {
 #pragma unroll
-                    for (int e = 0; e < 8; ++e) row[e * dv] = __uint_as_float(r[k][8 * h + e]);
+                    for (int e = 0; e < 8; ++e) __stcs(row + e * dv, __uint_as_float(r[k][8 * h + e]));
                   } else {
 #pragma unroll
                     for (int e = 0; e < 8; ++e)
-                      if (e < vcols) row[e * dv] = __uint_as_float(r[k][8 * h + e]);
+                      if (e < vcols) __stcs(row + e * dv, __uint_as_float(r[k][8 * h + e]));
                   }
                 }
               }
