@@ -1,5 +1,6 @@
 // conv_tc_wgrad.cu -- tcgen05 backward-kernel (weight gradient) for float32
-// data in BF16, TF32 or split-BF16 precision, stride 1, any dilation, 2-D/3-D.
+// data in BF16, TF32 or split-BF16 precision, strides up to 8, any dilation,
+// 2-D/3-D.
 //
 //   dW[t][ci][co] = sum over output pixels p of X[p + off(t)][ci] * dY[p][co]
 //
@@ -9,7 +10,10 @@
 // [pixel][16 B] layout as the forward kernel's halo.  Read MN-major, 8
 // consecutive pixels x 8 channels of that layout form one core matrix, so
 // every tap of a tap group reads the same X halo through a shifted descriptor
-// and all of them share one staged dY tile.
+// and all of them share one staged dY tile.  Taps are grouped by phase
+// (k*d mod s per dimension), so a strided convolution's halo holds only the
+// input rows and columns its group reads: a quarter of the footprint at
+// stride 2 in 2-D.
 //
 // Work split: a CTA owns (tap group, ci block, co block, pixel range).  It
 // accumulates the group's taps in TMEM (TG * BN columns) over all the pixel
@@ -44,6 +48,9 @@ constexpr int kProducerWarps = kWarps - 1;
 constexpr int kProducerThreads = kProducerWarps * 32;
 __device__ __forceinline__ int producer_index(int warp) { return warp - 1; }
 constexpr int kSmemMax = 232448;
+// Taps are grouped through a table in the launch parameters when the
+// convolution is strided (and, up to this many taps, always).
+constexpr int kMaxOrderedTaps = 256;
 constexpr long long kSpinLimit = 4000000000LL;
 
 enum Kind { K_BF16 = 0, K_TF32 = 1, K_BF16X3 = 2 };
@@ -65,6 +72,14 @@ struct WgParams {
   int NS;
   unsigned idesc, tmem_cols;
   int vec_x, vec_y;
+  // Tap groups.  ordered: group g holds taps tap_order[gstart[g] ..
+  // gstart[g+1]); else group g holds taps g*TG .. min(T, (g+1)*TG) - 1.
+  // Every group is phase-uniform: all its taps have the same k*d mod s in
+  // each dimension, so its X halo needs only input rows and columns of
+  // that phase (every s-th one).
+  int ordered;
+  unsigned short tap_order[kMaxOrderedTaps];
+  unsigned short gstart[kMaxOrderedTaps + 1];
 };
 
 __device__ int g_tc_status_wg;
@@ -85,7 +100,7 @@ __device__ __forceinline__ bool wait_bar(uint32_t bar, uint32_t parity, volatile
 }
 
 template <int KIND>
-__global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p) {
+__global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const __grid_constant__ WgParams p) {
   constexpr int EB = (KIND == K_TF32) ? 4 : 2;
   constexpr int EPC = 16 / EB;
   constexpr int PARTS = (KIND == K_BF16X3) ? 2 : 1;
@@ -104,26 +119,28 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
   const int r = (int)(u / p.n_mb);
   const long long t_begin = (long long)r * p.tiles_per_range;
   const long long t_end = min(p.total_tiles, t_begin + p.tiles_per_range);
-  const int tap0 = tg * p.TG;
-  const int ntap = min(p.TG, p.T - tap0);
+  const int gbeg = p.ordered ? (int)p.gstart[tg] : tg * p.TG;
+  const int ntap = p.ordered ? (int)p.gstart[tg + 1] - gbeg : min(p.TG, p.T - gbeg);
+  auto tap_of = [&](int i) { return p.ordered ? (int)p.tap_order[gbeg + i] : gbeg + i; };
 
   // bounding box of this group's tap offsets -> halo extents
   int minw = 1 << 30, minu = 1 << 30, minv = 1 << 30, maxw = -1, maxu = -1, maxv = -1;
   for (int i = 0; i < ntap; ++i) {
-    const int t = tap0 + i;
+    const int t = tap_of(i);
     const int kv = t % p.KV, ku = (t / p.KV) % p.KU, kw = t / (p.KV * p.KU);
     minw = min(minw, kw * p.dw); maxw = max(maxw, kw * p.dw);
     minu = min(minu, ku * p.du); maxu = max(maxu, ku * p.du);
     minv = min(minv, kv * p.dv); maxv = max(maxv, kv * p.dv);
   }
-  // X halo rows: w (one output w per tile), u (16 output rows at stride su);
-  // along v the halo is split into sv residue classes of HVR columns so that
-  // 8 consecutive output columns are 8 consecutive stored pixels.
-  const int HW = maxw - minw + 1, HU = (p.TU - 1) * p.su + (maxu - minu) + 1;
-  const int HVR = 8 + (maxv - minv) / p.sv, HV = p.sv * HVR;
+  // X halo of a phase-uniform group: input rows and columns of the group's
+  // phase only, so halo row (hw, hu) is input (minw + hw*sw, minu + hu*su)
+  // relative to the tile origin, and its HVR pixels are every sv-th input
+  // column: 8 consecutive output columns are 8 consecutive stored pixels.
+  const int HW = (maxw - minw) / p.sw + 1, HU = p.TU + (maxu - minu) / p.su;
+  const int HVR = 8 + (maxv - minv) / p.sv;
   // X halo rows; when both operand tiles have at most one row per producer
   // warp, each warp stages its X row and dY row together in a single pass
-  const int xrows = HW * HU * p.sv;
+  const int xrows = HW * HU;
   const bool paired = xrows <= kProducerWarps && p.TU <= kProducerWarps &&
                       HVR * XPL <= 32 * 5 && 8 * YPL <= 32 * 4;
 
@@ -139,11 +156,10 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
   uint32_t *tap_off = tmem_slot + 2;  // per-tap start pixel in the X halo (16-byte units)
 
   for (int i = threadIdx.x; i < ntap; i += blockDim.x) {
-    const int tt = tap0 + i;
+    const int tt = tap_of(i);
     const int kv = tt % p.KV, ku = (tt / p.KV) % p.KU, kw = tt / (p.KV * p.KU);
-    const int qv = kv * p.dv - minv;
-    tap_off[i] = (uint32_t)(((kw * p.dw - minw) * HU + (ku * p.du - minu)) * HV +
-                            (qv % p.sv) * HVR + qv / p.sv);
+    tap_off[i] = (uint32_t)((((kw * p.dw - minw) / p.sw) * HU + (ku * p.du - minu) / p.su) * HVR +
+                            (kv * p.dv - minv) / p.sv);
   }
 
   if (threadIdx.x == 0) {
@@ -184,15 +200,14 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
       }
       uint8_t *xd = xs + (size_t)st * PARTS * p.x_bytes;
       uint8_t *yd = ys + (size_t)st * PARTS * p.y_bytes;
-      // X halo: rows (w, u, residue class) of HVR pixels x 128 channels of
-      // ci block mb; dY tile: TU rows (u) of 8 output pixels x BN channels
-      // of co block nb.
+      // X halo: rows (w, u) of HVR pixels x 128 channels of ci block mb;
+      // dY tile: TU rows (u) of 8 output pixels x BN channels of co block nb.
       const int xcb = mb * 128, ycb = nb * p.BN;
       auto xrow = [&](int r) {
-        const int hr = r % p.sv, t3 = r / p.sv;
-        const int hu = t3 % HU, hw = t3 / HU;
-        const int iw = ow * p.sw - p.pw + minw + hw, iu = u0 * p.su - p.pu + minu + hu;
-        const int ivs = v0 * p.sv - p.pv + minv + hr;
+        const int hu = r % HU, hw = r / HU;
+        const int iw = ow * p.sw - p.pw + minw + hw * p.sw;
+        const int iu = u0 * p.su - p.pu + minu + hu * p.su;
+        const int ivs = v0 * p.sv - p.pv + minv;
         stage::Row row;
         row.ok = iw >= 0 && iw < p.IW && iu >= 0 && iu < p.IU;
         row.rowp = p.x + ((long long)b * p.xsb + (long long)iw * p.xsw + (long long)iu * p.xsu +
@@ -239,7 +254,7 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
       if (wait_bar(smem_u32(acc_full), 0, abort_flag, p.status)) {
         tc_fence_after();
         for (int i = 0; i < ntap; ++i) {
-          const int tt = tap0 + i;
+          const int tt = tap_of(i);
           float *out = p.out + (((long long)r * p.T + tt) * p.Ci + ci) * p.Co + nb * p.BN;
           const uint32_t tcol = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(i * p.BN);
           for (int c0 = 0; c0 < p.BN; c0 += 16) {
@@ -269,12 +284,12 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const WgParams p)
     // ===================== MMA issuer =====================
     if (lane == 0) {
       const uint32_t x0 = smem_u32(xs), y0 = smem_u32(ys);
-      const uint32_t a_lbo = (uint32_t)(p.su * HV) * 16, a_sbo = (uint32_t)p.PS * 16;
+      const uint32_t a_lbo = (uint32_t)HVR * 16, a_sbo = (uint32_t)p.PS * 16;
       const uint32_t b_lbo = 128, b_sbo = (uint32_t)p.YPS * 16;
       const uint32_t xlo16 = p.x_bytes >> 4, ylo16 = p.y_bytes >> 4;
-      // per K step: 16 pixels = two 8-pixel u-groups further into the X
-      // halo, 16 pixels further into the dY tile (16-byte units)
-      const uint32_t xk16 = (uint32_t)(KSTEP_PIX / 8) * (uint32_t)(p.su * HV);
+      // per K step: 16 pixels = two halo rows further into the X halo, 16
+      // pixels further into the dY tile (16-byte units)
+      const uint32_t xk16 = (uint32_t)(KSTEP_PIX / 8) * (uint32_t)HVR;
       const int nks = p.TP / KSTEP_PIX;
       // up to four taps' A offsets in registers (the common tap groups)
       const bool few = ntap <= 4;
@@ -468,10 +483,71 @@ int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, c
   p.ysb = g.OC * g.OR * g.OD;
   p.T = (int)g.taps();
   p.n_mb = (p.Ci + 127) / 128;
+  // Tap order: taps sorted by phase class (k*d mod s in each dimension), in
+  // tap order within a class, so that every group of consecutive taps of a
+  // class reads only input rows and columns of one phase.  Unstrided
+  // convolutions have a single class (the identity order).
+  const bool strided = p.sw > 1 || p.su > 1 || p.sv > 1;
+  if (strided && p.T > kMaxOrderedTaps) return kErrUnsupported;
+  p.ordered = p.T <= kMaxOrderedTaps;
+  int order[kMaxOrderedTaps], cls_begin[kMaxOrderedTaps + 1], n_cls = 0;
+  if (p.ordered) {
+    auto phase = [&](int t) {
+      const int kv = t % p.KV, ku = (t / p.KV) % p.KU, kw = t / (p.KV * p.KU);
+      return ((kw * p.dw % p.sw) * p.su + ku * p.du % p.su) * p.sv + kv * p.dv % p.sv;
+    };
+    for (int t = 0; t < p.T; ++t) order[t] = t;
+    std::stable_sort(order, order + p.T, [&](int a, int b) { return phase(a) < phase(b); });
+    for (int i = 0; i < p.T; ++i)
+      if (i == 0 || phase(order[i]) != phase(order[i - 1])) cls_begin[n_cls++] = i;
+    cls_begin[n_cls] = p.T;
+    for (int i = 0; i < p.T; ++i) p.tap_order[i] = (unsigned short)order[i];
+  }
+  // Groups of at most tg taps: each class split into the fewest groups,
+  // sizes as even as possible.  Returns the number of groups and fills
+  // gstart (ordered) or sets the contiguous split (unordered).
+  auto make_groups = [&](int tg) {
+    if (!p.ordered) {
+      const int n = (p.T + tg - 1) / tg;
+      p.TG = (p.T + n - 1) / n;
+      return (p.T + p.TG - 1) / p.TG;
+    }
+    int n = 0, widest = 0;
+    for (int c = 0; c < n_cls; ++c) {
+      const int nc = cls_begin[c + 1] - cls_begin[c];
+      const int ng = (nc + tg - 1) / tg;
+      for (int g = 0, at = cls_begin[c]; g < ng; ++g) {
+        const int sz = nc / ng + (g < nc % ng ? 1 : 0);
+        p.gstart[n++] = (unsigned short)at;
+        at += sz;
+        widest = std::max(widest, sz);
+      }
+    }
+    p.gstart[n] = (unsigned short)p.T;
+    p.TG = widest;
+    return n;
+  };
+  // Halo pixels of the largest group for tile height tu.
+  auto max_halo = [&](int tu) {
+    int maxHP = 0;
+    for (int gi = 0; gi < p.n_tg; ++gi) {
+      const int b0 = p.ordered ? p.gstart[gi] : gi * p.TG;
+      const int b1 = p.ordered ? p.gstart[gi + 1] : std::min(p.T, b0 + p.TG);
+      int mnw = 1 << 30, mnu = 1 << 30, mnv = 1 << 30, mxw = -1, mxu = -1, mxv = -1;
+      for (int i = b0; i < b1; ++i) {
+        const int t = p.ordered ? p.tap_order[i] : i;
+        const int kv = t % p.KV, ku = (t / p.KV) % p.KU, kw = t / (p.KV * p.KU);
+        mnw = std::min(mnw, kw * p.dw); mxw = std::max(mxw, kw * p.dw);
+        mnu = std::min(mnu, ku * p.du); mxu = std::max(mxu, ku * p.du);
+        mnv = std::min(mnv, kv * p.dv); mxv = std::max(mxv, kv * p.dv);
+      }
+      maxHP = std::max(maxHP, ((mxw - mnw) / p.sw + 1) * (tu + (mxu - mnu) / p.su) *
+                                  (8 + (mxv - mnv) / p.sv));
+    }
+    return maxHP;
+  };
 
   // Plan: BN (co block), TG (taps per CTA, TG*BN <= 512 TMEM columns), NS = 2.
-  // Prefer wide co blocks and many taps per CTA; shrink until the two stages
-  // of X halo + dY tile fit in shared memory.
   // Tile height TU (even, so that TU*8 pixels fill whole 16-pixel K steps),
   // tried in order of estimated cost: rows staged including padding plus a
   // fixed per-tile cost of about four rows; a tile taller than the number of
@@ -496,7 +572,7 @@ int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, c
   }
   // Widest output-channel block first (it is the MMA's N: narrow blocks waste
   // the tensor core), then the cheapest tile height, then the fewest tap
-  // groups that fit shared memory.
+  // groups whose two stages of X halo + dY tile fit shared memory.
   bool planned = false;
   for (int bn : {256, 128, 64, 32, 16}) {
     if (planned) break;
@@ -507,26 +583,12 @@ int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, c
       p.TU = tu;
       p.TP = tu * 8;
       p.YPS = p.TP + 1;
-      // fewest tap groups whose accumulators fit TMEM (TG * BN <= 512
-      // columns), taps spread evenly over them (the last may be smaller)
-      for (int n_tg = (p.T + tg_max - 1) / tg_max; n_tg <= p.T && !planned; ++n_tg) {
-        const int tg = (p.T + n_tg - 1) / n_tg;
-        if ((p.T + tg - 1) / tg != n_tg) continue;
-        p.TG = tg;
-        p.n_tg = n_tg;
-        int maxHP = 0;
-        for (int gi = 0; gi < p.n_tg; ++gi) {
-          int mnw = 1 << 30, mnu = 1 << 30, mnv = 1 << 30, mxw = -1, mxu = -1, mxv = -1;
-          for (int i = 0; i < tg && gi * tg + i < p.T; ++i) {
-            const int t = gi * tg + i;
-            const int kv = t % p.KV, ku = (t / p.KV) % p.KU, kw = t / (p.KV * p.KU);
-            mnw = std::min(mnw, kw * p.dw); mxw = std::max(mxw, kw * p.dw);
-            mnu = std::min(mnu, ku * p.du); mxu = std::max(mxu, ku * p.du);
-            mnv = std::min(mnv, kv * p.dv); mxv = std::max(mxv, kv * p.dv);
-          }
-          maxHP = std::max(maxHP, (mxw - mnw + 1) * ((tu - 1) * p.su + mxu - mnu + 1) *
-                                      (p.sv * (8 + (mxv - mnv) / p.sv)));
-        }
+      int last_n = -1;
+      for (int tg = tg_max; tg >= 1 && !planned; --tg) {
+        p.n_tg = make_groups(tg);
+        if (p.n_tg == last_n) continue;
+        last_n = p.n_tg;
+        const int maxHP = max_halo(tu);
         p.PS = maxHP + (((1 - maxHP) % 8) + 8) % 8;
         if (p.PS >= 16384) continue;
         p.x_bytes = (unsigned)(128 * EB / 16) * (unsigned)p.PS * 16u;
