@@ -32,6 +32,9 @@
 //   dX[i] = sum_t dY[i + p - t*d] W[t]^T = sum_t' dY[i - ((K-1)d - p) + t'd] W[K-1-t']^T.
 // With stride s it splits into s^d residue classes of dX, each such a
 // stride-1 correlation over the taps that reach it (run_bwd_input_strided).
+// The classes run as the segments of one persistent launch (up to eight per
+// launch), so one class's epilogue overlaps the next tile's staging and MMAs
+// and the GPU is filled by all classes' tiles together.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -67,26 +70,43 @@ constexpr long long kSpinLimit = 4000000000LL;  // cycles (~2 s) before a wait g
 
 enum Kind { K_BF16 = 0, K_TF32 = 1, K_BF16X3 = 2 };
 
+// A launch covers up to kMaxSeg segments: convolutions that share the input,
+// the channels and the tile geometry but differ in output extents, output
+// origin, pads and taps (the residue classes of a strided backward_input).
+// Their tiles are numbered one segment after another.
+constexpr int kMaxSeg = 8;
+struct Seg {
+  long long tile0;  // first tile of the segment
+  long long yoff;   // output origin: element offset into y
+  long long woff;   // byte offset of the segment's weight images (per part)
+  int OW, OU, OV, u_tiles, v_tiles;
+  int KW, KU, KV, dw, du, dv, pw, pu, pv;
+  int T, NSL, toff;  // taps, weight slots per channel block, first tap_off entry
+};
+
 struct TcParams {
   const float *x;
   float *y;
   const uint8_t *wt_hi, *wt_lo;
   int *status;
-  int B, IW, IU, IV, OW, OU, OV, KW, KU, KV, dw, du, dv, pw, pu, pv;
+  int B, IW, IU, IV;  // input extents (output extents, taps and pads per segment)
   long long xsb, xsw, xsu, xsv, ysb, ysw, ysu, ysv;  // pixel strides
   int Cin, Cout;
-  int BN, CB, NCH, CPB, NCB, T, MH;
+  int BN, CB, NCH, CPB, NCB, MH;
+  int T;  // plan: taps of the longest segment
   int sw, su, sv;          // strides along w, u, v
   int HW, HU, HV, HVR, HP, PS;  // halo rows along w, u; pixels per u-row (= sv * HVR)
-  int n_tiles, u_tiles, v_tiles;
+  int n_tiles;
   int NCT, n_groups;  // output-channel tiles per CTA tile (1 or 2), and tile groups
   long long total_tiles;
   unsigned halo_bytes, b_bytes;  // one halo stage / one weight slot (TPS taps), per part
   unsigned tile_bytes;           // one tap's weight tile (BN x CB)
-  int TPS, NSL;                  // taps per weight slot, slots per channel block
+  int TPS, NSL;                  // taps per weight slot; plan: slots of the longest segment
   int NH, NB;
   unsigned idesc, tmem_cols;
   int vec_in, vec_out;
+  int nseg;
+  Seg seg[kMaxSeg];
 };
 
 __device__ int g_tc_status;
@@ -108,19 +128,29 @@ __device__ __forceinline__ bool wait_bar(uint32_t bar, uint32_t parity, volatile
 }
 
 struct Tile {
-  int nt, b, ow, u0, v0;
+  int nt, b, ow, u0, v0, c;  // c: segment
 };
 
-__device__ __forceinline__ Tile decode_tile(const TcParams &p, long long t) {
+// Segment of tile t, advancing from segment c (tiles are visited in
+// increasing order, so the search resumes where the last one ended).
+__device__ __forceinline__ int seg_of(const TcParams &p, long long t, int c) {
+  while (c + 1 < p.nseg && t >= p.seg[c + 1].tile0) ++c;
+  return c;
+}
+
+__device__ __forceinline__ Tile decode_tile(const TcParams &p, long long t, int c) {
   Tile r;
+  const Seg &sg = p.seg[c];
+  r.c = c;
+  t -= sg.tile0;
   r.nt = (int)(t % p.n_groups);  // co-tile group: tiles nt*NCT .. nt*NCT+NCT-1
   t /= p.n_groups;
-  r.v0 = (int)(t % p.v_tiles) * 8;
-  t /= p.v_tiles;
-  r.u0 = (int)(t % p.u_tiles) * 16 * p.MH;
-  t /= p.u_tiles;
-  r.ow = (int)(t % p.OW);
-  r.b = (int)(t / p.OW);
+  r.v0 = (int)(t % sg.v_tiles) * 8;
+  t /= sg.v_tiles;
+  r.u0 = (int)(t % sg.u_tiles) * 16 * p.MH;
+  t /= sg.u_tiles;
+  r.ow = (int)(t % sg.OW);
+  r.b = (int)(t / sg.OW);
   return r;
 }
 
@@ -137,8 +167,10 @@ __device__ __forceinline__ uint32_t to_tf32(float a) {
   return r;
 }
 
-template <int KIND>
-__global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) {
+// MULTI: the launch has several segments (else segment 0 only, read at a
+// constant offset of the parameters).
+template <int KIND, bool MULTI>
+__global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_constant__ TcParams p) {
   constexpr int EPC = (KIND == K_TF32) ? 4 : 8;  // channels per 16-byte chunk
   constexpr int PARTS = (KIND == K_BF16X3) ? 2 : 1;
   extern __shared__ __align__(1024) uint8_t smem[];
@@ -158,11 +190,15 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
   uint32_t *tap_off = tmem_slot + 2;  // per-tap start pixel in the halo (16-byte units)
 
-  for (int tap = threadIdx.x; tap < p.T; tap += blockDim.x) {
-    const int kv = tap % p.KV, ku = (tap / p.KV) % p.KU, kw = tap / (p.KV * p.KU);
-    const int qv = kv * p.dv;
-    tap_off[tap] =
-        (uint32_t)((kw * p.dw * p.HU + ku * p.du) * p.HV + (qv % p.sv) * p.HVR + qv / p.sv);
+  // tap offsets of every segment, segment c's at tap_off[seg[c].toff ..]
+  for (int c = 0; c < (MULTI ? p.nseg : 1); ++c) {
+    const Seg &sg = p.seg[c];
+    for (int tap = threadIdx.x; tap < sg.T; tap += blockDim.x) {
+      const int kv = tap % sg.KV, ku = (tap / sg.KV) % sg.KU, kw = tap / (sg.KV * sg.KU);
+      const int qv = kv * sg.dv;
+      tap_off[sg.toff + tap] = (uint32_t)((kw * sg.dw * p.HU + ku * sg.du) * p.HV +
+                                          (qv % p.sv) * p.HVR + qv / p.sv);
+    }
   }
   if (threadIdx.x == 0) {
     for (int i = 0; i < p.NH; ++i) {
@@ -202,8 +238,11 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
     const int nsh = (p.NCH & (p.NCH - 1)) == 0 ? __ffs(p.NCH) - 1 : -1;
     const long long vstep = (long long)p.sv * p.xsv * p.Cin;  // floats between row pixels
     long long k = 0;  // halo stage counter
+    int sc = 0;       // segment of the current tile
     for (long long t = blockIdx.x; t < p.total_tiles; t += gridDim.x) {
-      const Tile tl = decode_tile(p, t);
+      sc = MULTI ? seg_of(p, t, sc) : 0;
+      const Tile tl = decode_tile(p, t, sc);
+      const int pw = p.seg[sc].pw, pu = p.seg[sc].pu, pv = p.seg[sc].pv;
       for (int cb = 0; cb < p.NCB; ++cb, ++k) {
         const int hs = (int)(k % p.NH);
         const uint32_t ph = (uint32_t)((k / p.NH) & 1);
@@ -220,8 +259,8 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
             // row -> (w row, u row, residue class)
             const int hr = r % p.sv, t3 = r / p.sv;
             const int hu = t3 % p.HU, hw = t3 / p.HU;
-            const int iw = tl.ow * p.sw - p.pw + hw, iu = tl.u0 * p.su - p.pu + hu;
-            const int ivs = tl.v0 * p.sv - p.pv + hr;  // global v of the row's pixel 0
+            const int iw = tl.ow * p.sw - pw + hw, iu = tl.u0 * p.su - pu + hu;
+            const int ivs = tl.v0 * p.sv - pv + hr;  // global v of the row's pixel 0
             const bool row_ok = r < nrows && iw >= 0 && iw < p.IW && iu >= 0 && iu < p.IU;
             const float *rowp =
                 p.x + ((long long)tl.b * p.xsb + (long long)iw * p.xsw + (long long)iu * p.xsu +
@@ -289,9 +328,9 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
             for (int sl = lane + 32 * kSlots; sl < S; sl += 32) {
               const int hr = r % p.sv, t3 = r / p.sv;
               const int hu = t3 % p.HU, hw = t3 / p.HU;
-              const int iw = tl.ow * p.sw - p.pw + hw, iu = tl.u0 * p.su - p.pu + hu;
+              const int iw = tl.ow * p.sw - pw + hw, iu = tl.u0 * p.su - pu + hu;
               const int hc = sl / p.NCH, j = sl - hc * p.NCH;
-              const int iv = tl.v0 * p.sv - p.pv + hr + hc * p.sv;
+              const int iv = tl.v0 * p.sv - pv + hr + hc * p.sv;
               const int c = cbase + j * EPC;
               float w8[EPC];
 #pragma unroll
@@ -345,7 +384,11 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
       const uint32_t wslot16 = (PARTS * p.b_bytes) >> 4, wstep16 = (2 * b_lbo) >> 4;
       const uint32_t tile16 = p.tile_bytes >> 4;
       const uint32_t wlo16 = p.b_bytes >> 4, xstep16 = (2 * a_lbo) >> 4, xlo16 = p.halo_bytes >> 4;
+      int sc = 0;
       for (long long t = blockIdx.x; t < p.total_tiles; t += gridDim.x, ++tc) {
+        sc = MULTI ? seg_of(p, t, sc) : 0;
+        const int nsl = p.seg[sc].NSL, ntap = p.seg[sc].T;
+        const uint32_t *toffs = tap_off + p.seg[sc].toff;
         const int abuf = tc & 1;
         const uint32_t aph = (uint32_t)((tc >> 1) & 1);
         if (!wait_bar(smem_u32(&acc_empty[abuf]), aph ^ 1, abort_flag, p.status)) break;
@@ -364,17 +407,17 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
           // low 14 bits (16-byte units) and never carries out of them here.
           const uint64_t xd_stage =
               smem_desc(halo0 + (uint32_t)hs * PARTS * p.halo_bytes, a_lbo, a_sbo);
-          for (int sl = 0; sl < p.NSL; ++sl) {
+          for (int sl = 0; sl < nsl; ++sl) {
             if (!wait_bar(smem_u32(&b_full[bs]), bph, abort_flag, p.status)) {
               ok = false;
               break;
             }
             tc_fence_after();
-            const int t0 = sl * p.TPS, t1 = min(p.T, t0 + p.TPS);
+            const int t0 = sl * p.TPS, t1 = min(ntap, t0 + p.TPS);
             const uint64_t wslot = wd_ring + (uint64_t)(bs * wslot16);
             for (int tap = t0; tap < t1; ++tap) {
               const uint64_t wd0 = wslot + (uint64_t)((tap - t0) * tile16);
-              const uint64_t xd0 = xd_stage + (uint64_t)tap_off[tap];
+              const uint64_t xd0 = xd_stage + (uint64_t)toffs[tap];
               if (nct == 1) {
 #pragma unroll 4
                 for (int s = 0; s < ksteps; ++s) {
@@ -442,15 +485,20 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
       asm volatile("griddepcontrol.wait;" ::: "memory");
       long long kb = 0;
       const uint32_t b0 = smem_u32(bring);
+      int sc = 0;
       for (long long t = blockIdx.x; t < p.total_tiles; t += gridDim.x) {
-        const Tile tl = decode_tile(p, t);
+        sc = MULTI ? seg_of(p, t, sc) : 0;
+        const Tile tl = decode_tile(p, t, sc);
+        const int nsl = p.seg[sc].NSL, ntap = p.seg[sc].T;
+        const uint8_t *whi = p.wt_hi + p.seg[sc].woff;
+        const uint8_t *wlo = PARTS == 2 ? p.wt_lo + p.seg[sc].woff : nullptr;
         for (int cb = 0; cb < p.NCB; ++cb)
-          for (int sl = 0; sl < p.NSL; ++sl, ++kb) {
+          for (int sl = 0; sl < nsl; ++sl, ++kb) {
             const int bs = (int)(kb % p.NB);
             if (!wait_bar(smem_u32(&b_empty[bs]), (uint32_t)(((kb / p.NB) & 1) ^ 1), abort_flag,
                           p.status))
               goto loader_done;
-            const int t0 = sl * p.TPS, nt_ = min(p.T - t0, p.TPS);
+            const int t0 = sl * p.TPS, nt_ = min(ntap - t0, p.TPS);
             const uint32_t bytes = (uint32_t)nt_ * p.tile_bytes;
             const int nct = min(p.NCT, p.n_tiles - tl.nt * p.NCT);
             const uint32_t bar = smem_u32(&b_full[bs]);
@@ -458,13 +506,13 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
             // slot layout: [co tile c][tap][...], co tile c at c * TPS tiles
             for (int c = 0; c < nct; ++c) {
               const size_t src =
-                  ((size_t)((tl.nt * p.NCT + c) * p.NCB + cb) * p.T + t0) * p.tile_bytes;
+                  ((size_t)((tl.nt * p.NCT + c) * p.NCB + cb) * ntap + t0) * p.tile_bytes;
               const uint32_t dst = b0 + (uint32_t)bs * PARTS * p.b_bytes +
                                    (uint32_t)(c * p.TPS) * p.tile_bytes;
               for (uint32_t o = 0; o < bytes; o += 32768u) {
                 const uint32_t n = min(32768u, bytes - o);
-                bulk_g2s(dst + o, p.wt_hi + src + o, n, bar);
-                if (PARTS == 2) bulk_g2s(dst + p.b_bytes + o, p.wt_lo + src + o, n, bar);
+                bulk_g2s(dst + o, whi + src + o, n, bar);
+                if (PARTS == 2) bulk_g2s(dst + p.b_bytes + o, wlo + src + o, n, bar);
               }
             }
           }
@@ -485,9 +533,11 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
   } else if (warp >= kEpiWarp0) {
     // ===================== epilogue =====================
     const int q = warp & 3;  // TMEM lane quadrant this warp may access
-    int tc = 0;
+    int tc = 0, sc = 0;
     for (long long t = blockIdx.x; t < p.total_tiles; t += gridDim.x, ++tc) {
-      const Tile tl = decode_tile(p, t);
+      sc = MULTI ? seg_of(p, t, sc) : 0;
+      const Tile tl = decode_tile(p, t, sc);
+      const Seg &sg = p.seg[sc];
       const int abuf = tc & 1;
       if (!wait_bar(smem_u32(&acc_full[abuf]), (uint32_t)((tc >> 1) & 1), abort_flag, p.status))
         break;
@@ -504,10 +554,11 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const TcParams p) 
         // ytile + (u - u0) * du + (v - v0) * dv.  Streaming stores: the
         // output is not read again here, so it should not displace the
         // input halo lines the producers still read from L2.
-        float *ytile = p.y + ((long long)tl.b * p.ysb + (long long)tl.ow * p.ysw +
-                              (long long)tl.u0 * p.ysu + (long long)tl.v0 * p.ysv) * p.Cout + co;
+        float *ytile = p.y + sg.yoff +
+                       ((long long)tl.b * p.ysb + (long long)tl.ow * p.ysw +
+                        (long long)tl.u0 * p.ysu + (long long)tl.v0 * p.ysv) * p.Cout + co;
         const long long du = p.ysu * (long long)p.Cout, dv = p.ysv * (long long)p.Cout;
-        const int urows = min(p.MH * 16, p.OU - tl.u0), vcols = min(8, p.OV - tl.v0);
+        const int urows = min(p.MH * 16, sg.OU - tl.u0), vcols = min(8, sg.OV - tl.v0);
         for (int c0 = 0; c0 < p.MH * 128; c0 += 64) {
           uint32_t r[4][16];
 #pragma unroll
@@ -558,17 +609,30 @@ struct TapMap {
   int K[3], base[3], mul[3], KO[3];
 };
 
+// The B-tile images of every segment of a launch: segment c (blockIdx.y)
+// has T[c] taps chosen by tm[c], its images at byte off[c] of each part.
+struct PrepSegs {
+  int T[kMaxSeg];
+  long long off[kMaxSeg];
+  TapMap tm[kMaxSeg];
+};
+
 // Re-lay the kernel tensor into B-tile images: [ntile][cblock][tap][chunk j]
 // [n < BN][16 B], element (n, k) with k = cb*CPB + j*EPC + e.  FWD reads
 // W[tap][k][n]; BWDI reads the channel-exchanged kernel W[tap][n][k] (kernel
-// layout [tap][Ci][Co]), taps chosen by `tm`.
+// layout [tap][Ci][Co]), taps chosen by the segment's TapMap.
 template <int KIND>
-__global__ void prep_weights(const float *__restrict__ w, uint8_t *__restrict__ hi,
-                             uint8_t *__restrict__ lo, int T, int Ci, int Co, int K, int N,
-                             int BN, int CPB, int NCB, int n_tiles, int bwd_input, TapMap tm) {
+__global__ void prep_weights(const float *__restrict__ w, uint8_t *__restrict__ hi_base,
+                             uint8_t *__restrict__ lo_base, int Ci, int Co, int K, int N,
+                             int BN, int CPB, int NCB, int n_tiles, int bwd_input,
+                             const __grid_constant__ PrepSegs ps) {
   // the convolution launched next may start its prologue and halo staging
   // now; its weight loader waits for this grid (griddepcontrol.wait)
   asm volatile("griddepcontrol.launch_dependents;");
+  const int T = ps.T[blockIdx.y];
+  const TapMap &tm = ps.tm[blockIdx.y];
+  uint8_t *hi = hi_base + ps.off[blockIdx.y];
+  uint8_t *lo = lo_base ? lo_base + ps.off[blockIdx.y] : nullptr;
   constexpr int EPC = (KIND == K_TF32) ? 4 : 8;
   const int NCH = CPB / EPC;
   const long long total = (long long)n_tiles * NCB * T * NCH * BN;
@@ -697,12 +761,15 @@ int *status_ptr() {
 // Priorities: two 128-pixel halves (N = 256) first; then the widest channel
 // block (fewer, fuller halo stages for the producers); then the most taps per
 // weight slot (fewer barrier polls between MMAs).
-bool plan(TcParams &p, const View &v, int kind) {
+// `v` holds the largest halo extents of the launch's segments; t_slot is the
+// most taps of one segment (weight slots), t_table the taps of all segments
+// (the shared-memory tap table).
+bool plan(TcParams &p, const View &v, int kind, int t_slot, int t_table) {
   const int EB = (kind == K_TF32) ? 4 : 2;
   const int parts = (kind == K_BF16X3) ? 2 : 1;
   p.BN = 128;  // output channels per tile = the MMA's M
   p.n_tiles = (v.Cout + p.BN - 1) / p.BN;
-  p.T = v.KW * v.KU * v.KV;
+  p.T = t_slot;
   p.NH = 2;
   const int cb0 = std::min(128, (int)((v.Cin * EB + 31) / 32 * 32));
   bool found = false;
@@ -730,7 +797,7 @@ bool plan(TcParams &p, const View &v, int kind) {
       q.PS = q.HP + (((1 - q.HP) % 8) + 8) % 8;  // plane stride = 1 (mod 8) pixels
       if (q.PS >= 16384 || q.HV >= 16384) continue;
       q.halo_bytes = (unsigned)q.PS * 16u * (unsigned)q.NCH;
-      const long long fixed = (long long)q.NH * parts * q.halo_bytes + 512 + 4LL * q.T;
+      const long long fixed = (long long)q.NH * parts * q.halo_bytes + 512 + 4LL * t_table;
       const long long room = kSmemMax - fixed;
       if (room <= 0) continue;
       // at least two weight slots
@@ -759,13 +826,13 @@ bool plan(TcParams &p, const View &v, int kind) {
   return true;
 }
 
-template <int KIND>
+template <int KIND, bool MULTI>
 int launch(const TcParams &p, size_t smem, cudaStream_t s) {
   static bool attr_set[64] = {false};
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev >= 0 && dev < 64 && !attr_set[dev]) {
-    OWL_CUDA(cudaFuncSetAttribute(conv_tc_kernel<KIND>,
+    OWL_CUDA(cudaFuncSetAttribute(conv_tc_kernel<KIND, MULTI>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemMax));
     attr_set[dev] = true;
   }
@@ -781,7 +848,7 @@ int launch(const TcParams &p, size_t smem, cudaStream_t s) {
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  cudaError_t e = cudaLaunchKernelEx(&cfg, conv_tc_kernel<KIND>, p);
+  cudaError_t e = cudaLaunchKernelEx(&cfg, conv_tc_kernel<KIND, MULTI>, p);
   note_launch();
   if (e != cudaSuccess) return cuda_fail(e, "conv_tc_kernel");
   return kOk;
@@ -789,52 +856,105 @@ int launch(const TcParams &p, size_t smem, cudaStream_t s) {
 
 // One launch over a view: `x` is read, `y` written, `tm` picks the taps of
 // the kernel tensor `w` ([taps][Ci][Co]); bwd_input exchanges its channels.
-int run_view(int prec, const View &v, const TapMap &tm, bool bwd_input, int Ci, int Co,
+// One segment of a launch: a view (output extents, pads, taps), the kernel
+// taps it uses, and its output origin in y (elements).
+struct SegSpec {
+  View v;
+  TapMap tm;
+  long long yoff;
+};
+
+// One launch over up to kMaxSeg segments that share the input, the channels
+// and the strides: x is read, y written, `w` ([taps][Ci][Co]) re-laid out
+// per segment; bwd_input exchanges its channels.
+int run_segs(int prec, int nseg_in, const SegSpec *sp, bool bwd_input, int Ci, int Co,
              const float *x, const float *w, float *y, cudaStream_t s) {
   const int kind = prec == OWLGPU_PREC_TF32 ? K_TF32 : (prec == OWLGPU_PREC_BF16X3 ? K_BF16X3 : K_BF16);
-  if (v.OW * (long long)v.OU * v.OV * v.B == 0 || v.Cout == 0) return kOk;
+  // segments with work, and the union of their halo extents
+  int idx[kMaxSeg], nseg = 0, spw = 0, spu = 0, spv = 0, t_slot = 0, t_table = 0;
+  for (int c = 0; c < nseg_in && c < kMaxSeg; ++c) {
+    const View &v = sp[c].v;
+    if (v.OW * (long long)v.OU * v.OV * v.B == 0 || v.Cout == 0) continue;
+    idx[nseg++] = c;
+    spw = std::max(spw, (v.KW - 1) * v.dw);
+    spu = std::max(spu, (v.KU - 1) * v.du);
+    spv = std::max(spv, (v.KV - 1) * v.dv);
+    t_slot = std::max(t_slot, v.KW * v.KU * v.KV);
+    t_table += v.KW * v.KU * v.KV;
+  }
+  if (nseg == 0) return kOk;
+  View pv = sp[idx[0]].v;
+  pv.KW = spw + 1; pv.KU = spu + 1; pv.KV = spv + 1;
+  pv.dw = pv.du = pv.dv = 1;
   TcParams p{};
-  if (v.Cin == 0 || !plan(p, v, kind)) return kErrUnsupported;
+  if (pv.Cin == 0 || !plan(p, pv, kind, t_slot, t_table)) return kErrUnsupported;
   p.x = x; p.y = y;
-  p.B = v.B; p.IW = v.IW; p.IU = v.IU; p.IV = v.IV; p.OW = v.OW; p.OU = v.OU; p.OV = v.OV;
-  p.KW = v.KW; p.KU = v.KU; p.KV = v.KV; p.dw = v.dw; p.du = v.du; p.dv = v.dv;
-  p.pw = v.pw; p.pu = v.pu; p.pv = v.pv;
-  p.sw = v.sw; p.su = v.su; p.sv = v.sv;
-  p.xsb = v.xsb; p.xsw = v.xsw; p.xsu = v.xsu; p.xsv = v.xsv;
-  p.ysb = v.ysb; p.ysw = v.ysw; p.ysu = v.ysu; p.ysv = v.ysv;
-  p.Cin = v.Cin; p.Cout = v.Cout;
-  p.u_tiles = (v.OU + 16 * p.MH - 1) / (16 * p.MH);
-  p.v_tiles = (v.OV + 7) / 8;
-  p.total_tiles = (long long)v.B * v.OW * p.u_tiles * p.v_tiles * p.n_groups;
+  p.B = pv.B; p.IW = pv.IW; p.IU = pv.IU; p.IV = pv.IV;
+  p.sw = pv.sw; p.su = pv.su; p.sv = pv.sv;
+  p.xsb = pv.xsb; p.xsw = pv.xsw; p.xsu = pv.xsu; p.xsv = pv.xsv;
+  p.ysb = pv.ysb; p.ysw = pv.ysw; p.ysu = pv.ysu; p.ysv = pv.ysv;
+  p.Cin = pv.Cin; p.Cout = pv.Cout;
+  p.nseg = nseg;
+  long long tiles = 0;
+  size_t woff = 0;
+  int toff = 0;
+  for (int k = 0; k < nseg; ++k) {
+    const View &v = sp[idx[k]].v;
+    Seg &g = p.seg[k];
+    g.tile0 = tiles;
+    g.yoff = sp[idx[k]].yoff;
+    g.woff = (long long)woff;
+    g.OW = v.OW; g.OU = v.OU; g.OV = v.OV;
+    g.u_tiles = (v.OU + 16 * p.MH - 1) / (16 * p.MH);
+    g.v_tiles = (v.OV + 7) / 8;
+    g.KW = v.KW; g.KU = v.KU; g.KV = v.KV;
+    g.dw = v.dw; g.du = v.du; g.dv = v.dv;
+    g.pw = v.pw; g.pu = v.pu; g.pv = v.pv;
+    g.T = v.KW * v.KU * v.KV;
+    g.NSL = (g.T + p.TPS - 1) / p.TPS;
+    g.toff = toff;
+    tiles += (long long)v.B * v.OW * g.u_tiles * g.v_tiles * p.n_groups;
+    toff += g.T;
+    woff += (size_t)p.n_tiles * p.NCB * g.T * p.tile_bytes;
+  }
+  p.total_tiles = tiles;
   p.idesc = instr_desc(kind == K_TF32 ? 2u : 1u, (uint32_t)(128 * p.MH));
-  p.vec_in = ((uintptr_t)x % 16 == 0) && (v.Cin % 4 == 0);
-  p.vec_out = ((uintptr_t)y % 16 == 0) && (v.Cout % 4 == 0);
+  p.vec_in = ((uintptr_t)x % 16 == 0) && (pv.Cin % 4 == 0);
+  p.vec_out = ((uintptr_t)y % 16 == 0) && (pv.Cout % 4 == 0);
   p.status = status_ptr();
   if (!p.status) {
     set_error("conv_tc: cannot locate device status word");
     return kErrCuda;
   }
   const int parts = kind == K_BF16X3 ? 2 : 1;
-  const size_t wt_bytes = (size_t)p.n_tiles * p.NCB * p.T * p.tile_bytes;
+  const size_t wt_bytes = woff;
   void *wt = nullptr;
   int rc = scratch_alloc(&wt, wt_bytes * parts, s);
   if (rc) return rc;
   p.wt_hi = (const uint8_t *)wt;
   p.wt_lo = parts == 2 ? (const uint8_t *)wt + wt_bytes : nullptr;
   {
-    const long long n = (long long)p.n_tiles * p.NCB * p.T * p.NCH * p.BN;
-    const int blocks = (int)std::min<long long>((n + 255) / 256, 4096);
-    const int K = v.Cin, N = v.Cout;
+    // one launch for every segment's images (blockIdx.y = segment)
+    PrepSegs ps{};
+    for (int k = 0; k < nseg; ++k) {
+      ps.T[k] = p.seg[k].T;
+      ps.off[k] = p.seg[k].woff;
+      ps.tm[k] = sp[idx[k]].tm;
+    }
+    uint8_t *hi = (uint8_t *)wt;
+    uint8_t *lo = parts == 2 ? (uint8_t *)wt + wt_bytes : nullptr;
+    const long long n = (long long)p.n_tiles * p.NCB * t_slot * p.NCH * p.BN;
+    const dim3 grid((unsigned)std::min<long long>((n + 255) / 256, 4096), (unsigned)nseg);
+    const int K = pv.Cin, N = pv.Cout;
     if (kind == K_TF32)
-      prep_weights<K_TF32><<<blocks, 256, 0, s>>>(w, (uint8_t *)wt, nullptr, p.T, Ci, Co, K, N,
-                                                  p.BN, p.CPB, p.NCB, p.n_tiles, bwd_input, tm);
+      prep_weights<K_TF32><<<grid, 256, 0, s>>>(w, hi, nullptr, Ci, Co, K, N, p.BN, p.CPB, p.NCB,
+                                                p.n_tiles, bwd_input, ps);
     else if (kind == K_BF16X3)
-      prep_weights<K_BF16X3><<<blocks, 256, 0, s>>>(w, (uint8_t *)wt, (uint8_t *)wt + wt_bytes,
-                                                    p.T, Ci, Co, K, N, p.BN, p.CPB, p.NCB,
-                                                    p.n_tiles, bwd_input, tm);
+      prep_weights<K_BF16X3><<<grid, 256, 0, s>>>(w, hi, lo, Ci, Co, K, N, p.BN, p.CPB, p.NCB,
+                                                  p.n_tiles, bwd_input, ps);
     else
-      prep_weights<K_BF16><<<blocks, 256, 0, s>>>(w, (uint8_t *)wt, nullptr, p.T, Ci, Co, K, N,
-                                                  p.BN, p.CPB, p.NCB, p.n_tiles, bwd_input, tm);
+      prep_weights<K_BF16><<<grid, 256, 0, s>>>(w, hi, nullptr, Ci, Co, K, N, p.BN, p.CPB, p.NCB,
+                                                p.n_tiles, bwd_input, ps);
     cudaError_t e = cudaGetLastError();
     note_launch();
     if (e != cudaSuccess) {
@@ -843,12 +963,20 @@ int run_view(int prec, const View &v, const TapMap &tm, bool bwd_input, int Ci, 
     }
   }
   const size_t smem = (size_t)p.NH * parts * p.halo_bytes + (size_t)p.NB * parts * p.b_bytes +
-                      (2 * p.NH + 2 * p.NB + 5) * 8 + 16 + 4 * (size_t)p.T;
-  if (kind == K_TF32) rc = launch<K_TF32>(p, smem, s);
-  else if (kind == K_BF16X3) rc = launch<K_BF16X3>(p, smem, s);
-  else rc = launch<K_BF16>(p, smem, s);
+                      (2 * p.NH + 2 * p.NB + 5) * 8 + 16 + 4 * (size_t)t_table;
+  const bool multi = p.nseg > 1;
+  if (kind == K_TF32) rc = multi ? launch<K_TF32, true>(p, smem, s) : launch<K_TF32, false>(p, smem, s);
+  else if (kind == K_BF16X3)
+    rc = multi ? launch<K_BF16X3, true>(p, smem, s) : launch<K_BF16X3, false>(p, smem, s);
+  else rc = multi ? launch<K_BF16, true>(p, smem, s) : launch<K_BF16, false>(p, smem, s);
   scratch_free(wt, s);
   return rc;
+}
+
+int run_view(int prec, const View &v, const TapMap &tm, bool bwd_input, int Ci, int Co,
+             const float *x, const float *w, float *y, cudaStream_t s) {
+  SegSpec sp{v, tm, 0};
+  return run_segs(prec, 1, &sp, bwd_input, Ci, Co, x, w, y, s);
 }
 
 // The whole kernel over a geometry: forward, or stride-1 backward-input
@@ -923,6 +1051,15 @@ int run_bwd_input_strided(int prec, const ConvGeom &g, float *dx, const float *w
     }
   if (any_empty)
     OWL_CUDA(cudaMemsetAsync(dx, 0, sizeof(float) * (size_t)g.x_elems(), s));
+  // the classes that receive taps, kMaxSeg per launch
+  SegSpec segs[kMaxSeg];
+  int nseg = 0;
+  auto flush = [&]() {
+    const int rc = nseg ? run_segs(prec, nseg, segs, true, (int)g.Ci, (int)g.Co, dy, w, dx, s)
+                        : (int)kOk;
+    nseg = 0;
+    return rc;
+  };
   for (int r0 = 0; r0 < S[0]; ++r0)
     for (int r1 = 0; r1 < S[1]; ++r1)
       for (int r2 = 0; r2 < S[2]; ++r2) {
@@ -938,18 +1075,21 @@ int run_bwd_input_strided(int prec, const ConvGeom &g, float *dx, const float *w
         v.pw = ax[0].pad; v.pu = ax[1].pad; v.pv = ax[2].pad;
         v.sw = v.su = v.sv = 1;
         v.ysw = YS[0] * S[0]; v.ysu = YS[1] * S[1]; v.ysv = YS[2] * S[2];
-        float *y = dx + (r0 * YS[0] + r1 * YS[1] + r2 * YS[2]) * (long long)g.Ci;
-        TapMap tm;
+        SegSpec &sg = segs[nseg++];
+        sg.v = v;
+        sg.yoff = (r0 * YS[0] + r1 * YS[1] + r2 * YS[2]) * (long long)g.Ci;
         for (int a = 0; a < 3; ++a) {
-          tm.K[a] = ax[a].K;
-          tm.base[a] = ax[a].base;
-          tm.mul[a] = ax[a].mul;
-          tm.KO[a] = KO[a];
+          sg.tm.K[a] = ax[a].K;
+          sg.tm.base[a] = ax[a].base;
+          sg.tm.mul[a] = ax[a].mul;
+          sg.tm.KO[a] = KO[a];
         }
-        const int rc = run_view(prec, v, tm, true, (int)g.Ci, (int)g.Co, dy, w, y, s);
-        if (rc) return rc;
+        if (nseg == kMaxSeg) {
+          const int rc = flush();
+          if (rc) return rc;
+        }
       }
-  return kOk;
+  return flush();
 }
 
 }  // namespace
