@@ -364,7 +364,9 @@ def accuracy(nn, precision, batch=2):
 
 def bench_pool(reps: int = 20):
     """Config-3 pooling on [4;32;32;32;64] float32: max/avg pool3d 2x2x2
-    stride 2 forward and backward, plus config-1 max_pool2d with argmax.
+    stride 2 forward and backward, plus config-1 max_pool2d with argmax, and
+    upsampling2d 2x2 forward and backward on the same data seen as
+    [128;32;32;64] (33.5 MB in, 134 MB out).
 
     `us` is the device time per call of `reps` calls captured in one CUDA
     graph and replayed, each call on its own copy of the inputs; the copies
@@ -395,6 +397,9 @@ def bench_pool(reps: int = 20):
            for _ in range(copies)]
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     k3, s3 = [2, 2, 2], [2, 2, 2]
+    xv = [x.view(128, 32, 32, 64) for x in xs]
+    udys = [torch.from_numpy(rng.standard_normal((128, 64, 64, 64)).astype(np.float32)).cuda()
+            for _ in range(3)]
     cases = [
         ("max_pool3d", lambda i: nn.max_pool3d(xs[i], k3, s3, "SAME"), xb + yb),
         ("avg_pool3d", lambda i: nn.avg_pool3d(xs[i], k3, s3, "SAME"), xb + yb),
@@ -405,6 +410,9 @@ def bench_pool(reps: int = 20):
         ("max_pool2d_argmax c1",
          lambda i: nn.max_pool2d_argmax(x2s[i], [2, 2], [2, 2], "SAME"),
          x2s[0].numel() * 4 + x2s[0].numel() // 4 * (4 + 8)),
+        ("upsampling2d 2x2", lambda i: nn.upsampling2d(xv[i], [2, 2]), 5 * xb),
+        ("upsampling2d_backward 2x2",
+         lambda i: nn.upsampling2d_backward(xv[i], [2, 2], udys[i % len(udys)]), 5 * xb),
     ]
     out = {}
     stream = torch.cuda.current_stream()

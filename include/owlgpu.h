@@ -707,6 +707,56 @@ int owlgpu_float64_ndarray_avgpool_cuboid_backward(
     long row_stride, long dpt_stride, long padding OWLGPU_DEVICE_ARGS);
 
 /* ======================================================================
+ * Nearest-neighbour 2-D upsampling (Owl's upsampling2d), host drop-in
+ * (owl_*) and device-resident (owlgpu_*) forms.
+ *
+ * replaces stub_*_ndarray_upsampling_spatial_backward_native
+ * (owl_ndarray_upsampling.ml:9-35, owl_ndarray_upsampling_impl.h:9-58):
+ * (input_grad written, output_grad, batches, input_cols, input_rows,
+ * in_channel, output_cols, output_rows, col_scale, row_scale).
+ * input_grad[b][ic][ir][ch] = sum of output_grad over the output positions
+ * whose (min(c / col_scale, input_cols - 1), min(r / row_scale,
+ * input_rows - 1)) is (ic, ir), added in the stub's order.
+ *
+ * upsampling_spatial is the forward, which Owl computes in OCaml as
+ * repeat input [|1; col_scale; row_scale; 1|] (owl_dense_ndarray_generic.ml:
+ * 8223-8233): output[b][c][r][ch] = input[b][c / col_scale][r / row_scale][ch];
+ * output_cols/rows must equal input_cols/rows times the scales.
+ * ====================================================================== */
+int owl_float32_ndarray_upsampling_spatial_backward(
+    float *input_grad, const float *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long output_cols, long output_rows,
+    long col_scale, long row_scale);
+int owl_float64_ndarray_upsampling_spatial_backward(
+    double *input_grad, const double *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long output_cols, long output_rows,
+    long col_scale, long row_scale);
+int owl_float32_ndarray_upsampling_spatial(
+    const float *input, float *output, long batches, long input_cols,
+    long input_rows, long in_channel, long output_cols, long output_rows,
+    long col_scale, long row_scale);
+int owl_float64_ndarray_upsampling_spatial(
+    const double *input, double *output, long batches, long input_cols,
+    long input_rows, long in_channel, long output_cols, long output_rows,
+    long col_scale, long row_scale);
+int owlgpu_float32_ndarray_upsampling_spatial_backward(
+    float *input_grad, const float *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long output_cols, long output_rows,
+    long col_scale, long row_scale OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_ndarray_upsampling_spatial_backward(
+    double *input_grad, const double *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long output_cols, long output_rows,
+    long col_scale, long row_scale OWLGPU_DEVICE_ARGS);
+int owlgpu_float32_ndarray_upsampling_spatial(
+    const float *input, float *output, long batches, long input_cols,
+    long input_rows, long in_channel, long output_cols, long output_rows,
+    long col_scale, long row_scale OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_ndarray_upsampling_spatial(
+    const double *input, double *output, long batches, long input_cols,
+    long input_rows, long in_channel, long output_cols, long output_rows,
+    long col_scale, long row_scale OWLGPU_DEVICE_ARGS);
+
+/* ======================================================================
  * Allocation-free entry point.  No counterpart in the reference: Owl's C
  * stubs allocate their own scratch with malloc.  This is the float32 2-D
  * conv backward_kernel (same arguments and results as

@@ -339,3 +339,40 @@ DEF_POOL_ALL(double, float64, f64, avgpool, 1)
   }
 DEF_ARG(float, float32, f32)
 DEF_ARG(double, float64, f64)
+
+/* ---- nearest-neighbour 2-D upsampling ----------------------------------
+ * Backward: owl_ndarray_upsampling_impl.h:9-58 -- zero dX, then for every
+ * output position (b, c, r) in order, dX at (min(c / sc, IC - 1),
+ * min(r / sr, IR - 1)) += dY.  Forward: Owl's upsampling2d is
+ * `repeat x [|1; sc; sr; 1|]` (owl_dense_ndarray_generic.ml:8223-8233), so
+ * y[b][c][r] = x[b][c / sc][r / sr] over the repeated extents. */
+#define DEF_UP(TY, NAME)                                                                        \
+  int oracle_##NAME##_ndarray_upsampling_spatial_backward(                                      \
+      TY *dx, const TY *dy, long B, long IC, long IR, long Ch, long OC, long OR, long sc,       \
+      long sr) {                                                                                 \
+    memset(dx, 0, sizeof(TY) * (size_t)(B * IC * IR * Ch));                                     \
+    for (long b = 0; b < B; ++b)                                                                 \
+      for (long c = 0; c < OC; ++c) {                                                            \
+        const long ic = c / sc < IC - 1 ? c / sc : IC - 1;                                       \
+        for (long r = 0; r < OR; ++r) {                                                          \
+          const long ir = r / sr < IR - 1 ? r / sr : IR - 1;                                    \
+          TY *d = dx + ((b * IC + ic) * IR + ir) * Ch;                                           \
+          const TY *s = dy + ((b * OC + c) * OR + r) * Ch;                                       \
+          for (long i = 0; i < Ch; ++i) d[i] += s[i];                                            \
+        }                                                                                        \
+      }                                                                                          \
+    return 0;                                                                                    \
+  }                                                                                              \
+  int oracle_##NAME##_ndarray_upsampling_spatial(                                               \
+      const TY *x, TY *y, long B, long IC, long IR, long Ch, long OC, long OR, long sc,         \
+      long sr) {                                                                                 \
+    if (OC != IC * sc || OR != IR * sr) return -1;                                               \
+    for (long b = 0; b < B; ++b)                                                                 \
+      for (long c = 0; c < OC; ++c)                                                              \
+        for (long r = 0; r < OR; ++r)                                                            \
+          memcpy(y + ((b * OC + c) * OR + r) * Ch, x + ((b * IC + c / sc) * IR + r / sr) * Ch,   \
+                 sizeof(TY) * (size_t)Ch);                                                       \
+    return 0;                                                                                    \
+  }
+DEF_UP(float, float32)
+DEF_UP(double, float64)

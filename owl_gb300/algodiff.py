@@ -406,6 +406,13 @@ class _NNOps:
         return self._pool("avg_pool3d", lambda x: g.avg_pool3d(x, b, s, padding),
                           lambda x, o: g.avg_pool3d_backward(padding, x, b, s, o), a)
 
+    def upsampling2d(self, a, s):
+        """AD:2889-2910 upsampling2d (a:input, s:size); reverse =
+        upsampling2d_backward on the output adjoint."""
+        g = self.g
+        return self._pool("upsampling2d", lambda x: g.upsampling2d(x, s),
+                          lambda x, o: g.upsampling2d_backward(x, s, o), a)
+
 
 class Algodiff:
     """``Algodiff`` over one stub provider: ``ad.NN`` (conv/pool),

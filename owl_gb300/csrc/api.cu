@@ -170,6 +170,22 @@ static int make_pool(const char *fn, PoolGeom &g, long B, long IC, long IR, long
   return kOk;
 }
 
+static int make_up(const char *fn, UpGeom &g, bool fwd, long B, long IC, long IR, long Ch,
+                   long OC, long OR, long sc, long sr) {
+  if (bad_dims({B, IC, IR, Ch, OC, OR})) return invalid(fn, "negative or oversized dimension");
+  if (bad_pos({sc, sr})) return invalid(fn, "scale must be >= 1");
+  // forward: the output is exactly the repeated input (Owl's repeat); the
+  // backward stub accepts any output extent but needs an input position
+  // to clamp into
+  if (fwd && (OC != IC * sc || OR != IR * sr))
+    return invalid(fn, "output must be input_cols * col_scale x input_rows * row_scale");
+  if (!fwd && B * Ch > 0 && (IC == 0 || IR == 0) && OC * OR > 0)
+    return invalid(fn, "empty input with a non-empty output gradient");
+  g.B = B; g.IC = IC; g.IR = IR; g.Ch = Ch; g.OC = OC; g.OR = OR;
+  g.sc = (int)sc; g.sr = (int)sr;
+  return kOk;
+}
+
 // ---- host drop-in staging --------------------------------------------------
 
 static std::atomic<int> g_precision{-1};
@@ -403,6 +419,27 @@ static int pool_fwd_host(PoolMode mode, const PoolGeom &g, const void *x, void *
     gc.B = nb;
     return pool_fwd(dtype_of<T>(), mode, gc, (T *)p[0] + b0 * xs, (T *)p[1] + b0 * ys,
                     arg ? (int64_t *)p[2] : nullptr, s);
+  });
+}
+
+// Upsampling is independent per sample: staged in batch chunks.  `x` is the
+// array read (input, or dy), `y` the array written (output, or dx).
+template <typename T>
+static int up_host(bool fwd, const UpGeom &g, const void *x, void *y) {
+  const size_t xb = sizeof(T) * (size_t)(fwd ? g.x_elems() : g.y_elems());
+  const size_t yb = sizeof(T) * (size_t)(fwd ? g.y_elems() : g.x_elems());
+  std::vector<Buf> bufs = {{x, xb, true, false, true}, {y, yb, false, true, true}};
+  const int chunks = chunks_for(bufs, g.B);
+  const int64_t xs = (int64_t)(xb / sizeof(T)) / std::max<int64_t>(g.B, 1);
+  const int64_t ys = (int64_t)(yb / sizeof(T)) / std::max<int64_t>(g.B, 1);
+  return host_call(bufs, g.B, chunks,
+                   [&](std::vector<void *> &p, int64_t b0, int64_t nb, cudaStream_t s) {
+    UpGeom gc = g;
+    gc.B = nb;
+    const T *px = (const T *)p[0] + b0 * xs;
+    T *py = (T *)p[1] + b0 * ys;
+    return fwd ? upsample_fwd(dtype_of<T>(), gc, px, py, s)
+               : upsample_bwd(dtype_of<T>(), gc, py, px, s);
   });
 }
 
@@ -855,5 +892,53 @@ CONV3D_ALL(float64, double)
 
 POOL_ALL(float32, float)
 POOL_ALL(float64, double)
+
+// Upsampling: the backward keeps the stub's argument order (input_grad
+// written first, then output_grad); the forward, which Owl computes with
+// repeat in OCaml, takes the same geometry.
+#define UPSAMPLE(KIND, T)                                                                     \
+  int owl_##KIND##_ndarray_upsampling_spatial_backward(                                      \
+      T *input_grad, const T *output_grad, long batches, long input_cols, long input_rows,   \
+      long in_channel, long output_cols, long output_rows, long col_scale, long row_scale) { \
+    UpGeom g;                                                                               \
+    int rc = make_up("upsampling_spatial_backward", g, false, batches, input_cols,          \
+                     input_rows, in_channel, output_cols, output_rows, col_scale, row_scale); \
+    if (rc) return rc;                                                                      \
+    return up_host<T>(false, g, output_grad, input_grad);                                   \
+  }                                                                                         \
+  int owlgpu_##KIND##_ndarray_upsampling_spatial_backward(                                   \
+      T *input_grad, const T *output_grad, long batches, long input_cols, long input_rows,   \
+      long in_channel, long output_cols, long output_rows, long col_scale, long row_scale,   \
+      int precision, void *stream) {                                                        \
+    (void)precision;                                                                        \
+    UpGeom g;                                                                               \
+    int rc = make_up("upsampling_spatial_backward", g, false, batches, input_cols,          \
+                     input_rows, in_channel, output_cols, output_rows, col_scale, row_scale); \
+    if (rc) return rc;                                                                      \
+    return upsample_bwd(dtype_of<T>(), g, input_grad, output_grad, (cudaStream_t)stream);   \
+  }                                                                                         \
+  int owl_##KIND##_ndarray_upsampling_spatial(                                               \
+      const T *input, T *output, long batches, long input_cols, long input_rows,            \
+      long in_channel, long output_cols, long output_rows, long col_scale, long row_scale) { \
+    UpGeom g;                                                                               \
+    int rc = make_up("upsampling_spatial", g, true, batches, input_cols, input_rows,        \
+                     in_channel, output_cols, output_rows, col_scale, row_scale);           \
+    if (rc) return rc;                                                                      \
+    return up_host<T>(true, g, input, output);                                              \
+  }                                                                                         \
+  int owlgpu_##KIND##_ndarray_upsampling_spatial(                                            \
+      const T *input, T *output, long batches, long input_cols, long input_rows,            \
+      long in_channel, long output_cols, long output_rows, long col_scale, long row_scale,  \
+      int precision, void *stream) {                                                        \
+    (void)precision;                                                                        \
+    UpGeom g;                                                                               \
+    int rc = make_up("upsampling_spatial", g, true, batches, input_cols, input_rows,        \
+                     in_channel, output_cols, output_rows, col_scale, row_scale);           \
+    if (rc) return rc;                                                                      \
+    return upsample_fwd(dtype_of<T>(), g, input, output, (cudaStream_t)stream);             \
+  }
+
+UPSAMPLE(float32, float)
+UPSAMPLE(float64, double)
 
 }  // extern "C"

@@ -51,6 +51,16 @@ struct PoolGeom {
 
 enum PoolMode { POOL_MAX = 0, POOL_AVG = 1 };
 
+// Nearest-neighbour 2-D upsampling geometry (owl_ndarray_upsampling_impl.h:
+// 9-32): input [B][IC][IR][Ch], output [B][OC][OR][Ch], scales sc (cols) and
+// sr (rows).
+struct UpGeom {
+  int64_t B, IC, IR, Ch, OC, OR;
+  int sc, sr;
+  int64_t x_elems() const { return B * IC * IR * Ch; }
+  int64_t y_elems() const { return B * OC * OR * Ch; }
+};
+
 // Status codes (mirrors include/owlgpu.h).
 constexpr int kOk = 0;
 constexpr int kErrInvalid = -1;
@@ -98,6 +108,11 @@ int pool_fwd(Dtype dt, PoolMode mode, const PoolGeom &g, const void *x, void *y,
              int64_t *argmax, cudaStream_t s);
 int pool_bwd(Dtype dt, PoolMode mode, const PoolGeom &g, const void *x, const void *dy,
              void *dx, cudaStream_t s);
+
+// y = x repeated sc times along cols and sr times along rows; dx = the sum of
+// dy over each input element's block, in Owl's order.
+int upsample_fwd(Dtype dt, const UpGeom &g, const void *x, void *y, cudaStream_t s);
+int upsample_bwd(Dtype dt, const UpGeom &g, void *dx, const void *dy, cudaStream_t s);
 
 // SIMT (CUDA-core) implementations: the plain FP32 path and the FP64 path.
 int simt_conv_fwd(Dtype dt, const ConvGeom &g, const void *x, const void *w, void *y,

@@ -700,6 +700,38 @@ class NN:
         """G:8158 avg_pool1d_backward."""
         return self._pool1d_backward("avg", padding, input, kernel, stride, output_, out)
 
+    # ======================= upsampling2d (G:8223-8330) =======================
+
+    def upsampling2d(self, input, size, out=None):
+        """G:8223 upsampling2d: `repeat input [|1; size0; size1; 1|]`."""
+        _verify(self._dims(input) == 4 and len(size) == 2,
+                f"upsampling2d: input dimension = {self._dims(input)} (should be 4); "
+                f"size dimension = {len(size)} (should be 2).")
+        B, IC, IR, C = self._shape(input)
+        cs, rs = size
+        output = self._out(out, input, (B, IC * cs, IR * rs, C))
+        self.b.stub(_kind(input), "upsampling_spatial", input, output, B, IC, IR, C, IC * cs,
+                    IR * rs, cs, rs)
+        return output
+
+    def upsampling2d_backward(self, input, size, output, out=None):
+        """G:8249 upsampling2d_backward input size output: the gradient for
+        `input` from the output gradient `output`."""
+        _verify(self._dims(input) == 4 and len(size) == 2,
+                f"upsampling2d_backward: input dimension = {self._dims(input)} (should be 4); "
+                f"size dimension = {len(size)} (should be 2).")
+        B, IC, IR, C = self._shape(input)
+        cs, rs = size
+        osh = self._shape(output)
+        OC, OR = IC * cs, IR * rs
+        _verify(len(osh) == 4 and OC == osh[1] and OR == osh[2],
+                f"upsampling2d_backward: output shape is {list(osh)}; scaled output cols is "
+                f"{OC}, should be equal to the 2nd dimension of output shape; scaled output "
+                f"rows is {OR}, should be equal to the 3rd dimension of output shape.")
+        input_ = self._out(out, input, (B, IC, IR, C))
+        self.b.stub(_kind(input), "upsampling_spatial_backward", input_, output, B, IC, IR, C,
+                    OC, OR, cs, rs)
+        return input_
 
 def _int64_like(a) -> Any:
     if type(a).__module__.startswith("torch"):

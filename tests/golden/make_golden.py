@@ -128,6 +128,35 @@ def parse_file(path: Path) -> list[dict]:
     return cases
 
 
+def parse_upsampling(path: Path) -> list[dict]:
+    """test/unit_upsampling_generic.ml: forward cases compare upsampling2d
+    with ``repeat`` (``test_upsampling2d_forward shape size``); backward
+    cases run upsampling2d_backward with input = ones and output' =
+    sequential (from 0) and list the expected input gradient
+    (``verify_value shape size expected``)."""
+    text = re.sub(r"\(\*.*?\*\)", " ", path.read_text(), flags=re.S)
+    mod = re.search(r"module To_test_upsampling2d = struct(.*?)\n\s*end\b", text, re.S)
+    body = mod.group(1)
+    starts = list(re.finditer(r"let (fun\d+) \(\) =", body))
+    cases = []
+    for i, m in enumerate(starts):
+        blk = body[m.end():starts[i + 1].start() if i + 1 < len(starts) else len(body)]
+        fwd = re.search(r"test_upsampling2d_forward\s*" + ARR + r"\s*" + ARR, blk, re.S)
+        if fwd:
+            cases.append({"file": path.name, "fun": m.group(1), "op": "forward",
+                          "shape": [int(v) for v in _nums(fwd.group(1))],
+                          "size": [int(v) for v in _nums(fwd.group(2))]})
+            continue
+        ex = re.search(r"let expected\s*=\s*" + ARR, blk, re.S)
+        vv = re.search(r"verify_value\s*" + ARR + r"\s*" + ARR, blk, re.S)
+        if ex and vv:
+            cases.append({"file": path.name, "fun": m.group(1), "op": "backward",
+                          "shape": [int(v) for v in _nums(vv.group(1))],
+                          "size": [int(v) for v in _nums(vv.group(2))],
+                          "expected": _nums(ex.group(1))})
+    return cases
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -137,12 +166,15 @@ def main() -> None:
     cases = []
     for f in FILES:
         cases += parse_file(tdir / f)
+    up = parse_upsampling(tdir / "unit_upsampling_generic.ml")
     doc = {"source": "owl test/ alcotest files", "files": FILES,
            "tolerance_sum_abs": 5e-4, "helpers": HELPERS, "cases": cases}
     lines = ",\n".join(json.dumps(c, separators=(",", ":")) for c in cases)
+    up_lines = ",\n".join(json.dumps(c, separators=(",", ":")) for c in up)
     head = json.dumps({k: v for k, v in doc.items() if k != "cases"}, separators=(",", ":"))
-    Path(a.out).write_text(head[:-1] + ',"cases":[\n' + lines + "\n]}\n")
-    print(f"{len(cases)} cases -> {a.out}")
+    Path(a.out).write_text(head[:-1] + ',"cases":[\n' + lines + '\n],"upsampling_cases":[\n' +
+                           up_lines + "\n]}\n")
+    print(f"{len(cases)} cases + {len(up)} upsampling cases -> {a.out}")
 
 
 if __name__ == "__main__":

@@ -81,6 +81,7 @@ POOL_CASES = [
                                                                      [2, 2, 2])),
     ("avg_pool3d", (1, 5, 4, 6, 2), lambda N: lambda x: N.avg_pool3d(SAME, x, [2, 3, 2],
                                                                      [1, 2, 2])),
+    ("upsampling2d", (2, 3, 4, 3), lambda N: lambda x: N.upsampling2d(x, [2, 3])),
 ]
 
 
