@@ -39,6 +39,7 @@
 
 #include <algorithm>
 #include <mutex>
+#include <vector>
 
 #include "../../include/owlgpu.h"
 #include "common.cuh"
@@ -104,9 +105,16 @@ struct TcParams {
   int TPS, NSL;                  // taps per weight slot; plan: slots of the longest segment
   int NH, NB;
   unsigned idesc, tmem_cols;
-  int vec_in, vec_out;
+  int vec_in;
   int nseg;
   Seg seg[kMaxSeg];
+  // Output channels per pixel of y (Cout, or fuse_n).  fuse_n > 0: the
+  // Cout = classes * fuse_n output channels are the residue classes of a
+  // strided backward_input with one tap each, side by side: channel co
+  // belongs to class co / fuse_n, whose outputs start at fuse_yoff[class]
+  // (a depth-to-space epilogue; one staged input tile serves all classes).
+  int ych, fuse_n;
+  long long fuse_yoff[kMaxSeg];
 };
 
 __device__ int g_tc_status;
@@ -554,10 +562,17 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
         // ytile + (u - u0) * du + (v - v0) * dv.  Streaming stores: the
         // output is not read again here, so it should not displace the
         // input halo lines the producers still read from L2.
-        float *ytile = p.y + sg.yoff +
+        int cy = co;
+        long long yo = sg.yoff;
+        if (p.fuse_n > 0) {
+          const int cls = min(co / p.fuse_n, kMaxSeg - 1);
+          cy = co - cls * p.fuse_n;
+          yo = p.fuse_yoff[cls];
+        }
+        float *ytile = p.y + yo +
                        ((long long)tl.b * p.ysb + (long long)tl.ow * p.ysw +
-                        (long long)tl.u0 * p.ysu + (long long)tl.v0 * p.ysv) * p.Cout + co;
-        const long long du = p.ysu * (long long)p.Cout, dv = p.ysv * (long long)p.Cout;
+                        (long long)tl.u0 * p.ysu + (long long)tl.v0 * p.ysv) * p.ych + cy;
+        const long long du = p.ysu * (long long)p.ych, dv = p.ysv * (long long)p.ych;
         const int urows = min(p.MH * 16, sg.OU - tl.u0), vcols = min(8, sg.OV - tl.v0);
         for (int c0 = 0; c0 < p.MH * 128; c0 += 64) {
           uint32_t r[4][16];
@@ -615,6 +630,7 @@ struct PrepSegs {
   int T[kMaxSeg];
   long long off[kMaxSeg];
   TapMap tm[kMaxSeg];
+  int fuse_n;  // > 0: one segment whose output channel n is class n / fuse_n
 };
 
 // Re-lay the kernel tensor into B-tile images: [ntile][cblock][tap][chunk j]
@@ -630,7 +646,6 @@ __global__ void prep_weights(const float *__restrict__ w, uint8_t *__restrict__ 
   // now; its weight loader waits for this grid (griddepcontrol.wait)
   asm volatile("griddepcontrol.launch_dependents;");
   const int T = ps.T[blockIdx.y];
-  const TapMap &tm = ps.tm[blockIdx.y];
   uint8_t *hi = hi_base + ps.off[blockIdx.y];
   uint8_t *lo = lo_base ? lo_base + ps.off[blockIdx.y] : nullptr;
   constexpr int EPC = (KIND == K_TF32) ? 4 : 8;
@@ -644,7 +659,13 @@ __global__ void prep_weights(const float *__restrict__ w, uint8_t *__restrict__ 
     const int tap = (int)(r % T); r /= T;
     const int cb = (int)(r % NCB);
     const int nt = (int)(r / NCB);
-    const int ng = nt * BN + n;
+    const int nf = nt * BN + n;  // output channel of the launch
+    int ng = nf, seg = blockIdx.y;
+    if (ps.fuse_n > 0) {  // class-fused channels: class nf / fuse_n, its channel ng
+      seg = min(nf / ps.fuse_n, kMaxSeg - 1);
+      ng = nf - seg * ps.fuse_n;
+    }
+    const TapMap &tm = ps.tm[seg];
     const int ta = tap / (tm.K[1] * tm.K[2]), tb = tap / tm.K[2] % tm.K[1], tc = tap % tm.K[2];
     const long long orig =
         ((long long)(tm.base[0] + tm.mul[0] * ta) * tm.KO[1] + (tm.base[1] + tm.mul[1] * tb)) *
@@ -654,7 +675,7 @@ __global__ void prep_weights(const float *__restrict__ w, uint8_t *__restrict__ 
     for (int e = 0; e < EPC; ++e) {
       const int k = cb * CPB + j * EPC + e;
       float val = 0.f;
-      if (k < K && ng < N) {
+      if (k < K && nf < N) {
         val = bwd_input ? w[(orig * Ci + ng) * Co + k] : w[(orig * Ci + k) * Co + ng];
       }
       v[e] = val;
@@ -867,8 +888,12 @@ struct SegSpec {
 // One launch over up to kMaxSeg segments that share the input, the channels
 // and the strides: x is read, y written, `w` ([taps][Ci][Co]) re-laid out
 // per segment; bwd_input exchanges its channels.
+//
+// fuse > 0: the segments are residue classes with one tap each and the same
+// extents and pads; they run as a single segment with fuse * nseg output
+// channels and a depth-to-space epilogue (sp[0].v.Cout must be fuse).
 int run_segs(int prec, int nseg_in, const SegSpec *sp, bool bwd_input, int Ci, int Co,
-             const float *x, const float *w, float *y, cudaStream_t s) {
+             const float *x, const float *w, float *y, cudaStream_t s, int fuse = 0) {
   const int kind = prec == OWLGPU_PREC_TF32 ? K_TF32 : (prec == OWLGPU_PREC_BF16X3 ? K_BF16X3 : K_BF16);
   // segments with work, and the union of their halo extents
   int idx[kMaxSeg], nseg = 0, spw = 0, spu = 0, spv = 0, t_slot = 0, t_table = 0;
@@ -883,7 +908,21 @@ int run_segs(int prec, int nseg_in, const SegSpec *sp, bool bwd_input, int Ci, i
     t_table += v.KW * v.KU * v.KV;
   }
   if (nseg == 0) return kOk;
+  int fuse_n = 0, nclass = 1;
+  long long fuse_yoff[kMaxSeg] = {0};
+  TapMap fuse_tm[kMaxSeg];
+  if (fuse > 0 && nseg > 1) {
+    fuse_n = fuse;
+    nclass = nseg;
+    for (int k = 0; k < nseg; ++k) {
+      fuse_yoff[k] = sp[idx[k]].yoff;
+      fuse_tm[k] = sp[idx[k]].tm;
+    }
+    nseg = 1;  // one launch segment; the classes are output channels
+    t_table = t_slot;
+  }
   View pv = sp[idx[0]].v;
+  if (fuse_n) pv.Cout = fuse_n * nclass;
   pv.KW = spw + 1; pv.KU = spu + 1; pv.KV = spv + 1;
   pv.dw = pv.du = pv.dv = 1;
   TcParams p{};
@@ -894,6 +933,9 @@ int run_segs(int prec, int nseg_in, const SegSpec *sp, bool bwd_input, int Ci, i
   p.xsb = pv.xsb; p.xsw = pv.xsw; p.xsu = pv.xsu; p.xsv = pv.xsv;
   p.ysb = pv.ysb; p.ysw = pv.ysw; p.ysu = pv.ysu; p.ysv = pv.ysv;
   p.Cin = pv.Cin; p.Cout = pv.Cout;
+  p.ych = fuse_n ? fuse_n : pv.Cout;
+  p.fuse_n = fuse_n;
+  for (int k = 0; k < kMaxSeg; ++k) p.fuse_yoff[k] = fuse_yoff[k];
   p.nseg = nseg;
   long long tiles = 0;
   size_t woff = 0;
@@ -902,7 +944,7 @@ int run_segs(int prec, int nseg_in, const SegSpec *sp, bool bwd_input, int Ci, i
     const View &v = sp[idx[k]].v;
     Seg &g = p.seg[k];
     g.tile0 = tiles;
-    g.yoff = sp[idx[k]].yoff;
+    g.yoff = fuse_n ? 0 : sp[idx[k]].yoff;
     g.woff = (long long)woff;
     g.OW = v.OW; g.OU = v.OU; g.OV = v.OV;
     g.u_tiles = (v.OU + 16 * p.MH - 1) / (16 * p.MH);
@@ -920,7 +962,6 @@ int run_segs(int prec, int nseg_in, const SegSpec *sp, bool bwd_input, int Ci, i
   p.total_tiles = tiles;
   p.idesc = instr_desc(kind == K_TF32 ? 2u : 1u, (uint32_t)(128 * p.MH));
   p.vec_in = ((uintptr_t)x % 16 == 0) && (pv.Cin % 4 == 0);
-  p.vec_out = ((uintptr_t)y % 16 == 0) && (pv.Cout % 4 == 0);
   p.status = status_ptr();
   if (!p.status) {
     set_error("conv_tc: cannot locate device status word");
@@ -940,6 +981,12 @@ int run_segs(int prec, int nseg_in, const SegSpec *sp, bool bwd_input, int Ci, i
       ps.T[k] = p.seg[k].T;
       ps.off[k] = p.seg[k].woff;
       ps.tm[k] = sp[idx[k]].tm;
+    }
+    if (fuse_n) {
+      ps.fuse_n = fuse_n;
+      // channels past the last class (tile padding) read no weight; their
+      // map entry is any valid one
+      for (int k = 0; k < kMaxSeg; ++k) ps.tm[k] = fuse_tm[k < nclass ? k : 0];
     }
     uint8_t *hi = (uint8_t *)wt;
     uint8_t *lo = parts == 2 ? (uint8_t *)wt + wt_bytes : nullptr;
@@ -1051,15 +1098,8 @@ int run_bwd_input_strided(int prec, const ConvGeom &g, float *dx, const float *w
     }
   if (any_empty)
     OWL_CUDA(cudaMemsetAsync(dx, 0, sizeof(float) * (size_t)g.x_elems(), s));
-  // the classes that receive taps, kMaxSeg per launch
-  SegSpec segs[kMaxSeg];
-  int nseg = 0;
-  auto flush = [&]() {
-    const int rc = nseg ? run_segs(prec, nseg, segs, true, (int)g.Ci, (int)g.Co, dy, w, dx, s)
-                        : (int)kOk;
-    nseg = 0;
-    return rc;
-  };
+  // the classes that receive taps
+  std::vector<SegSpec> segs;
   for (int r0 = 0; r0 < S[0]; ++r0)
     for (int r1 = 0; r1 < S[1]; ++r1)
       for (int r2 = 0; r2 < S[2]; ++r2) {
@@ -1075,7 +1115,8 @@ int run_bwd_input_strided(int prec, const ConvGeom &g, float *dx, const float *w
         v.pw = ax[0].pad; v.pu = ax[1].pad; v.pv = ax[2].pad;
         v.sw = v.su = v.sv = 1;
         v.ysw = YS[0] * S[0]; v.ysu = YS[1] * S[1]; v.ysv = YS[2] * S[2];
-        SegSpec &sg = segs[nseg++];
+        segs.emplace_back();
+        SegSpec &sg = segs.back();
         sg.v = v;
         sg.yoff = (r0 * YS[0] + r1 * YS[1] + r2 * YS[2]) * (long long)g.Ci;
         for (int a = 0; a < 3; ++a) {
@@ -1084,12 +1125,26 @@ int run_bwd_input_strided(int prec, const ConvGeom &g, float *dx, const float *w
           sg.tm.mul[a] = ax[a].mul;
           sg.tm.KO[a] = KO[a];
         }
-        if (nseg == kMaxSeg) {
-          const int rc = flush();
-          if (rc) return rc;
-        }
       }
-  return flush();
+  // One tap per class with common extents and pads (kernel <= stride, as in
+  // a stride-s transpose convolution with kernel s): all classes read the
+  // same dY pixel for an output tile, so they run as one 1x1 convolution
+  // to classes * Ci channels with a depth-to-space epilogue.
+  bool fuse = segs.size() > 1 && segs.size() <= (size_t)kMaxSeg;
+  for (const SegSpec &sg : segs) {
+    const View &a = sg.v, &b0 = segs[0].v;
+    fuse = fuse && a.KW * a.KU * a.KV == 1 && a.OW == b0.OW && a.OU == b0.OU &&
+           a.OV == b0.OV && a.pw == b0.pw && a.pu == b0.pu && a.pv == b0.pv;
+  }
+  if (fuse)
+    return run_segs(prec, (int)segs.size(), segs.data(), true, (int)g.Ci, (int)g.Co, dy, w, dx,
+                    s, (int)g.Ci);
+  for (size_t k0 = 0; k0 < segs.size(); k0 += kMaxSeg) {
+    const int n = (int)std::min<size_t>(kMaxSeg, segs.size() - k0);
+    const int rc = run_segs(prec, n, segs.data() + k0, true, (int)g.Ci, (int)g.Co, dy, w, dx, s);
+    if (rc) return rc;
+  }
+  return kOk;
 }
 
 }  // namespace

@@ -216,3 +216,29 @@ def test_strided_conv3d_tc(gpu_lib, f64_nn):
     dw = from_dev(G.conv3d_backward_kernel(to_dev(x), to_dev(w), st, to_dev(dy)))
     assert _path() == 1
     assert rel(dw, f64_nn.conv3d_backward_kernel(x64, w64, st, dy.astype(np.float64))) <= 1e-2
+
+
+# transpose convolutions whose kernel is not larger than the stride: every
+# residue class of the output receives one tap (or none), so the classes run
+# as one 1x1 convolution with a depth-to-space epilogue
+TCONV = [
+    ((2, 7, 9, 48), (2, 2, 48, 40), (2, 2), SAME),
+    ((1, 6, 5, 24), (2, 2, 24, 16), (3, 3), SAME),
+    ((2, 5, 6, 32), (3, 3, 32, 8), (3, 3), VALID),
+    ((1, 4, 5, 6, 64), (2, 2, 2, 64, 32), (2, 2, 2), SAME),
+]
+
+
+@pytest.mark.parametrize("prec", ["bf16", "bf16x3"])
+@pytest.mark.parametrize("case", TCONV)
+def test_transpose_conv_kernel_le_stride_tc(gpu_lib, f64_nn, prec, case):
+    xs, ks, st, pad = case
+    rng = np.random.default_rng(27)
+    x = rng.uniform(-1, 1, xs).astype(np.float32)
+    w = (rng.standard_normal(ks) * 0.2).astype(np.float32)
+    G = _nn(prec)
+    x64, w64 = x.astype(np.float64), w.astype(np.float64)
+    f = "transpose_conv3d" if len(xs) == 5 else "transpose_conv2d"
+    y = from_dev(getattr(G, f)(to_dev(x), to_dev(w), list(st), pad))
+    assert _path() == 1
+    assert rel(y, getattr(f64_nn, f)(x64, w64, list(st), pad)) <= TOL[prec]
