@@ -706,6 +706,14 @@ int owlgpu_float64_ndarray_avgpool_cuboid_backward(
     long output_cols, long output_rows, long output_dpts, long col_stride,
     long row_stride, long dpt_stride, long padding OWLGPU_DEVICE_ARGS);
 
+/* Pipeline-wait watchdog of the tensor-core kernels: a wait that polls
+ * longer than `cycles` SM clock cycles makes its CTA unwind (wait for its own
+ * copies and MMAs, free tensor memory, return) and sets the device status
+ * word (owlgpu_device_status; host drop-ins return OWLGPU_ERR_TIMEOUT).
+ * cycles <= 0 restores the default (4e9, about 2 s).  Returns the previous
+ * limit; applies to launches made after the call. */
+long long owlgpu_set_wait_limit(long long cycles);
+
 /* ======================================================================
  * Nearest-neighbour 2-D upsampling (Owl's upsampling2d), host drop-in
  * (owl_*) and device-resident (owlgpu_*) forms.

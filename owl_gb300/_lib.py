@@ -36,7 +36,8 @@ def parse_header(path: Path = HEADER) -> dict[str, tuple[str, list[tuple[str, st
     text = re.sub(r"//[^\n]*", " ", text)
     text = text.replace("OWLGPU_DEVICE_ARGS", ", int precision, void *stream")
     out = {}
-    for m in re.finditer(r"\b(int|uint64_t|const char \*)\s*(owl\w+)\s*\(([^;{]*)\)\s*;", text):
+    for m in re.finditer(r"\b(long long|int|uint64_t|const char \*)\s*(owl\w+)\s*\(([^;{]*)\)\s*;",
+                         text):
         ret, name, args = m.group(1), m.group(2), m.group(3)
         params = []
         a = " ".join(args.split())
@@ -53,7 +54,21 @@ def _ctype(t: str):
     if "*" in t:
         return ctypes.c_void_p
     t = t.replace("const", "").strip()
-    return {"long": ctypes.c_long, "int": ctypes.c_int, "uint64_t": ctypes.c_uint64}[t]
+    return {"long": ctypes.c_long, "long long": ctypes.c_longlong, "int": ctypes.c_int,
+            "uint64_t": ctypes.c_uint64}[t]
+
+
+RESTYPE = {"int": ctypes.c_int, "long long": ctypes.c_longlong, "uint64_t": ctypes.c_uint64,
+           "const char *": ctypes.c_char_p}
+
+
+def bind(L: ctypes.CDLL) -> ctypes.CDLL:
+    """Set every declared entry point's argument and result types on L."""
+    for name, (ret, params) in PROTOS.items():
+        f = getattr(L, name)
+        f.argtypes = [_ctype(t) for t, _ in params]
+        f.restype = RESTYPE[ret]
+    return L
 
 
 _lock = threading.Lock()
@@ -71,14 +86,8 @@ def lib() -> ctypes.CDLL:
             raise OSError(
                 f"{LIBPATH} is missing: build it with `python -c 'import __graft_entry__ as g; "
                 f"g.build()'` (there is no CPU fallback)")
-        L = ctypes.CDLL(str(LIBPATH))
-        for name, (ret, params) in PROTOS.items():
-            f = getattr(L, name)
-            f.argtypes = [_ctype(t) for t, _ in params]
-            f.restype = {"int": ctypes.c_int, "uint64_t": ctypes.c_uint64,
-                         "const char *": ctypes.c_char_p}[ret]
-        _lib = L
-        return L
+        _lib = bind(ctypes.CDLL(str(LIBPATH)))
+        return _lib
 
 
 def last_error() -> str:

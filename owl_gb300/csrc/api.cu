@@ -189,6 +189,12 @@ static int make_up(const char *fn, UpGeom &g, bool fwd, long B, long IC, long IR
 // ---- host drop-in staging --------------------------------------------------
 
 static std::atomic<int> g_precision{-1};
+static std::atomic<long long> g_wait_limit{4000000000LL};
+
+long long wait_limit() { return g_wait_limit.load(); }
+long long set_wait_limit(long long cycles) {
+  return g_wait_limit.exchange(cycles > 0 ? cycles : 4000000000LL);
+}
 static std::atomic<int> g_device{0};
 
 static int default_precision() {
@@ -489,6 +495,7 @@ int owlgpu_set_precision(int p) {
   return prev;
 }
 int owlgpu_get_precision(void) { return default_precision(); }
+long long owlgpu_set_wait_limit(long long cycles) { return set_wait_limit(cycles); }
 uint64_t owlgpu_launch_count(void) { return g_launches.load(); }
 int owlgpu_last_conv_path(void) { return t_last_path; }
 int owlgpu_device_status(void) {

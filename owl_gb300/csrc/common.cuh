@@ -138,6 +138,12 @@ int tc_conv_bwd_input(int prec, const ConvGeom &g, float *dx, const float *w, co
 int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, const float *dy,
                        cudaStream_t s);
 
+// Cycles a tensor-core pipeline wait polls before its CTA gives up and sets
+// the device error word (default about 2 s; shorter for a watchdog or for
+// exercising the give-up path).
+long long wait_limit();
+long long set_wait_limit(long long cycles);
+
 // Read (and clear) the tensor-core kernels' device error word on stream s.
 int tc_read_status(int *out, cudaStream_t s);
 int tc_wgrad_read_status(int *out, cudaStream_t s);

@@ -115,19 +115,20 @@ struct TcParams {
   // (a depth-to-space epilogue; one staged input tile serves all classes).
   int ych, fuse_n;
   long long fuse_yoff[kMaxSeg];
+  long long spin_limit;  // cycles a pipeline wait polls before the CTA gives up
 };
 
 __device__ int g_tc_status;
 
 // Bounded mbarrier wait.  Returns false when the CTA is aborting.
 __device__ __forceinline__ bool wait_bar(uint32_t bar, uint32_t parity, volatile int *abort_flag,
-                                         int *status) {
+                                         int *status, long long limit) {
   if (mbar_try_wait(bar, parity)) return true;
   long long t0 = clock64();
   while (true) {
     if (mbar_try_wait(bar, parity)) return true;
     if (*abort_flag) return false;
-    if (clock64() - t0 > kSpinLimit) {
+    if (clock64() - t0 > limit) {
       *abort_flag = 1;
       atomicExch(status, 1);
       return false;
@@ -254,7 +255,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
       for (int cb = 0; cb < p.NCB; ++cb, ++k) {
         const int hs = (int)(k % p.NH);
         const uint32_t ph = (uint32_t)((k / p.NH) & 1);
-        if (!wait_bar(smem_u32(&halo_empty[hs]), ph ^ 1, abort_flag, p.status)) goto done;
+        if (!wait_bar(smem_u32(&halo_empty[hs]), ph ^ 1, abort_flag, p.status, p.spin_limit)) goto done;
         uint8_t *dst = halo + (size_t)hs * PARTS * p.halo_bytes;
         const int cbase = cb * p.CPB;
         for (int r0 = pidx * 2; r0 < nrows; r0 += 2 * kProducerWarps) {
@@ -399,14 +400,14 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
         const uint32_t *toffs = tap_off + p.seg[sc].toff;
         const int abuf = tc & 1;
         const uint32_t aph = (uint32_t)((tc >> 1) & 1);
-        if (!wait_bar(smem_u32(&acc_empty[abuf]), aph ^ 1, abort_flag, p.status)) break;
+        if (!wait_bar(smem_u32(&acc_empty[abuf]), aph ^ 1, abort_flag, p.status, p.spin_limit)) break;
         tc_fence_after();
         const uint32_t d0 = tmem_base + (uint32_t)(abuf * p.NCT * p.MH * 128);
         const int nct = min(p.NCT, p.n_tiles - (int)(t % p.n_groups) * p.NCT);
         uint32_t acc = 0;
         bool ok = true;
         for (int cb = 0; cb < p.NCB && ok; ++cb) {
-          if (!wait_bar(smem_u32(&halo_full[hs]), hph, abort_flag, p.status)) {
+          if (!wait_bar(smem_u32(&halo_full[hs]), hph, abort_flag, p.status, p.spin_limit)) {
             ok = false;
             break;
           }
@@ -416,7 +417,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
           const uint64_t xd_stage =
               smem_desc(halo0 + (uint32_t)hs * PARTS * p.halo_bytes, a_lbo, a_sbo);
           for (int sl = 0; sl < nsl; ++sl) {
-            if (!wait_bar(smem_u32(&b_full[bs]), bph, abort_flag, p.status)) {
+            if (!wait_bar(smem_u32(&b_full[bs]), bph, abort_flag, p.status, p.spin_limit)) {
               ok = false;
               break;
             }
@@ -504,7 +505,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
           for (int sl = 0; sl < nsl; ++sl, ++kb) {
             const int bs = (int)(kb % p.NB);
             if (!wait_bar(smem_u32(&b_empty[bs]), (uint32_t)(((kb / p.NB) & 1) ^ 1), abort_flag,
-                          p.status))
+                          p.status, p.spin_limit))
               goto loader_done;
             const int t0 = sl * p.TPS, nt_ = min(ntap - t0, p.TPS);
             const uint32_t bytes = (uint32_t)nt_ * p.tile_bytes;
@@ -547,7 +548,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
       const Tile tl = decode_tile(p, t, sc);
       const Seg &sg = p.seg[sc];
       const int abuf = tc & 1;
-      if (!wait_bar(smem_u32(&acc_full[abuf]), (uint32_t)((tc >> 1) & 1), abort_flag, p.status))
+      if (!wait_bar(smem_u32(&acc_full[abuf]), (uint32_t)((tc >> 1) & 1), abort_flag, p.status, p.spin_limit))
         break;
       tc_fence_after();
       // TMEM lane = output channel, column = pixel (group g = col / 8, v = col % 8)
@@ -962,6 +963,7 @@ int run_segs(int prec, int nseg_in, const SegSpec *sp, bool bwd_input, int Ci, i
   p.total_tiles = tiles;
   p.idesc = instr_desc(kind == K_TF32 ? 2u : 1u, (uint32_t)(128 * p.MH));
   p.vec_in = ((uintptr_t)x % 16 == 0) && (pv.Cin % 4 == 0);
+  p.spin_limit = wait_limit();
   p.status = status_ptr();
   if (!p.status) {
     set_error("conv_tc: cannot locate device status word");

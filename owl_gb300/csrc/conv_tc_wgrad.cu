@@ -77,6 +77,7 @@ struct WgParams {
   // Every group is phase-uniform: all its taps have the same k*d mod s in
   // each dimension, so its X halo needs only input rows and columns of
   // that phase (every s-th one).
+  long long spin_limit;  // cycles a pipeline wait polls before the CTA gives up
   int ordered;
   unsigned short tap_order[kMaxOrderedTaps];
   unsigned short gstart[kMaxOrderedTaps + 1];
@@ -85,13 +86,13 @@ struct WgParams {
 __device__ int g_tc_status_wg;
 
 __device__ __forceinline__ bool wait_bar(uint32_t bar, uint32_t parity, volatile int *abort_flag,
-                                         int *status) {
+                                         int *status, long long limit) {
   if (mbar_try_wait(bar, parity)) return true;
   long long t0 = clock64();
   while (true) {
     if (mbar_try_wait(bar, parity)) return true;
     if (*abort_flag) return false;
-    if (clock64() - t0 > kSpinLimit) {
+    if (clock64() - t0 > limit) {
       *abort_flag = 1;
       atomicExch(status, 1);
       return false;
@@ -194,7 +195,7 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const __grid_cons
       const int b = (int)(q / p.OW);
       const int st = (int)(k % p.NS);
       if (!wait_bar(smem_u32(&empty[st]), (uint32_t)(((k / p.NS) & 1) ^ 1), abort_flag,
-                    p.status)) {
+                    p.status, p.spin_limit)) {
         staged = false;
         break;
       }
@@ -251,7 +252,7 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const __grid_cons
       // ===================== epilogue: TMEM -> partial dW =====================
       const int q = warp & 3;
       const int ci = mb * 128 + q * 32 + lane;
-      if (wait_bar(smem_u32(acc_full), 0, abort_flag, p.status)) {
+      if (wait_bar(smem_u32(acc_full), 0, abort_flag, p.status, p.spin_limit)) {
         tc_fence_after();
         for (int i = 0; i < ntap; ++i) {
           const int tt = tap_of(i);
@@ -304,7 +305,7 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const __grid_cons
       uint32_t acc = 0;
       bool ok = true;
       for (long long t = t_begin; t < t_end; ++t) {
-        if (!wait_bar(smem_u32(&full[st]), ph, abort_flag, p.status)) {
+        if (!wait_bar(smem_u32(&full[st]), ph, abort_flag, p.status, p.spin_limit)) {
           ok = false;
           break;
         }
@@ -619,6 +620,7 @@ int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, c
   p.idesc = idesc;
   p.vec_x = ((uintptr_t)x % 16 == 0) && (p.Ci % 4 == 0);
   p.vec_y = ((uintptr_t)dy % 16 == 0) && (p.Co % 4 == 0);
+  p.spin_limit = wait_limit();
   p.status = status_word();
   if (!p.status) {
     set_error("wgrad_tc: cannot locate device status word");
