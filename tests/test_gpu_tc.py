@@ -36,6 +36,13 @@ CASES2D = [
     # two co tiles per CTA tile, the last group holding one
     ((2, 13, 11, 64), (3, 3, 64, 384), None, SAME),
     ((1, 7, 7, 256), (3, 3, 256, 512), None, SAME),
+    # outputs taller than 32 rows split into equal tiles of an even height
+    # (MMA N = 8 x rows): 2 x 20, 2 x 26 (last 24), 2 x 28 (the config-2
+    # L1 height), 3 x 22 with dilation
+    ((1, 40, 9, 32), (3, 3, 32, 64), None, SAME),
+    ((1, 50, 8, 16), (3, 3, 16, 128), None, SAME),
+    ((1, 56, 16, 128), (3, 3, 128, 128), None, SAME),
+    ((1, 66, 10, 8), (3, 3, 8, 16), (2, 2), SAME),
 ]
 CASES3D = [
     ((2, 6, 7, 9, 8), (3, 3, 3, 8, 16), None, SAME),
