@@ -51,3 +51,55 @@ def test_chunked_pooling_equals_device_call(gpu_lib):
     da = nn.avg_pool3d_backward("SAME", x, k, s, g)
     assert np.array_equal(da, from_dev(nn.avg_pool3d_backward("SAME", to_dev(x), k, s,
                                                                to_dev(g))))
+
+
+def _pinned(a):
+    import torch
+
+    t = torch.empty(a.shape, dtype=torch.float32, pin_memory=True)
+    t.numpy()[...] = a
+    return t.numpy()
+
+
+CASES_IN_PLACE = [
+    # input, kernel, stride, rate, padding
+    ((6, 20, 18, 64), (3, 3, 64, 128), (1, 1), (1, 1), "SAME"),
+    ((4, 28, 28, 64), (3, 3, 64, 128), (2, 2), (1, 1), "VALID"),
+    ((3, 16, 16, 32), (1, 1, 32, 64), (2, 2), (1, 1), "SAME"),   # residue classes with no tap
+    ((2, 17, 19, 40), (3, 3, 40, 24), (1, 1), (2, 2), "SAME"),
+]
+
+
+@pytest.mark.parametrize("precision", ["bf16", "bf16x3"])
+@pytest.mark.parametrize("case", CASES_IN_PLACE)
+def test_page_locked_conv_equals_device_call(gpu_lib, precision, case):
+    """Tensor-core convolutions through the host drop-in from page-locked
+    arrays (staged in batch chunks on the copy streams) into page-locked
+    `~out` arrays: the result is the device call's, bit for bit, for forward,
+    backward_input (strided, including zero-filled residue classes) and
+    backward_kernel."""
+    from owl_gb300 import _lib
+    from owl_gb300.dense import NN, GpuBackend
+
+    nn = NN(GpuBackend(precision))
+    xs, ks, st, rate, pad = case
+    rng = np.random.default_rng(62)
+    x = rng.uniform(-1, 1, xs).astype(np.float32)
+    w = (rng.standard_normal(ks) * 0.05).astype(np.float32)
+    st, rate = list(st), list(rate)
+    y_dev = from_dev(nn.dilated_conv2d(to_dev(x), to_dev(w), st, rate, pad))
+    dy = rng.standard_normal(y_dev.shape).astype(np.float32)
+    dx_dev = from_dev(nn.dilated_conv2d_backward_input(to_dev(x), to_dev(w), st, rate, to_dev(dy)))
+    dw_dev = from_dev(nn.dilated_conv2d_backward_kernel(to_dev(x), to_dev(w), st, rate, to_dev(dy)))
+    px, pw, pdy = _pinned(x), _pinned(w), _pinned(dy)
+    oy = _pinned(np.full(y_dev.shape, np.nan, np.float32))
+    odx = _pinned(np.full(x.shape, np.nan, np.float32))
+    odw = _pinned(np.full(w.shape, np.nan, np.float32))
+    nn.dilated_conv2d(px, pw, st, rate, pad, out=oy)
+    assert _lib.lib().owlgpu_last_conv_path() == 1
+    nn.dilated_conv2d_backward_input(px, pw, st, rate, pdy, out=odx)
+    nn.dilated_conv2d_backward_kernel(px, pw, st, rate, pdy, out=odw)
+    assert np.array_equal(oy, y_dev)
+    assert np.array_equal(odx, dx_dev)
+    assert np.array_equal(odw, dw_dev)
+    assert _lib.lib().owlgpu_device_status() == 0
