@@ -636,6 +636,32 @@ def bench_algodiff(precision: str, steps: int = 10):
         out[prec] = {"ms_per_step": ms, "images_per_s": 256 / (ms / 1e3),
                      "loss_after": float(loss.item()),
                      "owl_launches_per_step": (_lib.launch_count() - n0) / steps}
+        # The same step captured once as a CUDA graph and replayed (the
+        # parameters are updated in place, so each replay is a real step):
+        # the device time without the Python tape's per-op host cost.
+        try:
+            g = torch.cuda.CUDAGraph()
+            s = torch.cuda.Stream()
+            s.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(s):
+                sgd_step(ad, params, x, onehot, lr=0.01)
+            torch.cuda.current_stream().wait_stream(s)
+            with torch.cuda.graph(g):
+                gloss, _ = sgd_step(ad, params, x, onehot, lr=0.01)
+            for _ in range(3):
+                g.replay()
+            torch.cuda.synchronize()
+            a.record()
+            for _ in range(steps):
+                g.replay()
+            b.record()
+            torch.cuda.synchronize()
+            gms = a.elapsed_time(b) / steps
+            out[prec]["graph"] = {"ms_per_step": gms, "images_per_s": 256 / (gms / 1e3),
+                                  "loss_after": float(gloss.item())}
+            del g
+        except Exception as e:  # report, never lose the bench line
+            out[prec]["graph"] = {"error": f"{type(e).__name__}: {e}"[:200]}
     out["note"] = ("batch 256; conv/pool through libowlgpu, dense layers and softmax in torch "
                    "(cuBLAS); gradients checked against float64 finite differences and the "
                    "oracle in tests/test_gpu_algodiff.py")
