@@ -49,6 +49,14 @@ void scratch_free(void *p, cudaStream_t s) {
   if (p) cudaFreeAsync(p, s);
 }
 
+static thread_local bool t_tc_launched = false;
+void note_tc_launch() { t_tc_launched = true; }
+bool take_tc_launched() {
+  const bool v = t_tc_launched;
+  t_tc_launched = false;
+  return v;
+}
+
 // ---- dispatch between SIMT and tensor-core kernels -----------------------
 
 static bool tc_requested(Dtype dt, int prec) { return dt == F32 && prec != OWLGPU_PREC_FP32; }
@@ -301,12 +309,17 @@ static int host_call(std::vector<Buf> bufs, int64_t batch, int chunks, F body) {
   if (batch <= 0) chunks = 1;
   rc = host_events(*hs, 2 * (size_t)chunks);
   if (rc) return rc;
+  take_tc_launched();  // clear: the status words are read below only if this call used them
+  // one piece: copies and compute in order on one stream (no cross-stream
+  // events, one synchronisation)
+  const bool one = chunks == 1;
+  cudaStream_t cin = one ? hs->s : hs->cin, cout = one ? hs->s : hs->cout;
   for (auto &b : bufs) {
     if (b.bytes == 0) continue;
-    rc = scratch_alloc(&b.dev, b.bytes, hs->cin);
+    rc = scratch_alloc(&b.dev, b.bytes, cin);
     if (rc) break;
     if (b.in && !b.batched) {
-      cudaError_t e = cudaMemcpyAsync(b.dev, b.host, b.bytes, cudaMemcpyHostToDevice, hs->cin);
+      cudaError_t e = cudaMemcpyAsync(b.dev, b.host, b.bytes, cudaMemcpyHostToDevice, cin);
       if (e != cudaSuccess) { rc = cuda_fail(e, "cudaMemcpyAsync(H2D)"); break; }
     }
   }
@@ -319,21 +332,25 @@ static int host_call(std::vector<Buf> bufs, int64_t batch, int chunks, F body) {
       if (!b.in || !b.batched || b.bytes == 0) continue;
       const size_t per = b.bytes / (size_t)batch;
       cudaError_t e = cudaMemcpyAsync((char *)b.dev + per * b0, (const char *)b.host + per * b0,
-                                      per * (b1 - b0), cudaMemcpyHostToDevice, hs->cin);
+                                      per * (b1 - b0), cudaMemcpyHostToDevice, cin);
       if (e != cudaSuccess) { rc = cuda_fail(e, "cudaMemcpyAsync(H2D)"); break; }
     }
     if (rc) break;
-    OWL_CUDA(cudaEventRecord(ein, hs->cin));
-    OWL_CUDA(cudaStreamWaitEvent(hs->s, ein, 0));
+    if (!one) {
+      OWL_CUDA(cudaEventRecord(ein, hs->cin));
+      OWL_CUDA(cudaStreamWaitEvent(hs->s, ein, 0));
+    }
     rc = body(ptrs, b0, b1 - b0, hs->s);
     if (rc) break;
-    OWL_CUDA(cudaEventRecord(ecomp, hs->s));
-    OWL_CUDA(cudaStreamWaitEvent(hs->cout, ecomp, 0));
+    if (!one) {
+      OWL_CUDA(cudaEventRecord(ecomp, hs->s));
+      OWL_CUDA(cudaStreamWaitEvent(hs->cout, ecomp, 0));
+    }
     for (auto &b : bufs) {
       if (!b.out || !b.batched || b.bytes == 0) continue;
       const size_t per = b.bytes / (size_t)batch;
       cudaError_t e = cudaMemcpyAsync((char *)b.host + per * b0, (char *)b.dev + per * b0,
-                                      per * (b1 - b0), cudaMemcpyDeviceToHost, hs->cout);
+                                      per * (b1 - b0), cudaMemcpyDeviceToHost, cout);
       if (e != cudaSuccess) { rc = cuda_fail(e, "cudaMemcpyAsync(D2H)"); break; }
     }
   }
@@ -345,13 +362,13 @@ static int host_call(std::vector<Buf> bufs, int64_t batch, int chunks, F body) {
       if (e != cudaSuccess) { rc = cuda_fail(e, "cudaMemcpyAsync(D2H)"); break; }
     }
   }
-  cudaError_t e1 = cudaStreamSynchronize(hs->cin);
+  cudaError_t e1 = one ? cudaSuccess : cudaStreamSynchronize(hs->cin);
   cudaError_t e2 = cudaStreamSynchronize(hs->s);
-  cudaError_t e3 = cudaStreamSynchronize(hs->cout);
+  cudaError_t e3 = one ? cudaSuccess : cudaStreamSynchronize(hs->cout);
   for (auto &b : bufs) scratch_free(b.dev, hs->s);
   cudaError_t e = e1 != cudaSuccess ? e1 : e2 != cudaSuccess ? e2 : e3;
   if (rc == kOk && e != cudaSuccess) rc = cuda_fail(e, "cudaStreamSynchronize");
-  if (rc == kOk) {
+  if (rc == kOk && take_tc_launched()) {
     int st = 0;
     rc = tc_read_status(&st, hs->s);
     if (rc == kOk && st) {

@@ -146,7 +146,11 @@ long long set_wait_limit(long long cycles);
 
 // Read (and clear) the tensor-core kernels' device error word on stream s.
 int tc_read_status(int *out, cudaStream_t s);
-int tc_wgrad_read_status(int *out, cudaStream_t s);
+int *tc_wgrad_status_word();  // device address of the weight-gradient kernel's status word
+// The calling thread launched a tensor-core kernel (whose watchdog status the
+// host drop-in then reads); take_tc_launched() returns and clears the mark.
+void note_tc_launch();
+bool take_tc_launched();
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 

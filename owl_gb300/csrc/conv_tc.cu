@@ -872,6 +872,7 @@ int launch(const TcParams &p, size_t smem, cudaStream_t s) {
   cfg.numAttrs = 1;
   cudaError_t e = cudaLaunchKernelEx(&cfg, conv_tc_kernel<KIND, MULTI>, p);
   note_launch();
+  note_tc_launch();
   if (e != cudaSuccess) return cuda_fail(e, "conv_tc_kernel");
   return kOk;
 }
@@ -1163,16 +1164,18 @@ int tc_conv_bwd_input(int prec, const ConvGeom &g, float *dx, const float *w, co
   return run_bwd_input_strided(prec, g, dx, w, dy, s);
 }
 
+// Both tensor-core kernels' status words, read with one synchronisation and
+// cleared when set.
 int tc_read_status(int *out, cudaStream_t s) {
-  int *p = status_ptr();
-  if (!p) return kErrCuda;
-  OWL_CUDA(cudaMemcpyAsync(out, p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  int *p = status_ptr(), *pw = tc_wgrad_status_word();
+  if (!p || !pw) return kErrCuda;
+  int v[2] = {0, 0};
+  OWL_CUDA(cudaMemcpyAsync(&v[0], p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  OWL_CUDA(cudaMemcpyAsync(&v[1], pw, sizeof(int), cudaMemcpyDeviceToHost, s));
   OWL_CUDA(cudaStreamSynchronize(s));
-  if (*out) OWL_CUDA(cudaMemsetAsync(p, 0, sizeof(int), s));
-  int wg = 0;
-  int rc = tc_wgrad_read_status(&wg, s);
-  if (rc) return rc;
-  *out |= wg;
+  if (v[0]) OWL_CUDA(cudaMemsetAsync(p, 0, sizeof(int), s));
+  if (v[1]) OWL_CUDA(cudaMemsetAsync(pw, 0, sizeof(int), s));
+  *out = v[0] | v[1];
   return kOk;
 }
 

@@ -434,20 +434,14 @@ int launch(const WgParams &p, size_t smem, int grid, cudaStream_t s) {
     attr[dev] = true;
   }
   wgrad_tc_kernel<KIND><<<grid, kThreads, smem, s>>>(p);
+  note_tc_launch();
   OWL_CHECK_LAUNCH("wgrad_tc_kernel");
   return kOk;
 }
 
 }  // namespace
 
-int tc_wgrad_read_status(int *out, cudaStream_t s) {
-  int *p = status_word();
-  if (!p) return kErrCuda;
-  OWL_CUDA(cudaMemcpyAsync(out, p, sizeof(int), cudaMemcpyDeviceToHost, s));
-  OWL_CUDA(cudaStreamSynchronize(s));
-  if (*out) OWL_CUDA(cudaMemsetAsync(p, 0, sizeof(int), s));
-  return kOk;
-}
+int *tc_wgrad_status_word() { return status_word(); }
 
 int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, const float *dy,
                        cudaStream_t s) {
