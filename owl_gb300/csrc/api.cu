@@ -301,8 +301,14 @@ static int chunks_for(const std::vector<Buf> &bufs, int64_t batch) {
 // streams; only calls whose every batch sample is independent are chunked,
 // and they give the same results as one call.  Device memory comes from the
 // stream-ordered pool, so repeated calls of the same size reuse it.
-template <typename F>
-static int host_call(std::vector<Buf> bufs, int64_t batch, int chunks, F body) {
+// `finish(dev pointers, stream)` runs on the compute stream after the last
+// chunk, before the unbatched outputs are copied back.
+struct NoFinish {
+  int operator()(std::vector<void *> &, cudaStream_t) const { return kOk; }
+};
+template <typename F, typename Fin = NoFinish>
+static int host_call(std::vector<Buf> bufs, int64_t batch, int chunks, F body,
+                     Fin finish = NoFinish()) {
   HostStream *hs;
   int rc = host_stream(&hs);
   if (rc) return rc;
@@ -354,6 +360,7 @@ static int host_call(std::vector<Buf> bufs, int64_t batch, int chunks, F body) {
       if (e != cudaSuccess) { rc = cuda_fail(e, "cudaMemcpyAsync(D2H)"); break; }
     }
   }
+  if (rc == kOk) rc = finish(ptrs, hs->s);
   if (rc == kOk) {
     for (auto &b : bufs) {
       if (!b.out || b.batched || b.bytes == 0) continue;
@@ -402,27 +409,54 @@ template <typename T>
 static int conv_host(ConvOp op, const ConvGeom &g, const void *a, const void *b, const void *c) {
   size_t xb = sizeof(T) * g.x_elems(), wb = sizeof(T) * g.w_elems(), yb = sizeof(T) * g.y_elems();
   // forward and backward_input are independent per batch sample: staged in
-  // chunks; backward_kernel sums over the batch: one piece.
-  const bool chunk = op != OP_BWDK;
+  // chunks.  A float32 backward_kernel is staged in chunks too: each chunk's
+  // weight gradient lands in its own partial, and the partials are summed
+  // in chunk order at the end (deterministic), so the kernels run while the
+  // later chunks are still being copied in.
+  const bool bwdk = op == OP_BWDK;
+  const bool chunk = !bwdk || sizeof(T) == 4;
   std::vector<Buf> bufs;
   if (op == OP_FWD)
     bufs = {{a, xb, true, false, chunk}, {b, wb, true, false, false}, {c, yb, false, true, chunk}};
   else if (op == OP_BWDI)
     bufs = {{a, xb, false, true, chunk}, {b, wb, true, false, false}, {c, yb, true, false, chunk}};
   else
-    bufs = {{a, xb, true, false, false}, {b, wb, false, true, false}, {c, yb, true, false, false}};
+    bufs = {{a, xb, true, false, chunk}, {b, wb, false, true, false}, {c, yb, true, false, chunk}};
   int prec = default_precision();
   const int chunks = chunk ? chunks_for(bufs, g.B) : 1;
   const int64_t xs = g.x_elems() / std::max<int64_t>(g.B, 1);
   const int64_t ys = g.y_elems() / std::max<int64_t>(g.B, 1);
-  return host_call(bufs, g.B, chunks,
-                   [&](std::vector<void *> &p, int64_t b0, int64_t nb, cudaStream_t s) {
-    ConvGeom gc = g;
-    gc.B = nb;
-    T *x = (T *)p[0] + (chunk ? b0 * xs : 0);
-    T *y = (T *)p[2] + (chunk ? b0 * ys : 0);
-    return conv_device<T>(op, gc, x, p[1], y, prec, s);
-  });
+  const long long welems = g.w_elems();
+  float *part = nullptr;  // [chunks][welems] when a backward_kernel is split
+  int ci = 0;
+  const bool split = bwdk && chunks > 1;
+  int rc = host_call(
+      bufs, g.B, chunks,
+      [&](std::vector<void *> &p, int64_t b0, int64_t nb, cudaStream_t s) {
+        ConvGeom gc = g;
+        gc.B = nb;
+        T *x = (T *)p[0] + (chunk ? b0 * xs : 0);
+        T *y = (T *)p[2] + (chunk ? b0 * ys : 0);
+        void *w = p[1];
+        if (split) {
+          if (ci == 0) {
+            const int r = scratch_alloc((void **)&part, sizeof(float) * (size_t)welems * chunks, s);
+            if (r) return r;
+          }
+          w = part + (size_t)welems * ci++;
+        }
+        return conv_device<T>(op, gc, x, w, y, prec, s);
+      },
+      [&](std::vector<void *> &p, cudaStream_t s) {
+        if (!split) return (int)kOk;
+        return sum_partials_f32(part, (float *)p[1], welems, chunks, s);
+      });
+  if (part) {
+    // the call has synchronised its streams; the pool takes the memory back
+    HostStream *hs;
+    if (host_stream(&hs) == kOk) scratch_free(part, hs->s);
+  }
+  return rc;
 }
 
 template <typename T>

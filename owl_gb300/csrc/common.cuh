@@ -147,6 +147,8 @@ long long set_wait_limit(long long cycles);
 // Read (and clear) the tensor-core kernels' device error word on stream s.
 int tc_read_status(int *out, cudaStream_t s);
 int *tc_wgrad_status_word();  // device address of the weight-gradient kernel's status word
+// out[i] = sum over r = 0 .. R-1 of part[r * n + i], in that order.
+int sum_partials_f32(const float *part, float *out, long long n, int R, cudaStream_t s);
 // The calling thread launched a tensor-core kernel (whose watchdog status the
 // host drop-in then reads); take_tc_launched() returns and clears the mark.
 void note_tc_launch();

@@ -443,6 +443,17 @@ int launch(const WgParams &p, size_t smem, int grid, cudaStream_t s) {
 
 int *tc_wgrad_status_word() { return status_word(); }
 
+// out[i] = sum_r part[r][i] for r = 0 .. R-1 in order (deterministic).
+int sum_partials_f32(const float *part, float *out, long long n, int R, cudaStream_t s) {
+  if (n <= 0) return kOk;
+  const bool v4 = n % 4 == 0 && (uintptr_t)out % 16 == 0 && (uintptr_t)part % 16 == 0;
+  const long long work = v4 ? n / 4 : n;
+  const int blocks = (int)std::max<long long>(1, std::min<long long>((work + 127) / 128, 8 * 152));
+  wgrad_reduce<<<blocks, 128, 0, s>>>(part, out, n, R, v4 ? 1 : 0);
+  OWL_CHECK_LAUNCH("wgrad_reduce");
+  return kOk;
+}
+
 int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, const float *dy,
                        cudaStream_t s) {
   if (g.sc > 8 || g.sr > 8 || g.sd > 8) return kErrUnsupported;
