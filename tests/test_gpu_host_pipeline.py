@@ -103,3 +103,29 @@ def test_page_locked_conv_equals_device_call(gpu_lib, precision, case):
     assert np.array_equal(odx, dx_dev)
     assert np.array_equal(odw, dw_dev)
     assert _lib.lib().owlgpu_device_status() == 0
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+def test_chunked_backward_kernel(gpu_lib, precision):
+    """A float32 backward_kernel from page-locked arrays large enough to be
+    staged in batch chunks (51 MB of X and dY): each chunk's weight gradient
+    goes to its own partial and the partials are summed in chunk order.  The
+    products are the device call's; only the grouping of the float32 sums
+    differs, so the result agrees with the device call to float32 rounding
+    (1e-5 relative) and is bit-identical from one call to the next."""
+    from owl_gb300.dense import NN, GpuBackend
+
+    nn = NN(GpuBackend(precision))
+    rng = np.random.default_rng(63)
+    x = rng.uniform(-1, 1, (32, 56, 56, 64)).astype(np.float32)
+    w = (rng.standard_normal((3, 3, 64, 64)) * 0.05).astype(np.float32)
+    dy = rng.standard_normal((32, 56, 56, 64)).astype(np.float32)
+    dw_dev = from_dev(nn.conv2d_backward_kernel(to_dev(x), to_dev(w), [1, 1], to_dev(dy)))
+    px, pw, pdy = _pinned(x), _pinned(w), _pinned(dy)
+    a = _pinned(np.zeros(w.shape, np.float32))
+    b = _pinned(np.zeros(w.shape, np.float32))
+    nn.conv2d_backward_kernel(px, pw, [1, 1], pdy, out=a)
+    nn.conv2d_backward_kernel(px, pw, [1, 1], pdy, out=b)
+    assert np.array_equal(a, b)
+    err = float(np.max(np.abs(a.astype(np.float64) - dw_dev)) / np.max(np.abs(dw_dev)))
+    assert err <= 1e-5, err
