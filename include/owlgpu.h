@@ -765,6 +765,596 @@ int owlgpu_float64_ndarray_upsampling_spatial(
     long col_scale, long row_scale OWLGPU_DEVICE_ARGS);
 
 /* ======================================================================
+ * Complex32 / Complex64: the same entry points for Owl's complex kinds
+ * (elements are {re, im} pairs, the layout of C's float/double _Complex).
+ * They replace the complex stubs Owl binds next to each real one:
+ * conv owl_ndarray_conv.ml:55, :76 (spatial), :137, :157 (backward_input),
+ * :217, :237 (backward_kernel), :543-777 (spatial/cuboid im2col families),
+ * :2266-2515 (dilated); pool owl_ndarray_pool.ml:525-740 (complex32),
+ * :783-1022 (complex64); upsampling owl_ndarray_upsampling.ml:37, :51.
+ * Semantics are those of the complex stubs: conv products without
+ * conjugation (cblas_cgemm / cblas_zgemm, owl_ndarray_conv_stub.c);
+ * average pooling sums componentwise and divides by the count; max pooling
+ * orders by magnitude then argument (CLTF / CLT, owl_core.h:125, :133)
+ * starting from -INFINITY, i.e. (-inf, 0).  The upsampling forward, which
+ * Owl computes with `repeat`, is provided for symmetry.  `precision` is
+ * ignored: complex convolutions run on the CUDA cores in the element type.
+ * ====================================================================== */
+
+typedef struct { float re, im; } owlgpu_complex32;
+typedef struct { double re, im; } owlgpu_complex64;
+
+int owl_complex32_ndarray_conv_spatial(
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride);
+int owl_complex64_ndarray_conv_spatial(
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride);
+int owl_complex32_ndarray_conv_spatial_backward_input(
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_complex64_ndarray_conv_spatial_backward_input(
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_complex32_ndarray_conv_spatial_backward_kernel(
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_complex64_ndarray_conv_spatial_backward_kernel(
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_complex32_ndarray_conv_spatial_im2col(
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride);
+int owl_complex64_ndarray_conv_spatial_im2col(
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride);
+int owl_complex32_ndarray_conv_spatial_backward_input_im2col(
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_complex64_ndarray_conv_spatial_backward_input_im2col(
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_complex32_ndarray_conv_spatial_backward_kernel_im2col(
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_complex64_ndarray_conv_spatial_backward_kernel_im2col(
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_complex32_ndarray_conv_cuboid_im2col(
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long padding);
+int owl_complex64_ndarray_conv_cuboid_im2col(
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long padding);
+int owl_complex32_ndarray_conv_cuboid_backward_input_im2col(
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride);
+int owl_complex64_ndarray_conv_cuboid_backward_input_im2col(
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride);
+int owl_complex32_ndarray_conv_cuboid_backward_kernel_im2col(
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride);
+int owl_complex64_ndarray_conv_cuboid_backward_kernel_im2col(
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride);
+int owl_complex32_ndarray_conv_dilated_spatial_im2col(
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride);
+int owl_complex64_ndarray_conv_dilated_spatial_im2col(
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride);
+int owl_complex32_ndarray_conv_dilated_spatial_backward_input_im2col(
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_complex64_ndarray_conv_dilated_spatial_backward_input_im2col(
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_complex32_ndarray_conv_dilated_spatial_backward_kernel_im2col(
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_complex64_ndarray_conv_dilated_spatial_backward_kernel_im2col(
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_complex32_ndarray_conv_dilated_cuboid_im2col(
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long dpt_in_stride, long row_in_stride,
+    long col_in_stride, long padding);
+int owl_complex64_ndarray_conv_dilated_cuboid_im2col(
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long dpt_in_stride, long row_in_stride,
+    long col_in_stride, long padding);
+int owl_complex32_ndarray_conv_dilated_cuboid_backward_input_im2col(
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride, long dpt_in_stride,
+    long row_in_stride, long col_in_stride);
+int owl_complex64_ndarray_conv_dilated_cuboid_backward_input_im2col(
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride, long dpt_in_stride,
+    long row_in_stride, long col_in_stride);
+int owl_complex32_ndarray_conv_dilated_cuboid_backward_kernel_im2col(
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride, long dpt_in_stride,
+    long row_in_stride, long col_in_stride);
+int owl_complex64_ndarray_conv_dilated_cuboid_backward_kernel_im2col(
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride, long dpt_in_stride,
+    long row_in_stride, long col_in_stride);
+int owl_complex32_ndarray_maxpool_spatial(
+    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride);
+int owl_complex64_ndarray_maxpool_spatial(
+    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride);
+int owl_complex32_ndarray_avgpool_spatial(
+    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride);
+int owl_complex64_ndarray_avgpool_spatial(
+    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride);
+int owl_complex32_ndarray_maxpool_spatial_backward(
+    const owlgpu_complex32 *input, const owlgpu_complex32 *output_grad, owlgpu_complex32 *input_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long row_stride, long col_stride, long pad_rows, long pad_cols);
+int owl_complex64_ndarray_maxpool_spatial_backward(
+    const owlgpu_complex64 *input, const owlgpu_complex64 *output_grad, owlgpu_complex64 *input_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long row_stride, long col_stride, long pad_rows, long pad_cols);
+int owl_complex32_ndarray_avgpool_spatial_backward(
+    const owlgpu_complex32 *input, const owlgpu_complex32 *output_grad, owlgpu_complex32 *input_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long row_stride, long col_stride, long pad_rows, long pad_cols);
+int owl_complex64_ndarray_avgpool_spatial_backward(
+    const owlgpu_complex64 *input, const owlgpu_complex64 *output_grad, owlgpu_complex64 *input_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long row_stride, long col_stride, long pad_rows, long pad_cols);
+int owl_complex32_ndarray_maxpool_argmax_spatial(
+    const owlgpu_complex32 *input, owlgpu_complex32 *output, int64_t *argmax, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long row_stride,
+    long col_stride, long pad_rows, long pad_cols);
+int owl_complex64_ndarray_maxpool_argmax_spatial(
+    const owlgpu_complex64 *input, owlgpu_complex64 *output, int64_t *argmax, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long row_stride,
+    long col_stride, long pad_rows, long pad_cols);
+int owl_complex32_ndarray_maxpool_cuboid(
+    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long dpt_stride, long row_stride, long col_stride,
+    long padding);
+int owl_complex64_ndarray_maxpool_cuboid(
+    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long dpt_stride, long row_stride, long col_stride,
+    long padding);
+int owl_complex32_ndarray_avgpool_cuboid(
+    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long dpt_stride, long row_stride, long col_stride,
+    long padding);
+int owl_complex64_ndarray_avgpool_cuboid(
+    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long dpt_stride, long row_stride, long col_stride,
+    long padding);
+int owl_complex32_ndarray_maxpool_cuboid_backward(
+    const owlgpu_complex32 *input, const owlgpu_complex32 *output_grad, owlgpu_complex32 *input_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long col_stride,
+    long row_stride, long dpt_stride, long padding);
+int owl_complex64_ndarray_maxpool_cuboid_backward(
+    const owlgpu_complex64 *input, const owlgpu_complex64 *output_grad, owlgpu_complex64 *input_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long col_stride,
+    long row_stride, long dpt_stride, long padding);
+int owl_complex32_ndarray_avgpool_cuboid_backward(
+    const owlgpu_complex32 *input, const owlgpu_complex32 *output_grad, owlgpu_complex32 *input_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long col_stride,
+    long row_stride, long dpt_stride, long padding);
+int owl_complex64_ndarray_avgpool_cuboid_backward(
+    const owlgpu_complex64 *input, const owlgpu_complex64 *output_grad, owlgpu_complex64 *input_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long col_stride,
+    long row_stride, long dpt_stride, long padding);
+int owl_complex32_ndarray_upsampling_spatial_backward(
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long output_cols, long output_rows,
+    long col_scale, long row_scale);
+int owl_complex64_ndarray_upsampling_spatial_backward(
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long output_cols, long output_rows,
+    long col_scale, long row_scale);
+int owl_complex32_ndarray_upsampling_spatial(
+    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches, long input_cols,
+    long input_rows, long in_channel, long output_cols, long output_rows,
+    long col_scale, long row_scale);
+int owl_complex64_ndarray_upsampling_spatial(
+    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches, long input_cols,
+    long input_rows, long in_channel, long output_cols, long output_rows,
+    long col_scale, long row_scale);
+
+int owlgpu_complex32_ndarray_conv_spatial(
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_complex64_ndarray_conv_spatial(
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_complex32_ndarray_conv_spatial_backward_input(
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_complex64_ndarray_conv_spatial_backward_input(
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_complex32_ndarray_conv_spatial_backward_kernel(
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_complex64_ndarray_conv_spatial_backward_kernel(
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_complex32_ndarray_conv_cuboid_im2col(
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long padding OWLGPU_DEVICE_ARGS);
+int owlgpu_complex64_ndarray_conv_cuboid_im2col(
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long padding OWLGPU_DEVICE_ARGS);
+int owlgpu_complex32_ndarray_conv_cuboid_backward_input_im2col(
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_complex64_ndarray_conv_cuboid_backward_input_im2col(
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_complex32_ndarray_conv_cuboid_backward_kernel_im2col(
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_complex64_ndarray_conv_cuboid_backward_kernel_im2col(
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_complex32_ndarray_conv_dilated_spatial_im2col(
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_complex64_ndarray_conv_dilated_spatial_im2col(
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_complex32_ndarray_conv_dilated_spatial_backward_input_im2col(
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_complex64_ndarray_conv_dilated_spatial_backward_input_im2col(
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_complex32_ndarray_conv_dilated_spatial_backward_kernel_im2col(
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_complex64_ndarray_conv_dilated_spatial_backward_kernel_im2col(
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_complex32_ndarray_conv_dilated_cuboid_im2col(
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long dpt_in_stride, long row_in_stride,
+    long col_in_stride, long padding OWLGPU_DEVICE_ARGS);
+int owlgpu_complex64_ndarray_conv_dilated_cuboid_im2col(
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long dpt_in_stride, long row_in_stride,
+    long col_in_stride, long padding OWLGPU_DEVICE_ARGS);
+int owlgpu_complex32_ndarray_conv_dilated_cuboid_backward_input_im2col(
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride, long dpt_in_stride,
+    long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_complex64_ndarray_conv_dilated_cuboid_backward_input_im2col(
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride, long dpt_in_stride,
+    long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_complex32_ndarray_conv_dilated_cuboid_backward_kernel_im2col(
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride, long dpt_in_stride,
+    long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_complex64_ndarray_conv_dilated_cuboid_backward_kernel_im2col(
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride, long dpt_in_stride,
+    long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_complex32_ndarray_maxpool_spatial(
+    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_complex64_ndarray_maxpool_spatial(
+    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_complex32_ndarray_avgpool_spatial(
+    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_complex64_ndarray_avgpool_spatial(
+    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
+int owlgpu_complex32_ndarray_maxpool_spatial_backward(
+    const owlgpu_complex32 *input, const owlgpu_complex32 *output_grad, owlgpu_complex32 *input_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long row_stride, long col_stride, long pad_rows,
+    long pad_cols OWLGPU_DEVICE_ARGS);
+int owlgpu_complex64_ndarray_maxpool_spatial_backward(
+    const owlgpu_complex64 *input, const owlgpu_complex64 *output_grad, owlgpu_complex64 *input_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long row_stride, long col_stride, long pad_rows,
+    long pad_cols OWLGPU_DEVICE_ARGS);
+int owlgpu_complex32_ndarray_avgpool_spatial_backward(
+    const owlgpu_complex32 *input, const owlgpu_complex32 *output_grad, owlgpu_complex32 *input_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long row_stride, long col_stride, long pad_rows,
+    long pad_cols OWLGPU_DEVICE_ARGS);
+int owlgpu_complex64_ndarray_avgpool_spatial_backward(
+    const owlgpu_complex64 *input, const owlgpu_complex64 *output_grad, owlgpu_complex64 *input_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long row_stride, long col_stride, long pad_rows,
+    long pad_cols OWLGPU_DEVICE_ARGS);
+int owlgpu_complex32_ndarray_maxpool_argmax_spatial(
+    const owlgpu_complex32 *input, owlgpu_complex32 *output, int64_t *argmax, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long row_stride,
+    long col_stride, long pad_rows, long pad_cols OWLGPU_DEVICE_ARGS);
+int owlgpu_complex64_ndarray_maxpool_argmax_spatial(
+    const owlgpu_complex64 *input, owlgpu_complex64 *output, int64_t *argmax, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long row_stride,
+    long col_stride, long pad_rows, long pad_cols OWLGPU_DEVICE_ARGS);
+int owlgpu_complex32_ndarray_maxpool_cuboid(
+    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long dpt_stride, long row_stride, long col_stride,
+    long padding OWLGPU_DEVICE_ARGS);
+int owlgpu_complex64_ndarray_maxpool_cuboid(
+    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long dpt_stride, long row_stride, long col_stride,
+    long padding OWLGPU_DEVICE_ARGS);
+int owlgpu_complex32_ndarray_avgpool_cuboid(
+    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long dpt_stride, long row_stride, long col_stride,
+    long padding OWLGPU_DEVICE_ARGS);
+int owlgpu_complex64_ndarray_avgpool_cuboid(
+    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long dpt_stride, long row_stride, long col_stride,
+    long padding OWLGPU_DEVICE_ARGS);
+int owlgpu_complex32_ndarray_maxpool_cuboid_backward(
+    const owlgpu_complex32 *input, const owlgpu_complex32 *output_grad, owlgpu_complex32 *input_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long col_stride,
+    long row_stride, long dpt_stride, long padding OWLGPU_DEVICE_ARGS);
+int owlgpu_complex64_ndarray_maxpool_cuboid_backward(
+    const owlgpu_complex64 *input, const owlgpu_complex64 *output_grad, owlgpu_complex64 *input_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long col_stride,
+    long row_stride, long dpt_stride, long padding OWLGPU_DEVICE_ARGS);
+int owlgpu_complex32_ndarray_avgpool_cuboid_backward(
+    const owlgpu_complex32 *input, const owlgpu_complex32 *output_grad, owlgpu_complex32 *input_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long col_stride,
+    long row_stride, long dpt_stride, long padding OWLGPU_DEVICE_ARGS);
+int owlgpu_complex64_ndarray_avgpool_cuboid_backward(
+    const owlgpu_complex64 *input, const owlgpu_complex64 *output_grad, owlgpu_complex64 *input_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long col_stride,
+    long row_stride, long dpt_stride, long padding OWLGPU_DEVICE_ARGS);
+int owlgpu_complex32_ndarray_upsampling_spatial_backward(
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long output_cols, long output_rows,
+    long col_scale, long row_scale OWLGPU_DEVICE_ARGS);
+int owlgpu_complex64_ndarray_upsampling_spatial_backward(
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long output_cols, long output_rows,
+    long col_scale, long row_scale OWLGPU_DEVICE_ARGS);
+int owlgpu_complex32_ndarray_upsampling_spatial(
+    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches, long input_cols,
+    long input_rows, long in_channel, long output_cols, long output_rows,
+    long col_scale, long row_scale OWLGPU_DEVICE_ARGS);
+int owlgpu_complex64_ndarray_upsampling_spatial(
+    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches, long input_cols,
+    long input_rows, long in_channel, long output_cols, long output_rows,
+    long col_scale, long row_scale OWLGPU_DEVICE_ARGS);
+
+/* ======================================================================
  * Allocation-free entry point.  No counterpart in the reference: Owl's C
  * stubs allocate their own scratch with malloc.  This is the float32 2-D
  * conv backward_kernel (same arguments and results as

@@ -57,8 +57,10 @@ def _find_openblas():
             suf = "64_" if ilp64 else ""
             s = getattr(L, f"scipy_cblas_sgemm{suf}")
             d = getattr(L, f"scipy_cblas_dgemm{suf}")
+            c = getattr(L, f"scipy_cblas_cgemm{suf}", None)
+            z = getattr(L, f"scipy_cblas_zgemm{suf}", None)
             setter = getattr(L, f"scipy_openblas_set_num_threads{suf}", None)
-            return L, s, d, ilp64, setter, path
+            return L, s, d, c, z, ilp64, setter, path
         except (OSError, AttributeError):
             continue
     return None
@@ -71,15 +73,20 @@ def load(threads: int | None = None) -> ctypes.CDLL:
     """Build (if needed) and load liboracle.so with a BLAS registered."""
     global _oracle
     if _oracle is None:
-        if not LIB.exists() or LIB.stat().st_mtime < (HERE / "owl_oracle.c").stat().st_mtime:
+        newest = max((HERE / f).stat().st_mtime for f in ("owl_oracle.c", "oracle_impl.h"))
+        if not LIB.exists() or LIB.stat().st_mtime < newest:
             subprocess.run(["make", "-s", "-C", str(HERE), "liboracle.so"], check=True)
         L = ctypes.CDLL(str(LIB))
         L.oracle_set_blas.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        L.oracle_set_blas_complex.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         found = _find_openblas()
         if found:
-            B, s, d, ilp64, setter, path = found
+            B, s, d, c, z, ilp64, setter, path = found
             L.oracle_set_blas(ctypes.cast(s, ctypes.c_void_p), ctypes.cast(d, ctypes.c_void_p),
                               1 if ilp64 else 0)
+            if c is not None and z is not None:
+                L.oracle_set_blas_complex(ctypes.cast(c, ctypes.c_void_p),
+                                          ctypes.cast(z, ctypes.c_void_p), 1 if ilp64 else 0)
             _blas_info.update(lib=B, setter=setter, path=path, ilp64=ilp64)
         _oracle = L
     if threads is not None:

@@ -5,8 +5,10 @@
  * this code; only the tests, the smoke check and the CPU-baseline leg of the
  * benchmark load it, and only as the checker (or as the timed CPU arm).
  *
- * This header is instantiated twice by owl_oracle.c, once with T=float
- * (Owl's S module) and once with T=double (Owl's D module).  Every function
+ * This header is instantiated four times by owl_oracle.c: T=float (Owl's S
+ * module), T=double (D), T=float _Complex (C) and T=double _Complex (Z).
+ * LT(a, b) is the ordering max pooling uses: `<` for the reals, magnitude
+ * then argument for the complex kinds (CLTF / CLT, owl_core.h:125, :133).  Every function
  * restates the algorithm of the Owl C stub named in its comment:
  *   conv  : im2col followed by one GEMM per block of output pixels, the
  *           strategy of src/owl/core/owl_ndarray_conv_impl.h:296-338 (2-D),
@@ -16,8 +18,8 @@
  *           results must match bit for bit.
  */
 
-#ifndef T
-#error "instantiate with T and SFX defined"
+#if !defined(T) || !defined(SFX) || !defined(LT)
+#error "instantiate with T, SFX and LT defined"
 #endif
 
 #define CAT_(a, b) a##b
@@ -180,7 +182,7 @@ static void FN(pool_fwd_)(const pgeom_t *g, const T *x, T *y, int64_t *argmax, i
                     long off = ((a * g->IR + b) * g->ID + c) * chs + l;
                     T t = xb[off];
                     if (mode == 0) {
-                      if (acc < t) { acc = t; midx = xbase + off; }
+                      if (LT(acc, t)) { acc = t; midx = xbase + off; }
                     } else {
                       acc += t;
                     }
@@ -221,7 +223,7 @@ static void FN(pool_bwd_)(const pgeom_t *g, const T *x, const T *dy, T *dx, int 
                     cnt++;
                     if (mode == 0) {
                       T t = x[off];
-                      if (acc < t) { acc = t; midx = off; }
+                      if (LT(acc, t)) { acc = t; midx = off; }
                     }
                   }
             if (mode == 0) {

@@ -20,6 +20,7 @@
  * use of cblas_?gemm; without one a plain triple loop is used.
  */
 
+#include <complex.h>
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -48,8 +49,22 @@ typedef void (*sgemm64_t)(int, int, int, int64_t, int64_t, int64_t, float, const
 typedef void (*dgemm64_t)(int, int, int, int64_t, int64_t, int64_t, double, const double *,
                           int64_t, const double *, int64_t, double, double *, int64_t);
 
-static void *g_sgemm = 0, *g_dgemm = 0;
-static int g_ilp64 = 0;
+/* cblas_cgemm / cblas_zgemm: alpha and beta by pointer, matrices as void *. */
+typedef void (*cgemm32_t)(int, int, int, int, int, int, const void *, const void *, int,
+                          const void *, int, const void *, void *, int);
+typedef void (*cgemm64_t)(int, int, int, int64_t, int64_t, int64_t, const void *, const void *,
+                          int64_t, const void *, int64_t, const void *, void *, int64_t);
+
+static void *g_sgemm = 0, *g_dgemm = 0, *g_cgemm = 0, *g_zgemm = 0;
+static int g_ilp64 = 0, g_cilp64 = 0;
+
+/* Register cblas_cgemm / cblas_zgemm for the complex kinds (Owl's
+ * owl_ndarray_conv_stub.c instantiates the complex stubs with them). */
+void oracle_set_blas_complex(void *cgemm, void *zgemm, int ilp64) {
+  g_cgemm = cgemm;
+  g_zgemm = zgemm;
+  g_cilp64 = ilp64;
+}
 
 /* Register cblas_sgemm / cblas_dgemm (LP64 when ilp64 == 0, else 64-bit
  * integer interface).  Passing nulls reverts to the built-in loops. */
@@ -105,8 +120,41 @@ static void gemm_f64(int transA, int transB, long m, long n, long k, const doubl
   LOOP_GEMM(double);
 }
 
-/* ---- instantiate the algorithms for float and double ------------------- */
+typedef float _Complex cf32;
+typedef double _Complex cf64;
 
+#define CGEMM_VIA(G, CT)                                                                      \
+  do {                                                                                        \
+    const CT one = 1, bet = beta;                                                             \
+    if (g_cilp64)                                                                             \
+      ((cgemm64_t)(G))(RowMajor, transA ? Trans : NoTrans, transB ? Trans : NoTrans, m, n, k, \
+                       &one, A, lda, B, ldb, &bet, C, ldc);                                   \
+    else                                                                                      \
+      ((cgemm32_t)(G))(RowMajor, transA ? Trans : NoTrans, transB ? Trans : NoTrans, (int)m,  \
+                       (int)n, (int)k, &one, A, (int)lda, B, (int)ldb, &bet, C, (int)ldc);    \
+  } while (0)
+
+static void gemm_c32(int transA, int transB, long m, long n, long k, const cf32 *A, long lda,
+                     const cf32 *B, long ldb, cf32 beta, cf32 *C, long ldc) {
+  if (g_cgemm) {
+    CGEMM_VIA(g_cgemm, cf32);
+    return;
+  }
+  LOOP_GEMM(cf32);
+}
+
+static void gemm_c64(int transA, int transB, long m, long n, long k, const cf64 *A, long lda,
+                     const cf64 *B, long ldb, cf64 beta, cf64 *C, long ldc) {
+  if (g_zgemm) {
+    CGEMM_VIA(g_zgemm, cf64);
+    return;
+  }
+  LOOP_GEMM(cf64);
+}
+
+/* ---- instantiate the algorithms for the four element kinds --------------- */
+
+#define LT(a, b) ((a) < (b))
 #define T float
 #define SFX f32
 #include "oracle_impl.h"
@@ -118,6 +166,27 @@ static void gemm_f64(int transA, int transB, long m, long n, long k, const doubl
 #include "oracle_impl.h"
 #undef T
 #undef SFX
+#undef LT
+
+/* Owl's complex max pooling starts from -INFINITY, the complex (-inf, 0),
+ * whose magnitude is infinite, and compares with CLTF / CLT; the same
+ * expressions here (owl_core.h:125, :133). */
+#define LT(a, b) \
+  ((cabsf(a) < cabsf(b)) || ((cabsf(a) == cabsf(b)) && (cargf(a) < cargf(b))))
+#define T cf32
+#define SFX c32
+#include "oracle_impl.h"
+#undef T
+#undef SFX
+#undef LT
+
+#define LT(a, b) ((cabs(a) < cabs(b)) || ((cabs(a) == cabs(b)) && (carg(a) < carg(b))))
+#define T cf64
+#define SFX c64
+#include "oracle_impl.h"
+#undef T
+#undef SFX
+#undef LT
 
 /* ---- padding rules ----------------------------------------------------- */
 
@@ -267,6 +336,8 @@ static geom_t geom3(long B, long IC, long IR, long ID, long Ci, long KC, long KR
 
 DEF_CONV_ALL(float, float32, f32)
 DEF_CONV_ALL(double, float64, f64)
+DEF_CONV_ALL(cf32, complex32, c32)
+DEF_CONV_ALL(cf64, complex64, c64)
 
 /* ---- pool entry points (Owl stub argument order) ----------------------- */
 
@@ -325,6 +396,10 @@ DEF_POOL_ALL(float, float32, f32, maxpool, 0)
 DEF_POOL_ALL(float, float32, f32, avgpool, 1)
 DEF_POOL_ALL(double, float64, f64, maxpool, 0)
 DEF_POOL_ALL(double, float64, f64, avgpool, 1)
+DEF_POOL_ALL(cf32, complex32, c32, maxpool, 0)
+DEF_POOL_ALL(cf32, complex32, c32, avgpool, 1)
+DEF_POOL_ALL(cf64, complex64, c64, maxpool, 0)
+DEF_POOL_ALL(cf64, complex64, c64, avgpool, 1)
 
 /* owl_ndarray_pool_impl.h:459-465: max value plus int64 flat argmax */
 #define DEF_ARG(TY, NAME, SFX2)                                                                 \
@@ -339,6 +414,8 @@ DEF_POOL_ALL(double, float64, f64, avgpool, 1)
   }
 DEF_ARG(float, float32, f32)
 DEF_ARG(double, float64, f64)
+DEF_ARG(cf32, complex32, c32)
+DEF_ARG(cf64, complex64, c64)
 
 /* ---- nearest-neighbour 2-D upsampling ----------------------------------
  * Backward: owl_ndarray_upsampling_impl.h:9-58 -- zero dX, then for every
@@ -376,3 +453,5 @@ DEF_ARG(double, float64, f64)
   }
 DEF_UP(float, float32)
 DEF_UP(double, float64)
+DEF_UP(cf32, complex32)
+DEF_UP(cf64, complex64)

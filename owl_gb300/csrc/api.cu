@@ -386,8 +386,22 @@ static int host_call(std::vector<Buf> bufs, int64_t batch, int chunks, F body,
   return rc;
 }
 
+// Element kind of each C-ABI element type.
 template <typename T>
-static Dtype dtype_of() { return sizeof(T) == 4 ? F32 : F64; }
+struct ElemKind;
+template <>
+struct ElemKind<float> { static constexpr Dtype v = F32; };
+template <>
+struct ElemKind<double> { static constexpr Dtype v = F64; };
+template <>
+struct ElemKind<owlgpu_complex32> { static constexpr Dtype v = C32; };
+template <>
+struct ElemKind<owlgpu_complex64> { static constexpr Dtype v = C64; };
+static_assert(sizeof(owlgpu_complex32) == sizeof(c32) && sizeof(owlgpu_complex64) == sizeof(c64),
+              "complex layouts");
+
+template <typename T>
+static Dtype dtype_of() { return ElemKind<T>::v; }
 
 // Conv op kinds.
 enum ConvOp { OP_FWD, OP_BWDI, OP_BWDK };
@@ -414,7 +428,7 @@ static int conv_host(ConvOp op, const ConvGeom &g, const void *a, const void *b,
   // in chunk order at the end (deterministic), so the kernels run while the
   // later chunks are still being copied in.
   const bool bwdk = op == OP_BWDK;
-  const bool chunk = !bwdk || sizeof(T) == 4;
+  const bool chunk = !bwdk || dtype_of<T>() == F32;
   std::vector<Buf> bufs;
   if (op == OP_FWD)
     bufs = {{a, xb, true, false, chunk}, {b, wb, true, false, false}, {c, yb, false, true, chunk}};
@@ -661,6 +675,8 @@ int owlgpu_trim(void) {
 
 CONV2D_ALL(float32, float)
 CONV2D_ALL(float64, double)
+CONV2D_ALL(complex32, owlgpu_complex32)
+CONV2D_ALL(complex64, owlgpu_complex64)
 
 // ---- 3-D conv (cuboid im2col family and dilated cuboid) ---------------------
 
@@ -776,6 +792,8 @@ CONV2D_ALL(float64, double)
 
 CONV3D_ALL(float32, float)
 CONV3D_ALL(float64, double)
+CONV3D_ALL(complex32, owlgpu_complex32)
+CONV3D_ALL(complex64, owlgpu_complex64)
 
 // ---- pooling -----------------------------------------------------------------
 
@@ -950,6 +968,8 @@ CONV3D_ALL(float64, double)
 
 POOL_ALL(float32, float)
 POOL_ALL(float64, double)
+POOL_ALL(complex32, owlgpu_complex32)
+POOL_ALL(complex64, owlgpu_complex64)
 
 // Upsampling: the backward keeps the stub's argument order (input_grad
 // written first, then output_grad); the forward, which Owl computes with
@@ -998,5 +1018,7 @@ POOL_ALL(float64, double)
 
 UPSAMPLE(float32, float)
 UPSAMPLE(float64, double)
+UPSAMPLE(complex32, owlgpu_complex32)
+UPSAMPLE(complex64, owlgpu_complex64)
 
 }  // extern "C"

@@ -14,7 +14,69 @@
 
 namespace owlgpu {
 
-enum Dtype { F32 = 0, F64 = 1 };
+enum Dtype { F32 = 0, F64 = 1, C32 = 2, C64 = 3 };
+
+// Complex elements of Owl's Complex32 / Complex64 arrays: two reals, real
+// part first (the layout of C's `float _Complex` / `double _Complex`).
+// Arithmetic follows Owl's complex stubs: products of the plain formula
+// (cblas_cgemm / cblas_zgemm, no conjugation anywhere), sums componentwise,
+// division by a count componentwise (C's complex / real), and ordering by
+// magnitude then argument (CLTF / CLT, src/owl/core/owl_core.h:125, :133).
+// Its own namespace, so that `fma` and the operators reach it only by
+// argument-dependent lookup and never hide the real overloads.
+namespace cx {
+template <typename R>
+struct __align__(2 * sizeof(R)) cplx {
+  R re, im;
+  cplx() = default;
+  __host__ __device__ explicit constexpr cplx(R r) : re(r), im(0) {}
+  __host__ __device__ constexpr cplx(R r, R i) : re(r), im(i) {}
+  __host__ __device__ cplx &operator+=(const cplx &b) {
+    re += b.re;
+    im += b.im;
+    return *this;
+  }
+};
+template <typename R>
+__host__ __device__ inline cplx<R> operator+(cplx<R> a, const cplx<R> &b) {
+  a += b;
+  return a;
+}
+// c + a*b, the real part as ((c.re + a.re*b.re) - a.im*b.im) with each step
+// fused, the imaginary part likewise.
+template <typename R>
+__device__ inline cplx<R> fma(const cplx<R> &a, const cplx<R> &b, const cplx<R> &c) {
+  cplx<R> r;
+  r.re = ::fma(-a.im, b.im, ::fma(a.re, b.re, c.re));
+  r.im = ::fma(a.im, b.re, ::fma(a.re, b.im, c.im));
+  return r;
+}
+__device__ inline float mag(const cplx<float> &a) { return hypotf(a.re, a.im); }
+__device__ inline double mag(const cplx<double> &a) { return hypot(a.re, a.im); }
+__device__ inline float arg(const cplx<float> &a) { return atan2f(a.im, a.re); }
+__device__ inline double arg(const cplx<double> &a) { return atan2(a.im, a.re); }
+template <typename R>
+__device__ inline bool operator<(const cplx<R> &a, const cplx<R> &b) {
+  const R ma = mag(a), mb = mag(b);
+  return ma < mb || (ma == mb && arg(a) < arg(b));
+}
+}  // namespace cx
+
+using c32 = cx::cplx<float>;
+using c64 = cx::cplx<double>;
+
+// x / n for a window count n: the element type's division, componentwise for
+// complex elements.
+template <typename T>
+__device__ __forceinline__ T div_count(const T &x, int n) { return x / (T)n; }
+template <>
+__device__ __forceinline__ c32 div_count<c32>(const c32 &x, int n) {
+  return c32(x.re / (float)n, x.im / (float)n);
+}
+template <>
+__device__ __forceinline__ c64 div_count<c64>(const c64 &x, int n) {
+  return c64(x.re / (double)n, x.im / (double)n);
+}
 
 // Convolution geometry.  Leading pads are the values Owl's C stubs derive
 // (owl_ndarray_conv_impl.h:288-294 forward, :502-505 backward); dilation is

@@ -1,6 +1,6 @@
-// conv_simt.cu -- CUDA-core implicit-GEMM convolutions (float32 "plain" and
-// float64), forward / backward-input / backward-kernel, 2-D, 3-D, strided,
-// dilated.  No im2col matrix is ever materialised: every GEMM operand element
+// conv_simt.cu -- CUDA-core implicit-GEMM convolutions (float32 "plain",
+// float64, complex32 and complex64), forward / backward-input /
+// backward-kernel, 2-D, 3-D, strided, dilated.  No im2col matrix is ever materialised: every GEMM operand element
 // is gathered from the NHWC-style Owl array while the tile is staged into
 // shared memory.
 //
@@ -14,6 +14,8 @@
 //                reduction over output pixels, split across CTAs and summed
 //                by a second kernel in a fixed order (deterministic).
 #include "common.cuh"
+
+#include <type_traits>
 
 namespace owlgpu {
 namespace {
@@ -331,7 +333,7 @@ int launch_cfg(const Dev &d, const T *A, const T *B, T *C, int splits, int64_t k
 template <typename T, int MODE>
 int launch_any(const Dev &d, const T *A, const T *B, T *C, int splits, int64_t kps,
                cudaStream_t s) {
-  if (sizeof(T) == 4) {
+  if constexpr (sizeof(T) == 4) {
     if (d.N > 64) return launch_cfg<T, MODE, 128, 128, 8, 8, 8>(d, A, B, C, splits, kps, s);
     if (d.N > 32) return launch_cfg<T, MODE, 128, 64, 8, 8, 4>(d, A, B, C, splits, kps, s);
     return launch_cfg<T, MODE, 128, 32, 8, 4, 4>(d, A, B, C, splits, kps, s);
@@ -444,22 +446,42 @@ int simt_conv_bwd_kernel_f32_into(const ConvGeom &g, const float *x, float *dw,
   return bwdk_f32_into(g, x, dw, dy, ws, ws_elems, s);
 }
 
+// Element type of each Dtype: float, double, and the complex pairs (whose
+// tiles are those of double: 8- and 16-byte elements).
+template <typename F>
+static int by_dtype(Dtype dt, F f) {
+  switch (dt) {
+    case F32: return f((float *)nullptr);
+    case F64: return f((double *)nullptr);
+    case C32: return f((c32 *)nullptr);
+    case C64: return f((c64 *)nullptr);
+  }
+  set_error("unknown element type");
+  return kErrInvalid;
+}
+
 int simt_conv_fwd(Dtype dt, const ConvGeom &g, const void *x, const void *w, void *y,
                   cudaStream_t s) {
-  return dt == F32 ? fwd_t<float>(g, (const float *)x, (const float *)w, (float *)y, s)
-                   : fwd_t<double>(g, (const double *)x, (const double *)w, (double *)y, s);
+  return by_dtype(dt, [&](auto *tag) {
+    using T = std::remove_pointer_t<decltype(tag)>;
+    return fwd_t<T>(g, (const T *)x, (const T *)w, (T *)y, s);
+  });
 }
 
 int simt_conv_bwd_input(Dtype dt, const ConvGeom &g, void *dx, const void *w, const void *dy,
                         cudaStream_t s) {
-  return dt == F32 ? bwdi_t<float>(g, (float *)dx, (const float *)w, (const float *)dy, s)
-                   : bwdi_t<double>(g, (double *)dx, (const double *)w, (const double *)dy, s);
+  return by_dtype(dt, [&](auto *tag) {
+    using T = std::remove_pointer_t<decltype(tag)>;
+    return bwdi_t<T>(g, (T *)dx, (const T *)w, (const T *)dy, s);
+  });
 }
 
 int simt_conv_bwd_kernel(Dtype dt, const ConvGeom &g, const void *x, void *dw, const void *dy,
                          cudaStream_t s) {
-  return dt == F32 ? bwdk_t<float>(g, (const float *)x, (float *)dw, (const float *)dy, s)
-                   : bwdk_t<double>(g, (const double *)x, (double *)dw, (const double *)dy, s);
+  return by_dtype(dt, [&](auto *tag) {
+    using T = std::remove_pointer_t<decltype(tag)>;
+    return bwdk_t<T>(g, (const T *)x, (T *)dw, (const T *)dy, s);
+  });
 }
 
 }  // namespace owlgpu

@@ -1,5 +1,5 @@
 // pool.cu -- max / average pooling, forward and backward, 2-D and 3-D,
-// float32 and float64, with Owl's exact semantics
+// float32, float64, complex32 and complex64, with Owl's exact semantics
 // (src/owl/core/owl_ndarray_pool_impl.h):
 //   * window scan order: cols outer, rows, dpts inner; out-of-range taps
 //     skipped (:60-77, :282-300);
@@ -38,6 +38,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <type_traits>
 
 namespace owlgpu {
 namespace {
@@ -96,6 +97,12 @@ template <>
 struct Vec<double, 2> { using type = double2; };
 template <>
 struct Vec<double, 1> { using type = double; };
+template <>
+struct Vec<c32, 2> { using type = float4; };
+template <>
+struct Vec<c32, 1> { using type = float2; };
+template <>
+struct Vec<c64, 1> { using type = double2; };
 
 template <typename T, int V>
 __device__ __forceinline__ void load_vec(const T *p, T (&v)[V]) {
@@ -240,7 +247,7 @@ __global__ void __launch_bounds__(256) pool_fwd_kernel(PG g, const T *__restrict
     } else {
       window_sum<T, V, kChunk>(x, xbase + cv * V, g, w, out);
 #pragma unroll
-      for (int i = 0; i < V; ++i) out[i] = out[i] / (T)w.n;
+      for (int i = 0; i < V; ++i) out[i] = div_count(out[i], w.n);
     }
     store_vec<T, V>(y + p * g.Ch + cv * V, out);
   }
@@ -307,7 +314,7 @@ __global__ void __launch_bounds__(256) pool_bwd_cell_kernel(PG g, const T *__res
       for (int i = 0; i < V; ++i) degen |= bt[i] < 0;
     } else {
 #pragma unroll
-      for (int i = 0; i < V; ++i) gv[i] = gv[i] / (T)w.n;
+      for (int i = 0; i < V; ++i) gv[i] = div_count(gv[i], w.n);
     }
     int alo, ahi, blo, bhi, clo, chi;
     cell_range(oc, g.sc, g.pc, g.OC, g.IC, alo, ahi);
@@ -391,7 +398,7 @@ __global__ void __launch_bounds__(256) pool_fwd_fixed_kernel(PG g, OutDecode dec
 #pragma unroll
         for (int i = 0; i < V; ++i) out[i] += v[u][i];
 #pragma unroll
-      for (int i = 0; i < V; ++i) out[i] = out[i] / (T)N;
+      for (int i = 0; i < V; ++i) out[i] = div_count(out[i], N);
     }
     store_vec<T, V>(y + p * g.Ch + cv * V, out);
   }
@@ -447,7 +454,7 @@ __global__ void __launch_bounds__(256) pool_bwd_tile_kernel(PG g, OutDecode dec,
       for (int i = 0; i < V; ++i) degen |= bt[i] < 0;
     } else {
 #pragma unroll
-      for (int i = 0; i < V; ++i) gv[i] = gv[i] / (T)N;
+      for (int i = 0; i < V; ++i) gv[i] = div_count(gv[i], N);
     }
 #pragma unroll
     for (int a = 0; a < KC; ++a)
@@ -519,7 +526,7 @@ __global__ void __launch_bounds__(256) pool_bwd_gather_kernel(PG g, const T *__r
                          gv);
           if (MODE == POOL_AVG) {
 #pragma unroll
-            for (int i = 0; i < V; ++i) acc[i] += gv[i] / (T)w.n;
+            for (int i = 0; i < V; ++i) acc[i] += div_count(gv[i], w.n);
           } else {
             T best[V];
             int bt[V];
@@ -597,11 +604,16 @@ int grid_for(int64_t work) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(blocks, 152 * 16));
 }
 
+// Elements per 16-byte vector: 4 floats, 2 doubles or complex32, 1 complex64.
+template <typename T>
+constexpr int kWide = (int)(16 / sizeof(T));
+
 template <typename T>
 int vec_width(int64_t ch, const void *a, const void *b, const void *c) {
   auto al = [](const void *p, int bytes) { return ((uintptr_t)p % bytes) == 0; };
-  if (sizeof(T) == 4 && ch % 4 == 0 && al(a, 16) && al(b, 16) && al(c, 16)) return 4;
-  if (ch % 2 == 0 && al(a, 2 * sizeof(T)) && al(b, 2 * sizeof(T)) && al(c, 2 * sizeof(T)))
+  if (kWide<T> >= 4 && ch % 4 == 0 && al(a, 16) && al(b, 16) && al(c, 16)) return 4;
+  if (kWide<T> >= 2 && ch % 2 == 0 && al(a, 2 * sizeof(T)) && al(b, 2 * sizeof(T)) &&
+      al(c, 2 * sizeof(T)))
     return 2;
   return 1;
 }
@@ -650,8 +662,6 @@ bool small_output(const PG &g, int V) {
 
 // Fixed-window kernels exist for the widest vector of each type (16 bytes)
 // and the common window shapes 2x2, 3x3 and 2x2x2.
-template <typename T>
-constexpr int kWide = sizeof(T) == 4 ? 4 : 2;
 
 template <typename T, int V>
 int fwd_launch(const PG &g, PoolMode mode, const T *x, T *y, int64_t *arg, cudaStream_t s) {
@@ -680,7 +690,9 @@ int fwd_t(const PoolGeom &pg, PoolMode mode, const T *x, T *y, int64_t *arg, cud
   if (pg.y_elems() == 0) return kOk;
   int v = vec_width<T>(g.Ch, x, y, y);
   if (v == 4) return fwd_launch<T, kWide<T>>(g, mode, x, y, arg, s);
-  if (v == 2) return fwd_launch<T, 2>(g, mode, x, y, arg, s);
+  if constexpr (kWide<T> >= 2) {
+    if (v == 2) return fwd_launch<T, 2>(g, mode, x, y, arg, s);
+  }
   return fwd_launch<T, 1>(g, mode, x, y, arg, s);
 }
 
@@ -750,7 +762,7 @@ int bwd_t(const PoolGeom &pg, PoolMode mode, const T *x, const T *dy, T *dx, cud
   int v = vec_width<T>(g.Ch, x ? (const void *)x : (const void *)dy, dy, dx);
   int rc;
   if (v == 4) rc = bwd_launch<T, kWide<T>>(g, mode, x, dy, dx, ticket, s);
-  else if (v == 2) rc = bwd_launch<T, 2>(g, mode, x, dy, dx, ticket, s);
+  else if (v == 2) rc = bwd_launch<T, kWide<T> >= 2 ? 2 : 1>(g, mode, x, dy, dx, ticket, s);
   else rc = bwd_launch<T, 1>(g, mode, x, dy, dx, ticket, s);
   if (rc == kOk && mode == POOL_MAX) {
     const int force = has_empty_window(g) ? 1 : 0;
@@ -774,17 +786,32 @@ int bwd_t(const PoolGeom &pg, PoolMode mode, const T *x, const T *dy, T *dx, cud
 
 }  // namespace
 
+template <typename F>
+static int by_dtype(Dtype dt, F f) {
+  switch (dt) {
+    case F32: return f((float *)nullptr);
+    case F64: return f((double *)nullptr);
+    case C32: return f((c32 *)nullptr);
+    case C64: return f((c64 *)nullptr);
+  }
+  set_error("unknown element type");
+  return kErrInvalid;
+}
+
 int pool_fwd(Dtype dt, PoolMode mode, const PoolGeom &g, const void *x, void *y,
              int64_t *argmax, cudaStream_t s) {
-  return dt == F32 ? fwd_t<float>(g, mode, (const float *)x, (float *)y, argmax, s)
-                   : fwd_t<double>(g, mode, (const double *)x, (double *)y, argmax, s);
+  return by_dtype(dt, [&](auto *tag) {
+    using T = std::remove_pointer_t<decltype(tag)>;
+    return fwd_t<T>(g, mode, (const T *)x, (T *)y, argmax, s);
+  });
 }
 
 int pool_bwd(Dtype dt, PoolMode mode, const PoolGeom &g, const void *x, const void *dy,
              void *dx, cudaStream_t s) {
-  return dt == F32
-             ? bwd_t<float>(g, mode, (const float *)x, (const float *)dy, (float *)dx, s)
-             : bwd_t<double>(g, mode, (const double *)x, (const double *)dy, (double *)dx, s);
+  return by_dtype(dt, [&](auto *tag) {
+    using T = std::remove_pointer_t<decltype(tag)>;
+    return bwd_t<T>(g, mode, (const T *)x, (const T *)dy, (T *)dx, s);
+  });
 }
 
 }  // namespace owlgpu

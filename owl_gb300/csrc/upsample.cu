@@ -1,5 +1,6 @@
 // upsample.cu -- nearest-neighbour 2-D upsampling (Owl's upsampling2d) and
-// its backward, float32 and float64.
+// its backward, float32 and float64 (complex32 / complex64 as twice the
+// channels of their real parts).
 //
 // Forward: Owl computes upsampling2d as `repeat x [|1; sc; sr; 1|]`
 // (owl_dense_ndarray_generic.ml:8223-8233):
@@ -129,6 +130,13 @@ int launch_up(bool fwd, const UpGeom &g, const void *x, void *y, int nv, cudaStr
 // x: the array read, y: the array written (forward: input -> output;
 // backward: dy -> dx).
 int run_up(Dtype dt, bool fwd, const UpGeom &g, const void *x, void *y, cudaStream_t s) {
+  // A complex element is two reals that are copied and summed independently:
+  // the same pass over twice the channels, in the same order.
+  if (dt == C32 || dt == C64) {
+    UpGeom h = g;
+    h.Ch *= 2;
+    return run_up(dt == C32 ? F32 : F64, fwd, h, x, y, s);
+  }
   const int64_t lim = 1LL << 31;
   if (std::max(g.OR, g.IR) * g.Ch >= lim || std::max(g.OC, g.OR) >= lim ||
       g.IC * g.sc >= lim || g.IR * g.sr >= lim) {

@@ -103,12 +103,20 @@ def _pad_typ(padding) -> int:
 # ---- stub name mapping -------------------------------------------------------
 
 def _kind(a) -> str:
+    """Owl's kind name of an array's element type: float32 / float64 (S, D)
+    and complex32 / complex64 (C, Z), the latter numpy's / torch's complex64
+    and complex128."""
     dt = str(getattr(a, "dtype", ""))
     if "float32" in dt:
         return "float32"
     if "float64" in dt:
         return "float64"
-    raise InvalidArgument(f"unsupported element kind {dt} (float32 and float64 only)")
+    if "complex64" in dt:
+        return "complex32"
+    if "complex128" in dt:
+        return "complex64"
+    raise InvalidArgument(f"unsupported element kind {dt} (float32, float64, complex64 and "
+                          "complex128 only)")
 
 
 class Backend:
