@@ -1355,6 +1355,308 @@ int owlgpu_complex64_ndarray_upsampling_spatial(
     long col_scale, long row_scale OWLGPU_DEVICE_ARGS);
 
 /* ======================================================================
+ * MEC and naive spellings.  Owl binds its memory-efficient (MEC) and naive
+ * CPU conv algorithms as separate stubs with the same arguments as the
+ * GEBP / im2col ones (owl_ndarray_conv.ml:856-1346 MEC, :1424-1914 naive;
+ * owl_ndarray_conv_impl.h:1570-3086); they compute the same functions, and
+ * Owl's unit_conv_mec_naive.ml runs its conv2d / conv3d suites on them.
+ * These host drop-ins are aliases of the entry points above:
+ *   conv_spatial[_backward_input|_backward_kernel]_{mec,naive}
+ *     = conv_spatial[_backward_input|_backward_kernel]
+ *   conv_cuboid[_backward_input|_backward_kernel]_{mec,naive}
+ *     = conv_cuboid[_backward_input|_backward_kernel]_im2col
+ * ====================================================================== */
+
+int owl_float32_ndarray_conv_spatial_mec(
+    const float *input, const float *kernel, float *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride);
+int owl_float32_ndarray_conv_spatial_backward_input_mec(
+    float *input_grad, const float *kernel, const float *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_float32_ndarray_conv_spatial_backward_kernel_mec(
+    const float *input, float *kernel_grad, const float *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_float32_ndarray_conv_cuboid_mec(
+    const float *input, const float *kernel, float *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long padding);
+int owl_float32_ndarray_conv_cuboid_backward_input_mec(
+    float *input_grad, const float *kernel, const float *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride);
+int owl_float32_ndarray_conv_cuboid_backward_kernel_mec(
+    const float *input, float *kernel_grad, const float *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride);
+int owl_float64_ndarray_conv_spatial_mec(
+    const double *input, const double *kernel, double *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride);
+int owl_float64_ndarray_conv_spatial_backward_input_mec(
+    double *input_grad, const double *kernel, const double *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_float64_ndarray_conv_spatial_backward_kernel_mec(
+    const double *input, double *kernel_grad, const double *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_float64_ndarray_conv_cuboid_mec(
+    const double *input, const double *kernel, double *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long padding);
+int owl_float64_ndarray_conv_cuboid_backward_input_mec(
+    double *input_grad, const double *kernel, const double *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride);
+int owl_float64_ndarray_conv_cuboid_backward_kernel_mec(
+    const double *input, double *kernel_grad, const double *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride);
+int owl_complex32_ndarray_conv_spatial_mec(
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride);
+int owl_complex32_ndarray_conv_spatial_backward_input_mec(
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_complex32_ndarray_conv_spatial_backward_kernel_mec(
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_complex32_ndarray_conv_cuboid_mec(
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long padding);
+int owl_complex32_ndarray_conv_cuboid_backward_input_mec(
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride);
+int owl_complex32_ndarray_conv_cuboid_backward_kernel_mec(
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride);
+int owl_complex64_ndarray_conv_spatial_mec(
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride);
+int owl_complex64_ndarray_conv_spatial_backward_input_mec(
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_complex64_ndarray_conv_spatial_backward_kernel_mec(
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_complex64_ndarray_conv_cuboid_mec(
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long padding);
+int owl_complex64_ndarray_conv_cuboid_backward_input_mec(
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride);
+int owl_complex64_ndarray_conv_cuboid_backward_kernel_mec(
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride);
+int owl_float32_ndarray_conv_spatial_naive(
+    const float *input, const float *kernel, float *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride);
+int owl_float32_ndarray_conv_spatial_backward_input_naive(
+    float *input_grad, const float *kernel, const float *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_float32_ndarray_conv_spatial_backward_kernel_naive(
+    const float *input, float *kernel_grad, const float *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_float32_ndarray_conv_cuboid_naive(
+    const float *input, const float *kernel, float *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long padding);
+int owl_float32_ndarray_conv_cuboid_backward_input_naive(
+    float *input_grad, const float *kernel, const float *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride);
+int owl_float32_ndarray_conv_cuboid_backward_kernel_naive(
+    const float *input, float *kernel_grad, const float *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride);
+int owl_float64_ndarray_conv_spatial_naive(
+    const double *input, const double *kernel, double *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride);
+int owl_float64_ndarray_conv_spatial_backward_input_naive(
+    double *input_grad, const double *kernel, const double *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_float64_ndarray_conv_spatial_backward_kernel_naive(
+    const double *input, double *kernel_grad, const double *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_float64_ndarray_conv_cuboid_naive(
+    const double *input, const double *kernel, double *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long padding);
+int owl_float64_ndarray_conv_cuboid_backward_input_naive(
+    double *input_grad, const double *kernel, const double *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride);
+int owl_float64_ndarray_conv_cuboid_backward_kernel_naive(
+    const double *input, double *kernel_grad, const double *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride);
+int owl_complex32_ndarray_conv_spatial_naive(
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride);
+int owl_complex32_ndarray_conv_spatial_backward_input_naive(
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_complex32_ndarray_conv_spatial_backward_kernel_naive(
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_complex32_ndarray_conv_cuboid_naive(
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long padding);
+int owl_complex32_ndarray_conv_cuboid_backward_input_naive(
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride);
+int owl_complex32_ndarray_conv_cuboid_backward_kernel_naive(
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride);
+int owl_complex64_ndarray_conv_spatial_naive(
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride);
+int owl_complex64_ndarray_conv_spatial_backward_input_naive(
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_complex64_ndarray_conv_spatial_backward_kernel_naive(
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long out_channel, long row_stride, long col_stride, long row_in_stride,
+    long col_in_stride);
+int owl_complex64_ndarray_conv_cuboid_naive(
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long padding);
+int owl_complex64_ndarray_conv_cuboid_backward_input_naive(
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride);
+int owl_complex64_ndarray_conv_cuboid_backward_kernel_naive(
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long input_dpts,
+    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
+    long output_cols, long output_rows, long output_dpts, long out_channel,
+    long dpt_stride, long row_stride, long col_stride);
+
+/* ======================================================================
  * Allocation-free entry point.  No counterpart in the reference: Owl's C
  * stubs allocate their own scratch with malloc.  This is the float32 2-D
  * conv backward_kernel (same arguments and results as

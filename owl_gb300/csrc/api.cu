@@ -795,6 +795,74 @@ CONV3D_ALL(float64, double)
 CONV3D_ALL(complex32, owlgpu_complex32)
 CONV3D_ALL(complex64, owlgpu_complex64)
 
+// ---- MEC and naive spellings of the conv stubs -------------------------------
+// Owl's memory-efficient (MEC) and naive CPU algorithms compute the same
+// functions as its GEBP / im2col ones, with the same stub arguments
+// (owl_ndarray_conv_impl.h:1570-3086; Owl's unit_conv_mec_naive.ml runs its
+// conv2d and conv3d test suites on them).  Host drop-in aliases of the same
+// GPU implementation.
+
+#define SP2_LONGS                                                                              \
+  long batches, long input_cols, long input_rows, long in_channel, long kernel_cols,           \
+      long kernel_rows, long output_cols, long output_rows, long out_channel, long row_stride, \
+      long col_stride
+#define SP2_VALS                                                                               \
+  batches, input_cols, input_rows, in_channel, kernel_cols, kernel_rows, output_cols,          \
+      output_rows, out_channel, row_stride, col_stride
+#define CU3_LONGS                                                                              \
+  long batches, long input_cols, long input_rows, long input_dpts, long in_channel,            \
+      long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols, long output_rows, \
+      long output_dpts, long out_channel, long dpt_stride, long row_stride, long col_stride
+#define CU3_VALS                                                                               \
+  batches, input_cols, input_rows, input_dpts, in_channel, kernel_cols, kernel_rows,           \
+      kernel_dpts, output_cols, output_rows, output_dpts, out_channel, dpt_stride, row_stride, \
+      col_stride
+
+#define CONV_SPELLINGS(KIND, T, SFX)                                                           \
+  int owl_##KIND##_ndarray_conv_spatial_##SFX(const T *input, const T *kernel, T *output,     \
+                                              SP2_LONGS, long padding, long row_in_stride,    \
+                                              long col_in_stride) {                           \
+    return owl_##KIND##_ndarray_conv_spatial(input, kernel, output, SP2_VALS, padding,        \
+                                             row_in_stride, col_in_stride);                   \
+  }                                                                                           \
+  int owl_##KIND##_ndarray_conv_spatial_backward_input_##SFX(                                 \
+      T *input_grad, const T *kernel, const T *output_grad, SP2_LONGS, long row_in_stride,    \
+      long col_in_stride) {                                                                   \
+    return owl_##KIND##_ndarray_conv_spatial_backward_input(input_grad, kernel, output_grad,  \
+                                                            SP2_VALS, row_in_stride,          \
+                                                            col_in_stride);                   \
+  }                                                                                           \
+  int owl_##KIND##_ndarray_conv_spatial_backward_kernel_##SFX(                                \
+      const T *input, T *kernel_grad, const T *output_grad, SP2_LONGS, long row_in_stride,    \
+      long col_in_stride) {                                                                   \
+    return owl_##KIND##_ndarray_conv_spatial_backward_kernel(input, kernel_grad, output_grad, \
+                                                             SP2_VALS, row_in_stride,         \
+                                                             col_in_stride);                  \
+  }                                                                                           \
+  int owl_##KIND##_ndarray_conv_cuboid_##SFX(const T *input, const T *kernel, T *output,      \
+                                             CU3_LONGS, long padding) {                       \
+    return owl_##KIND##_ndarray_conv_cuboid_im2col(input, kernel, output, CU3_VALS, padding); \
+  }                                                                                           \
+  int owl_##KIND##_ndarray_conv_cuboid_backward_input_##SFX(                                  \
+      T *input_grad, const T *kernel, const T *output_grad, CU3_LONGS) {                      \
+    return owl_##KIND##_ndarray_conv_cuboid_backward_input_im2col(input_grad, kernel,         \
+                                                                  output_grad, CU3_VALS);     \
+  }                                                                                           \
+  int owl_##KIND##_ndarray_conv_cuboid_backward_kernel_##SFX(                                 \
+      const T *input, T *kernel_grad, const T *output_grad, CU3_LONGS) {                      \
+    return owl_##KIND##_ndarray_conv_cuboid_backward_kernel_im2col(input, kernel_grad,        \
+                                                                   output_grad, CU3_VALS);    \
+  }
+
+#define CONV_SPELLINGS_ALL(KIND, T) \
+  CONV_SPELLINGS(KIND, T, mec)      \
+  CONV_SPELLINGS(KIND, T, naive)
+
+CONV_SPELLINGS_ALL(float32, float)
+CONV_SPELLINGS_ALL(float64, double)
+CONV_SPELLINGS_ALL(complex32, owlgpu_complex32)
+CONV_SPELLINGS_ALL(complex64, owlgpu_complex64)
+
 // ---- pooling -----------------------------------------------------------------
 
 #define POOL2D_FWD(KIND, T, WHICH, MODE)                                                        \

@@ -116,3 +116,37 @@ def matches(result, c) -> tuple[bool, float]:
         return False, float("inf")
     err = float(np.abs(r - exp).sum())
     return err < TOL, err
+
+
+# Owl's MEC and naive conv stubs take the im2col / GEBP stubs' arguments
+# (owl_ndarray_conv_impl.h:1570-3086); Owl's unit_conv_mec_naive.ml runs the
+# conv2d and conv3d suites on them.
+MEC = {"conv_spatial": "conv_spatial_mec",
+       "conv_spatial_backward_input": "conv_spatial_backward_input_mec",
+       "conv_spatial_backward_kernel": "conv_spatial_backward_kernel_mec",
+       "conv_cuboid_im2col": "conv_cuboid_mec",
+       "conv_cuboid_backward_input_im2col": "conv_cuboid_backward_input_mec",
+       "conv_cuboid_backward_kernel_im2col": "conv_cuboid_backward_kernel_mec"}
+NAIVE = {k: v.replace("_mec", "_naive") for k, v in MEC.items()}
+MEC_NAIVE_FILES = ("unit_conv2d_generic.ml", "unit_conv3d_generic.ml")
+
+
+class Spelling:
+    """A stub provider that sends the conv stubs to another spelling (MEC or
+    naive) of the same function; everything else goes through unchanged."""
+
+    def __init__(self, inner, names):
+        self.inner, self.names = inner, names
+        self.name = f"{inner.name}+{next(iter(names.values())).rsplit('_', 1)[1]}"
+
+    def stub(self, kind, op, *args):
+        self.inner.stub(kind, self.names.get(op, op), *args)
+
+    def empty(self, like, shape, dtype=None):
+        return self.inner.empty(like, shape, dtype)
+
+    def shape(self, a):
+        return self.inner.shape(a)
+
+    def reshape(self, a, shape):
+        return self.inner.reshape(a, shape)
