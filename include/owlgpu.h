@@ -785,574 +785,608 @@ typedef struct { float re, im; } owlgpu_complex32;
 typedef struct { double re, im; } owlgpu_complex64;
 
 int owl_complex32_ndarray_conv_spatial(
-    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
-    long input_cols, long input_rows, long in_channel, long kernel_cols,
-    long kernel_rows, long output_cols, long output_rows, long out_channel,
-    long row_stride, long col_stride, long padding, long row_in_stride,
-    long col_in_stride);
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel,
+    owlgpu_complex32 *output, long batches, long input_cols, long input_rows,
+    long in_channel, long kernel_cols, long kernel_rows, long output_cols,
+    long output_rows, long out_channel, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride);
 int owl_complex64_ndarray_conv_spatial(
-    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
-    long input_cols, long input_rows, long in_channel, long kernel_cols,
-    long kernel_rows, long output_cols, long output_rows, long out_channel,
-    long row_stride, long col_stride, long padding, long row_in_stride,
-    long col_in_stride);
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel,
+    owlgpu_complex64 *output, long batches, long input_cols, long input_rows,
+    long in_channel, long kernel_cols, long kernel_rows, long output_cols,
+    long output_rows, long out_channel, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride);
 int owl_complex32_ndarray_conv_spatial_backward_input(
-    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride);
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride);
 int owl_complex64_ndarray_conv_spatial_backward_input(
-    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride);
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride);
 int owl_complex32_ndarray_conv_spatial_backward_kernel(
-    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride);
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride);
 int owl_complex64_ndarray_conv_spatial_backward_kernel(
-    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride);
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride);
 int owl_complex32_ndarray_conv_spatial_im2col(
-    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
-    long input_cols, long input_rows, long in_channel, long kernel_cols,
-    long kernel_rows, long output_cols, long output_rows, long out_channel,
-    long row_stride, long col_stride, long padding, long row_in_stride,
-    long col_in_stride);
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel,
+    owlgpu_complex32 *output, long batches, long input_cols, long input_rows,
+    long in_channel, long kernel_cols, long kernel_rows, long output_cols,
+    long output_rows, long out_channel, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride);
 int owl_complex64_ndarray_conv_spatial_im2col(
-    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
-    long input_cols, long input_rows, long in_channel, long kernel_cols,
-    long kernel_rows, long output_cols, long output_rows, long out_channel,
-    long row_stride, long col_stride, long padding, long row_in_stride,
-    long col_in_stride);
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel,
+    owlgpu_complex64 *output, long batches, long input_cols, long input_rows,
+    long in_channel, long kernel_cols, long kernel_rows, long output_cols,
+    long output_rows, long out_channel, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride);
 int owl_complex32_ndarray_conv_spatial_backward_input_im2col(
-    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride);
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride);
 int owl_complex64_ndarray_conv_spatial_backward_input_im2col(
-    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride);
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride);
 int owl_complex32_ndarray_conv_spatial_backward_kernel_im2col(
-    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride);
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride);
 int owl_complex64_ndarray_conv_spatial_backward_kernel_im2col(
-    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride);
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride);
 int owl_complex32_ndarray_conv_cuboid_im2col(
-    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
-    long input_cols, long input_rows, long input_dpts, long in_channel,
-    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
-    long output_rows, long output_dpts, long out_channel, long dpt_stride,
-    long row_stride, long col_stride, long padding);
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel,
+    owlgpu_complex32 *output, long batches, long input_cols, long input_rows,
+    long input_dpts, long in_channel, long kernel_cols, long kernel_rows,
+    long kernel_dpts, long output_cols, long output_rows, long output_dpts,
+    long out_channel, long dpt_stride, long row_stride, long col_stride,
+    long padding);
 int owl_complex64_ndarray_conv_cuboid_im2col(
-    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
-    long input_cols, long input_rows, long input_dpts, long in_channel,
-    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
-    long output_rows, long output_dpts, long out_channel, long dpt_stride,
-    long row_stride, long col_stride, long padding);
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel,
+    owlgpu_complex64 *output, long batches, long input_cols, long input_rows,
+    long input_dpts, long in_channel, long kernel_cols, long kernel_rows,
+    long kernel_dpts, long output_cols, long output_rows, long output_dpts,
+    long out_channel, long dpt_stride, long row_stride, long col_stride,
+    long padding);
 int owl_complex32_ndarray_conv_cuboid_backward_input_im2col(
-    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride);
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long out_channel, long dpt_stride, long row_stride,
+    long col_stride);
 int owl_complex64_ndarray_conv_cuboid_backward_input_im2col(
-    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride);
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long out_channel, long dpt_stride, long row_stride,
+    long col_stride);
 int owl_complex32_ndarray_conv_cuboid_backward_kernel_im2col(
-    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride);
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long out_channel, long dpt_stride, long row_stride,
+    long col_stride);
 int owl_complex64_ndarray_conv_cuboid_backward_kernel_im2col(
-    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride);
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long out_channel, long dpt_stride, long row_stride,
+    long col_stride);
 int owl_complex32_ndarray_conv_dilated_spatial_im2col(
-    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
-    long input_cols, long input_rows, long in_channel, long kernel_cols,
-    long kernel_rows, long output_cols, long output_rows, long out_channel,
-    long row_stride, long col_stride, long padding, long row_in_stride,
-    long col_in_stride);
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel,
+    owlgpu_complex32 *output, long batches, long input_cols, long input_rows,
+    long in_channel, long kernel_cols, long kernel_rows, long output_cols,
+    long output_rows, long out_channel, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride);
 int owl_complex64_ndarray_conv_dilated_spatial_im2col(
-    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
-    long input_cols, long input_rows, long in_channel, long kernel_cols,
-    long kernel_rows, long output_cols, long output_rows, long out_channel,
-    long row_stride, long col_stride, long padding, long row_in_stride,
-    long col_in_stride);
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel,
+    owlgpu_complex64 *output, long batches, long input_cols, long input_rows,
+    long in_channel, long kernel_cols, long kernel_rows, long output_cols,
+    long output_rows, long out_channel, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride);
 int owl_complex32_ndarray_conv_dilated_spatial_backward_input_im2col(
-    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride);
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride);
 int owl_complex64_ndarray_conv_dilated_spatial_backward_input_im2col(
-    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride);
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride);
 int owl_complex32_ndarray_conv_dilated_spatial_backward_kernel_im2col(
-    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride);
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride);
 int owl_complex64_ndarray_conv_dilated_spatial_backward_kernel_im2col(
-    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride);
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride);
 int owl_complex32_ndarray_conv_dilated_cuboid_im2col(
-    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
-    long input_cols, long input_rows, long input_dpts, long in_channel,
-    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
-    long output_rows, long output_dpts, long out_channel, long dpt_stride,
-    long row_stride, long col_stride, long dpt_in_stride, long row_in_stride,
-    long col_in_stride, long padding);
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel,
+    owlgpu_complex32 *output, long batches, long input_cols, long input_rows,
+    long input_dpts, long in_channel, long kernel_cols, long kernel_rows,
+    long kernel_dpts, long output_cols, long output_rows, long output_dpts,
+    long out_channel, long dpt_stride, long row_stride, long col_stride,
+    long dpt_in_stride, long row_in_stride, long col_in_stride, long padding);
 int owl_complex64_ndarray_conv_dilated_cuboid_im2col(
-    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel,
+    owlgpu_complex64 *output, long batches, long input_cols, long input_rows,
+    long input_dpts, long in_channel, long kernel_cols, long kernel_rows,
+    long kernel_dpts, long output_cols, long output_rows, long output_dpts,
+    long out_channel, long dpt_stride, long row_stride, long col_stride,
+    long dpt_in_stride, long row_in_stride, long col_in_stride, long padding);
+int owl_complex32_ndarray_conv_dilated_cuboid_backward_input_im2col(
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long out_channel, long dpt_stride, long row_stride,
+    long col_stride, long dpt_in_stride, long row_in_stride, long col_in_stride);
+int owl_complex64_ndarray_conv_dilated_cuboid_backward_input_im2col(
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long out_channel, long dpt_stride, long row_stride,
+    long col_stride, long dpt_in_stride, long row_in_stride, long col_in_stride);
+int owl_complex32_ndarray_conv_dilated_cuboid_backward_kernel_im2col(
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long out_channel, long dpt_stride, long row_stride,
+    long col_stride, long dpt_in_stride, long row_in_stride, long col_in_stride);
+int owl_complex64_ndarray_conv_dilated_cuboid_backward_kernel_im2col(
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long out_channel, long dpt_stride, long row_stride,
+    long col_stride, long dpt_in_stride, long row_in_stride, long col_in_stride);
+int owl_complex32_ndarray_maxpool_spatial(
+    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long row_stride,
+    long col_stride, long padding, long row_in_stride, long col_in_stride);
+int owl_complex64_ndarray_maxpool_spatial(
+    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long row_stride,
+    long col_stride, long padding, long row_in_stride, long col_in_stride);
+int owl_complex32_ndarray_avgpool_spatial(
+    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long row_stride,
+    long col_stride, long padding, long row_in_stride, long col_in_stride);
+int owl_complex64_ndarray_avgpool_spatial(
+    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long row_stride,
+    long col_stride, long padding, long row_in_stride, long col_in_stride);
+int owl_complex32_ndarray_maxpool_spatial_backward(
+    const owlgpu_complex32 *input, const owlgpu_complex32 *output_grad,
+    owlgpu_complex32 *input_grad, long batches, long input_cols, long input_rows,
+    long in_channel, long kernel_cols, long kernel_rows, long output_cols,
+    long output_rows, long row_stride, long col_stride, long pad_rows,
+    long pad_cols);
+int owl_complex64_ndarray_maxpool_spatial_backward(
+    const owlgpu_complex64 *input, const owlgpu_complex64 *output_grad,
+    owlgpu_complex64 *input_grad, long batches, long input_cols, long input_rows,
+    long in_channel, long kernel_cols, long kernel_rows, long output_cols,
+    long output_rows, long row_stride, long col_stride, long pad_rows,
+    long pad_cols);
+int owl_complex32_ndarray_avgpool_spatial_backward(
+    const owlgpu_complex32 *input, const owlgpu_complex32 *output_grad,
+    owlgpu_complex32 *input_grad, long batches, long input_cols, long input_rows,
+    long in_channel, long kernel_cols, long kernel_rows, long output_cols,
+    long output_rows, long row_stride, long col_stride, long pad_rows,
+    long pad_cols);
+int owl_complex64_ndarray_avgpool_spatial_backward(
+    const owlgpu_complex64 *input, const owlgpu_complex64 *output_grad,
+    owlgpu_complex64 *input_grad, long batches, long input_cols, long input_rows,
+    long in_channel, long kernel_cols, long kernel_rows, long output_cols,
+    long output_rows, long row_stride, long col_stride, long pad_rows,
+    long pad_cols);
+int owl_complex32_ndarray_maxpool_argmax_spatial(
+    const owlgpu_complex32 *input, owlgpu_complex32 *output, int64_t *argmax,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long row_stride, long col_stride, long pad_rows, long pad_cols);
+int owl_complex64_ndarray_maxpool_argmax_spatial(
+    const owlgpu_complex64 *input, owlgpu_complex64 *output, int64_t *argmax,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long row_stride, long col_stride, long pad_rows, long pad_cols);
+int owl_complex32_ndarray_maxpool_cuboid(
+    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches,
     long input_cols, long input_rows, long input_dpts, long in_channel,
     long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
-    long output_rows, long output_dpts, long out_channel, long dpt_stride,
-    long row_stride, long col_stride, long dpt_in_stride, long row_in_stride,
-    long col_in_stride, long padding);
-int owl_complex32_ndarray_conv_dilated_cuboid_backward_input_im2col(
-    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride, long dpt_in_stride,
-    long row_in_stride, long col_in_stride);
-int owl_complex64_ndarray_conv_dilated_cuboid_backward_input_im2col(
-    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride, long dpt_in_stride,
-    long row_in_stride, long col_in_stride);
-int owl_complex32_ndarray_conv_dilated_cuboid_backward_kernel_im2col(
-    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride, long dpt_in_stride,
-    long row_in_stride, long col_in_stride);
-int owl_complex64_ndarray_conv_dilated_cuboid_backward_kernel_im2col(
-    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride, long dpt_in_stride,
-    long row_in_stride, long col_in_stride);
-int owl_complex32_ndarray_maxpool_spatial(
-    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches, long input_cols,
-    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
-    long output_cols, long output_rows, long row_stride, long col_stride,
-    long padding, long row_in_stride, long col_in_stride);
-int owl_complex64_ndarray_maxpool_spatial(
-    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches, long input_cols,
-    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
-    long output_cols, long output_rows, long row_stride, long col_stride,
-    long padding, long row_in_stride, long col_in_stride);
-int owl_complex32_ndarray_avgpool_spatial(
-    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches, long input_cols,
-    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
-    long output_cols, long output_rows, long row_stride, long col_stride,
-    long padding, long row_in_stride, long col_in_stride);
-int owl_complex64_ndarray_avgpool_spatial(
-    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches, long input_cols,
-    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
-    long output_cols, long output_rows, long row_stride, long col_stride,
-    long padding, long row_in_stride, long col_in_stride);
-int owl_complex32_ndarray_maxpool_spatial_backward(
-    const owlgpu_complex32 *input, const owlgpu_complex32 *output_grad, owlgpu_complex32 *input_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long row_stride, long col_stride, long pad_rows, long pad_cols);
-int owl_complex64_ndarray_maxpool_spatial_backward(
-    const owlgpu_complex64 *input, const owlgpu_complex64 *output_grad, owlgpu_complex64 *input_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long row_stride, long col_stride, long pad_rows, long pad_cols);
-int owl_complex32_ndarray_avgpool_spatial_backward(
-    const owlgpu_complex32 *input, const owlgpu_complex32 *output_grad, owlgpu_complex32 *input_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long row_stride, long col_stride, long pad_rows, long pad_cols);
-int owl_complex64_ndarray_avgpool_spatial_backward(
-    const owlgpu_complex64 *input, const owlgpu_complex64 *output_grad, owlgpu_complex64 *input_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long row_stride, long col_stride, long pad_rows, long pad_cols);
-int owl_complex32_ndarray_maxpool_argmax_spatial(
-    const owlgpu_complex32 *input, owlgpu_complex32 *output, int64_t *argmax, long batches,
-    long input_cols, long input_rows, long in_channel, long kernel_cols,
-    long kernel_rows, long output_cols, long output_rows, long row_stride,
-    long col_stride, long pad_rows, long pad_cols);
-int owl_complex64_ndarray_maxpool_argmax_spatial(
-    const owlgpu_complex64 *input, owlgpu_complex64 *output, int64_t *argmax, long batches,
-    long input_cols, long input_rows, long in_channel, long kernel_cols,
-    long kernel_rows, long output_cols, long output_rows, long row_stride,
-    long col_stride, long pad_rows, long pad_cols);
-int owl_complex32_ndarray_maxpool_cuboid(
-    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches, long input_cols,
-    long input_rows, long input_dpts, long in_channel, long kernel_cols,
-    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
-    long output_dpts, long dpt_stride, long row_stride, long col_stride,
-    long padding);
+    long output_rows, long output_dpts, long dpt_stride, long row_stride,
+    long col_stride, long padding);
 int owl_complex64_ndarray_maxpool_cuboid(
-    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches, long input_cols,
-    long input_rows, long input_dpts, long in_channel, long kernel_cols,
-    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
-    long output_dpts, long dpt_stride, long row_stride, long col_stride,
-    long padding);
+    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long dpt_stride, long row_stride,
+    long col_stride, long padding);
 int owl_complex32_ndarray_avgpool_cuboid(
-    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches, long input_cols,
-    long input_rows, long input_dpts, long in_channel, long kernel_cols,
-    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
-    long output_dpts, long dpt_stride, long row_stride, long col_stride,
-    long padding);
+    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long dpt_stride, long row_stride,
+    long col_stride, long padding);
 int owl_complex64_ndarray_avgpool_cuboid(
-    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches, long input_cols,
-    long input_rows, long input_dpts, long in_channel, long kernel_cols,
-    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
-    long output_dpts, long dpt_stride, long row_stride, long col_stride,
-    long padding);
+    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long dpt_stride, long row_stride,
+    long col_stride, long padding);
 int owl_complex32_ndarray_maxpool_cuboid_backward(
-    const owlgpu_complex32 *input, const owlgpu_complex32 *output_grad, owlgpu_complex32 *input_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long col_stride,
-    long row_stride, long dpt_stride, long padding);
+    const owlgpu_complex32 *input, const owlgpu_complex32 *output_grad,
+    owlgpu_complex32 *input_grad, long batches, long input_cols, long input_rows,
+    long input_dpts, long in_channel, long kernel_cols, long kernel_rows,
+    long kernel_dpts, long output_cols, long output_rows, long output_dpts,
+    long col_stride, long row_stride, long dpt_stride, long padding);
 int owl_complex64_ndarray_maxpool_cuboid_backward(
-    const owlgpu_complex64 *input, const owlgpu_complex64 *output_grad, owlgpu_complex64 *input_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long col_stride,
-    long row_stride, long dpt_stride, long padding);
+    const owlgpu_complex64 *input, const owlgpu_complex64 *output_grad,
+    owlgpu_complex64 *input_grad, long batches, long input_cols, long input_rows,
+    long input_dpts, long in_channel, long kernel_cols, long kernel_rows,
+    long kernel_dpts, long output_cols, long output_rows, long output_dpts,
+    long col_stride, long row_stride, long dpt_stride, long padding);
 int owl_complex32_ndarray_avgpool_cuboid_backward(
-    const owlgpu_complex32 *input, const owlgpu_complex32 *output_grad, owlgpu_complex32 *input_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long col_stride,
-    long row_stride, long dpt_stride, long padding);
+    const owlgpu_complex32 *input, const owlgpu_complex32 *output_grad,
+    owlgpu_complex32 *input_grad, long batches, long input_cols, long input_rows,
+    long input_dpts, long in_channel, long kernel_cols, long kernel_rows,
+    long kernel_dpts, long output_cols, long output_rows, long output_dpts,
+    long col_stride, long row_stride, long dpt_stride, long padding);
 int owl_complex64_ndarray_avgpool_cuboid_backward(
-    const owlgpu_complex64 *input, const owlgpu_complex64 *output_grad, owlgpu_complex64 *input_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long col_stride,
-    long row_stride, long dpt_stride, long padding);
+    const owlgpu_complex64 *input, const owlgpu_complex64 *output_grad,
+    owlgpu_complex64 *input_grad, long batches, long input_cols, long input_rows,
+    long input_dpts, long in_channel, long kernel_cols, long kernel_rows,
+    long kernel_dpts, long output_cols, long output_rows, long output_dpts,
+    long col_stride, long row_stride, long dpt_stride, long padding);
 int owl_complex32_ndarray_upsampling_spatial_backward(
-    owlgpu_complex32 *input_grad, const owlgpu_complex32 *output_grad, long batches, long input_cols,
-    long input_rows, long in_channel, long output_cols, long output_rows,
-    long col_scale, long row_scale);
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long output_cols, long output_rows, long col_scale, long row_scale);
 int owl_complex64_ndarray_upsampling_spatial_backward(
-    owlgpu_complex64 *input_grad, const owlgpu_complex64 *output_grad, long batches, long input_cols,
-    long input_rows, long in_channel, long output_cols, long output_rows,
-    long col_scale, long row_scale);
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long output_cols, long output_rows, long col_scale, long row_scale);
 int owl_complex32_ndarray_upsampling_spatial(
-    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches, long input_cols,
-    long input_rows, long in_channel, long output_cols, long output_rows,
-    long col_scale, long row_scale);
+    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long output_cols,
+    long output_rows, long col_scale, long row_scale);
 int owl_complex64_ndarray_upsampling_spatial(
-    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches, long input_cols,
-    long input_rows, long in_channel, long output_cols, long output_rows,
-    long col_scale, long row_scale);
+    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long output_cols,
+    long output_rows, long col_scale, long row_scale);
 
 int owlgpu_complex32_ndarray_conv_spatial(
-    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
-    long input_cols, long input_rows, long in_channel, long kernel_cols,
-    long kernel_rows, long output_cols, long output_rows, long out_channel,
-    long row_stride, long col_stride, long padding, long row_in_stride,
-    long col_in_stride OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel,
+    owlgpu_complex32 *output, long batches, long input_cols, long input_rows,
+    long in_channel, long kernel_cols, long kernel_rows, long output_cols,
+    long output_rows, long out_channel, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
 int owlgpu_complex64_ndarray_conv_spatial(
-    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
-    long input_cols, long input_rows, long in_channel, long kernel_cols,
-    long kernel_rows, long output_cols, long output_rows, long out_channel,
-    long row_stride, long col_stride, long padding, long row_in_stride,
-    long col_in_stride OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel,
+    owlgpu_complex64 *output, long batches, long input_cols, long input_rows,
+    long in_channel, long kernel_cols, long kernel_rows, long output_cols,
+    long output_rows, long out_channel, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
 int owlgpu_complex32_ndarray_conv_spatial_backward_input(
-    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride OWLGPU_DEVICE_ARGS);
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
 int owlgpu_complex64_ndarray_conv_spatial_backward_input(
-    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride OWLGPU_DEVICE_ARGS);
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
 int owlgpu_complex32_ndarray_conv_spatial_backward_kernel(
-    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
 int owlgpu_complex64_ndarray_conv_spatial_backward_kernel(
-    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
 int owlgpu_complex32_ndarray_conv_cuboid_im2col(
-    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
-    long input_cols, long input_rows, long input_dpts, long in_channel,
-    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
-    long output_rows, long output_dpts, long out_channel, long dpt_stride,
-    long row_stride, long col_stride, long padding OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel,
+    owlgpu_complex32 *output, long batches, long input_cols, long input_rows,
+    long input_dpts, long in_channel, long kernel_cols, long kernel_rows,
+    long kernel_dpts, long output_cols, long output_rows, long output_dpts,
+    long out_channel, long dpt_stride, long row_stride, long col_stride,
+    long padding OWLGPU_DEVICE_ARGS);
 int owlgpu_complex64_ndarray_conv_cuboid_im2col(
-    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
-    long input_cols, long input_rows, long input_dpts, long in_channel,
-    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
-    long output_rows, long output_dpts, long out_channel, long dpt_stride,
-    long row_stride, long col_stride, long padding OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel,
+    owlgpu_complex64 *output, long batches, long input_cols, long input_rows,
+    long input_dpts, long in_channel, long kernel_cols, long kernel_rows,
+    long kernel_dpts, long output_cols, long output_rows, long output_dpts,
+    long out_channel, long dpt_stride, long row_stride, long col_stride,
+    long padding OWLGPU_DEVICE_ARGS);
 int owlgpu_complex32_ndarray_conv_cuboid_backward_input_im2col(
-    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride OWLGPU_DEVICE_ARGS);
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long out_channel, long dpt_stride, long row_stride,
+    long col_stride OWLGPU_DEVICE_ARGS);
 int owlgpu_complex64_ndarray_conv_cuboid_backward_input_im2col(
-    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride OWLGPU_DEVICE_ARGS);
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long out_channel, long dpt_stride, long row_stride,
+    long col_stride OWLGPU_DEVICE_ARGS);
 int owlgpu_complex32_ndarray_conv_cuboid_backward_kernel_im2col(
-    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long out_channel, long dpt_stride, long row_stride,
+    long col_stride OWLGPU_DEVICE_ARGS);
 int owlgpu_complex64_ndarray_conv_cuboid_backward_kernel_im2col(
-    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long out_channel, long dpt_stride, long row_stride,
+    long col_stride OWLGPU_DEVICE_ARGS);
 int owlgpu_complex32_ndarray_conv_dilated_spatial_im2col(
-    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
-    long input_cols, long input_rows, long in_channel, long kernel_cols,
-    long kernel_rows, long output_cols, long output_rows, long out_channel,
-    long row_stride, long col_stride, long padding, long row_in_stride,
-    long col_in_stride OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel,
+    owlgpu_complex32 *output, long batches, long input_cols, long input_rows,
+    long in_channel, long kernel_cols, long kernel_rows, long output_cols,
+    long output_rows, long out_channel, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
 int owlgpu_complex64_ndarray_conv_dilated_spatial_im2col(
-    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
-    long input_cols, long input_rows, long in_channel, long kernel_cols,
-    long kernel_rows, long output_cols, long output_rows, long out_channel,
-    long row_stride, long col_stride, long padding, long row_in_stride,
-    long col_in_stride OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel,
+    owlgpu_complex64 *output, long batches, long input_cols, long input_rows,
+    long in_channel, long kernel_cols, long kernel_rows, long output_cols,
+    long output_rows, long out_channel, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
 int owlgpu_complex32_ndarray_conv_dilated_spatial_backward_input_im2col(
-    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride OWLGPU_DEVICE_ARGS);
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
 int owlgpu_complex64_ndarray_conv_dilated_spatial_backward_input_im2col(
-    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride OWLGPU_DEVICE_ARGS);
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
 int owlgpu_complex32_ndarray_conv_dilated_spatial_backward_kernel_im2col(
-    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
 int owlgpu_complex64_ndarray_conv_dilated_spatial_backward_kernel_im2col(
-    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
 int owlgpu_complex32_ndarray_conv_dilated_cuboid_im2col(
-    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
-    long input_cols, long input_rows, long input_dpts, long in_channel,
-    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
-    long output_rows, long output_dpts, long out_channel, long dpt_stride,
-    long row_stride, long col_stride, long dpt_in_stride, long row_in_stride,
-    long col_in_stride, long padding OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel,
+    owlgpu_complex32 *output, long batches, long input_cols, long input_rows,
+    long input_dpts, long in_channel, long kernel_cols, long kernel_rows,
+    long kernel_dpts, long output_cols, long output_rows, long output_dpts,
+    long out_channel, long dpt_stride, long row_stride, long col_stride,
+    long dpt_in_stride, long row_in_stride, long col_in_stride,
+    long padding OWLGPU_DEVICE_ARGS);
 int owlgpu_complex64_ndarray_conv_dilated_cuboid_im2col(
-    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
-    long input_cols, long input_rows, long input_dpts, long in_channel,
-    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
-    long output_rows, long output_dpts, long out_channel, long dpt_stride,
-    long row_stride, long col_stride, long dpt_in_stride, long row_in_stride,
-    long col_in_stride, long padding OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel,
+    owlgpu_complex64 *output, long batches, long input_cols, long input_rows,
+    long input_dpts, long in_channel, long kernel_cols, long kernel_rows,
+    long kernel_dpts, long output_cols, long output_rows, long output_dpts,
+    long out_channel, long dpt_stride, long row_stride, long col_stride,
+    long dpt_in_stride, long row_in_stride, long col_in_stride,
+    long padding OWLGPU_DEVICE_ARGS);
 int owlgpu_complex32_ndarray_conv_dilated_cuboid_backward_input_im2col(
-    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride, long dpt_in_stride,
-    long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long out_channel, long dpt_stride, long row_stride,
+    long col_stride, long dpt_in_stride, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
 int owlgpu_complex64_ndarray_conv_dilated_cuboid_backward_input_im2col(
-    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride, long dpt_in_stride,
-    long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long out_channel, long dpt_stride, long row_stride,
+    long col_stride, long dpt_in_stride, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
 int owlgpu_complex32_ndarray_conv_dilated_cuboid_backward_kernel_im2col(
-    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride, long dpt_in_stride,
-    long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long out_channel, long dpt_stride, long row_stride,
+    long col_stride, long dpt_in_stride, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
 int owlgpu_complex64_ndarray_conv_dilated_cuboid_backward_kernel_im2col(
-    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride, long dpt_in_stride,
-    long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long out_channel, long dpt_stride, long row_stride,
+    long col_stride, long dpt_in_stride, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
 int owlgpu_complex32_ndarray_maxpool_spatial(
-    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches, long input_cols,
-    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
-    long output_cols, long output_rows, long row_stride, long col_stride,
-    long padding, long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long row_stride,
+    long col_stride, long padding, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
 int owlgpu_complex64_ndarray_maxpool_spatial(
-    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches, long input_cols,
-    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
-    long output_cols, long output_rows, long row_stride, long col_stride,
-    long padding, long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long row_stride,
+    long col_stride, long padding, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
 int owlgpu_complex32_ndarray_avgpool_spatial(
-    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches, long input_cols,
-    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
-    long output_cols, long output_rows, long row_stride, long col_stride,
-    long padding, long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long row_stride,
+    long col_stride, long padding, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
 int owlgpu_complex64_ndarray_avgpool_spatial(
-    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches, long input_cols,
-    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
-    long output_cols, long output_rows, long row_stride, long col_stride,
-    long padding, long row_in_stride, long col_in_stride OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long row_stride,
+    long col_stride, long padding, long row_in_stride,
+    long col_in_stride OWLGPU_DEVICE_ARGS);
 int owlgpu_complex32_ndarray_maxpool_spatial_backward(
-    const owlgpu_complex32 *input, const owlgpu_complex32 *output_grad, owlgpu_complex32 *input_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long row_stride, long col_stride, long pad_rows,
+    const owlgpu_complex32 *input, const owlgpu_complex32 *output_grad,
+    owlgpu_complex32 *input_grad, long batches, long input_cols, long input_rows,
+    long in_channel, long kernel_cols, long kernel_rows, long output_cols,
+    long output_rows, long row_stride, long col_stride, long pad_rows,
     long pad_cols OWLGPU_DEVICE_ARGS);
 int owlgpu_complex64_ndarray_maxpool_spatial_backward(
-    const owlgpu_complex64 *input, const owlgpu_complex64 *output_grad, owlgpu_complex64 *input_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long row_stride, long col_stride, long pad_rows,
+    const owlgpu_complex64 *input, const owlgpu_complex64 *output_grad,
+    owlgpu_complex64 *input_grad, long batches, long input_cols, long input_rows,
+    long in_channel, long kernel_cols, long kernel_rows, long output_cols,
+    long output_rows, long row_stride, long col_stride, long pad_rows,
     long pad_cols OWLGPU_DEVICE_ARGS);
 int owlgpu_complex32_ndarray_avgpool_spatial_backward(
-    const owlgpu_complex32 *input, const owlgpu_complex32 *output_grad, owlgpu_complex32 *input_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long row_stride, long col_stride, long pad_rows,
+    const owlgpu_complex32 *input, const owlgpu_complex32 *output_grad,
+    owlgpu_complex32 *input_grad, long batches, long input_cols, long input_rows,
+    long in_channel, long kernel_cols, long kernel_rows, long output_cols,
+    long output_rows, long row_stride, long col_stride, long pad_rows,
     long pad_cols OWLGPU_DEVICE_ARGS);
 int owlgpu_complex64_ndarray_avgpool_spatial_backward(
-    const owlgpu_complex64 *input, const owlgpu_complex64 *output_grad, owlgpu_complex64 *input_grad,
+    const owlgpu_complex64 *input, const owlgpu_complex64 *output_grad,
+    owlgpu_complex64 *input_grad, long batches, long input_cols, long input_rows,
+    long in_channel, long kernel_cols, long kernel_rows, long output_cols,
+    long output_rows, long row_stride, long col_stride, long pad_rows,
+    long pad_cols OWLGPU_DEVICE_ARGS);
+int owlgpu_complex32_ndarray_maxpool_argmax_spatial(
+    const owlgpu_complex32 *input, owlgpu_complex32 *output, int64_t *argmax,
     long batches, long input_cols, long input_rows, long in_channel,
     long kernel_cols, long kernel_rows, long output_cols, long output_rows,
     long row_stride, long col_stride, long pad_rows,
     long pad_cols OWLGPU_DEVICE_ARGS);
-int owlgpu_complex32_ndarray_maxpool_argmax_spatial(
-    const owlgpu_complex32 *input, owlgpu_complex32 *output, int64_t *argmax, long batches,
-    long input_cols, long input_rows, long in_channel, long kernel_cols,
-    long kernel_rows, long output_cols, long output_rows, long row_stride,
-    long col_stride, long pad_rows, long pad_cols OWLGPU_DEVICE_ARGS);
 int owlgpu_complex64_ndarray_maxpool_argmax_spatial(
-    const owlgpu_complex64 *input, owlgpu_complex64 *output, int64_t *argmax, long batches,
-    long input_cols, long input_rows, long in_channel, long kernel_cols,
-    long kernel_rows, long output_cols, long output_rows, long row_stride,
-    long col_stride, long pad_rows, long pad_cols OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex64 *input, owlgpu_complex64 *output, int64_t *argmax,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
+    long row_stride, long col_stride, long pad_rows,
+    long pad_cols OWLGPU_DEVICE_ARGS);
 int owlgpu_complex32_ndarray_maxpool_cuboid(
-    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches, long input_cols,
-    long input_rows, long input_dpts, long in_channel, long kernel_cols,
-    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
-    long output_dpts, long dpt_stride, long row_stride, long col_stride,
-    long padding OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long dpt_stride, long row_stride,
+    long col_stride, long padding OWLGPU_DEVICE_ARGS);
 int owlgpu_complex64_ndarray_maxpool_cuboid(
-    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches, long input_cols,
-    long input_rows, long input_dpts, long in_channel, long kernel_cols,
-    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
-    long output_dpts, long dpt_stride, long row_stride, long col_stride,
-    long padding OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long dpt_stride, long row_stride,
+    long col_stride, long padding OWLGPU_DEVICE_ARGS);
 int owlgpu_complex32_ndarray_avgpool_cuboid(
-    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches, long input_cols,
-    long input_rows, long input_dpts, long in_channel, long kernel_cols,
-    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
-    long output_dpts, long dpt_stride, long row_stride, long col_stride,
-    long padding OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long dpt_stride, long row_stride,
+    long col_stride, long padding OWLGPU_DEVICE_ARGS);
 int owlgpu_complex64_ndarray_avgpool_cuboid(
-    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches, long input_cols,
-    long input_rows, long input_dpts, long in_channel, long kernel_cols,
-    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
-    long output_dpts, long dpt_stride, long row_stride, long col_stride,
-    long padding OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long dpt_stride, long row_stride,
+    long col_stride, long padding OWLGPU_DEVICE_ARGS);
 int owlgpu_complex32_ndarray_maxpool_cuboid_backward(
-    const owlgpu_complex32 *input, const owlgpu_complex32 *output_grad, owlgpu_complex32 *input_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long col_stride,
-    long row_stride, long dpt_stride, long padding OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex32 *input, const owlgpu_complex32 *output_grad,
+    owlgpu_complex32 *input_grad, long batches, long input_cols, long input_rows,
+    long input_dpts, long in_channel, long kernel_cols, long kernel_rows,
+    long kernel_dpts, long output_cols, long output_rows, long output_dpts,
+    long col_stride, long row_stride, long dpt_stride,
+    long padding OWLGPU_DEVICE_ARGS);
 int owlgpu_complex64_ndarray_maxpool_cuboid_backward(
-    const owlgpu_complex64 *input, const owlgpu_complex64 *output_grad, owlgpu_complex64 *input_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long col_stride,
-    long row_stride, long dpt_stride, long padding OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex64 *input, const owlgpu_complex64 *output_grad,
+    owlgpu_complex64 *input_grad, long batches, long input_cols, long input_rows,
+    long input_dpts, long in_channel, long kernel_cols, long kernel_rows,
+    long kernel_dpts, long output_cols, long output_rows, long output_dpts,
+    long col_stride, long row_stride, long dpt_stride,
+    long padding OWLGPU_DEVICE_ARGS);
 int owlgpu_complex32_ndarray_avgpool_cuboid_backward(
-    const owlgpu_complex32 *input, const owlgpu_complex32 *output_grad, owlgpu_complex32 *input_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long col_stride,
-    long row_stride, long dpt_stride, long padding OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex32 *input, const owlgpu_complex32 *output_grad,
+    owlgpu_complex32 *input_grad, long batches, long input_cols, long input_rows,
+    long input_dpts, long in_channel, long kernel_cols, long kernel_rows,
+    long kernel_dpts, long output_cols, long output_rows, long output_dpts,
+    long col_stride, long row_stride, long dpt_stride,
+    long padding OWLGPU_DEVICE_ARGS);
 int owlgpu_complex64_ndarray_avgpool_cuboid_backward(
-    const owlgpu_complex64 *input, const owlgpu_complex64 *output_grad, owlgpu_complex64 *input_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long col_stride,
-    long row_stride, long dpt_stride, long padding OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex64 *input, const owlgpu_complex64 *output_grad,
+    owlgpu_complex64 *input_grad, long batches, long input_cols, long input_rows,
+    long input_dpts, long in_channel, long kernel_cols, long kernel_rows,
+    long kernel_dpts, long output_cols, long output_rows, long output_dpts,
+    long col_stride, long row_stride, long dpt_stride,
+    long padding OWLGPU_DEVICE_ARGS);
 int owlgpu_complex32_ndarray_upsampling_spatial_backward(
-    owlgpu_complex32 *input_grad, const owlgpu_complex32 *output_grad, long batches, long input_cols,
-    long input_rows, long in_channel, long output_cols, long output_rows,
-    long col_scale, long row_scale OWLGPU_DEVICE_ARGS);
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long output_cols, long output_rows, long col_scale,
+    long row_scale OWLGPU_DEVICE_ARGS);
 int owlgpu_complex64_ndarray_upsampling_spatial_backward(
-    owlgpu_complex64 *input_grad, const owlgpu_complex64 *output_grad, long batches, long input_cols,
-    long input_rows, long in_channel, long output_cols, long output_rows,
-    long col_scale, long row_scale OWLGPU_DEVICE_ARGS);
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *output_grad,
+    long batches, long input_cols, long input_rows, long in_channel,
+    long output_cols, long output_rows, long col_scale,
+    long row_scale OWLGPU_DEVICE_ARGS);
 int owlgpu_complex32_ndarray_upsampling_spatial(
-    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches, long input_cols,
-    long input_rows, long in_channel, long output_cols, long output_rows,
-    long col_scale, long row_scale OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex32 *input, owlgpu_complex32 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long output_cols,
+    long output_rows, long col_scale, long row_scale OWLGPU_DEVICE_ARGS);
 int owlgpu_complex64_ndarray_upsampling_spatial(
-    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches, long input_cols,
-    long input_rows, long in_channel, long output_cols, long output_rows,
-    long col_scale, long row_scale OWLGPU_DEVICE_ARGS);
+    const owlgpu_complex64 *input, owlgpu_complex64 *output, long batches,
+    long input_cols, long input_rows, long in_channel, long output_cols,
+    long output_rows, long col_scale, long row_scale OWLGPU_DEVICE_ARGS);
 
 /* ======================================================================
  * MEC and naive spellings.  Owl binds its memory-efficient (MEC) and naive
@@ -1374,17 +1408,15 @@ int owl_float32_ndarray_conv_spatial_mec(
     long row_stride, long col_stride, long padding, long row_in_stride,
     long col_in_stride);
 int owl_float32_ndarray_conv_spatial_backward_input_mec(
-    float *input_grad, const float *kernel, const float *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride);
+    float *input_grad, const float *kernel, const float *output_grad, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long row_in_stride, long col_in_stride);
 int owl_float32_ndarray_conv_spatial_backward_kernel_mec(
-    const float *input, float *kernel_grad, const float *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride);
+    const float *input, float *kernel_grad, const float *output_grad, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long row_in_stride, long col_in_stride);
 int owl_float32_ndarray_conv_cuboid_mec(
     const float *input, const float *kernel, float *output, long batches,
     long input_cols, long input_rows, long input_dpts, long in_channel,
@@ -1392,17 +1424,17 @@ int owl_float32_ndarray_conv_cuboid_mec(
     long output_rows, long output_dpts, long out_channel, long dpt_stride,
     long row_stride, long col_stride, long padding);
 int owl_float32_ndarray_conv_cuboid_backward_input_mec(
-    float *input_grad, const float *kernel, const float *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride);
+    float *input_grad, const float *kernel, const float *output_grad, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride);
 int owl_float32_ndarray_conv_cuboid_backward_kernel_mec(
-    const float *input, float *kernel_grad, const float *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride);
+    const float *input, float *kernel_grad, const float *output_grad, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride);
 int owl_float64_ndarray_conv_spatial_mec(
     const double *input, const double *kernel, double *output, long batches,
     long input_cols, long input_rows, long in_channel, long kernel_cols,
@@ -1440,77 +1472,83 @@ int owl_float64_ndarray_conv_cuboid_backward_kernel_mec(
     long output_cols, long output_rows, long output_dpts, long out_channel,
     long dpt_stride, long row_stride, long col_stride);
 int owl_complex32_ndarray_conv_spatial_mec(
-    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
-    long input_cols, long input_rows, long in_channel, long kernel_cols,
-    long kernel_rows, long output_cols, long output_rows, long out_channel,
-    long row_stride, long col_stride, long padding, long row_in_stride,
-    long col_in_stride);
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel,
+    owlgpu_complex32 *output, long batches, long input_cols, long input_rows,
+    long in_channel, long kernel_cols, long kernel_rows, long output_cols,
+    long output_rows, long out_channel, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride);
 int owl_complex32_ndarray_conv_spatial_backward_input_mec(
-    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride);
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride);
 int owl_complex32_ndarray_conv_spatial_backward_kernel_mec(
-    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride);
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride);
 int owl_complex32_ndarray_conv_cuboid_mec(
-    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
-    long input_cols, long input_rows, long input_dpts, long in_channel,
-    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
-    long output_rows, long output_dpts, long out_channel, long dpt_stride,
-    long row_stride, long col_stride, long padding);
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel,
+    owlgpu_complex32 *output, long batches, long input_cols, long input_rows,
+    long input_dpts, long in_channel, long kernel_cols, long kernel_rows,
+    long kernel_dpts, long output_cols, long output_rows, long output_dpts,
+    long out_channel, long dpt_stride, long row_stride, long col_stride,
+    long padding);
 int owl_complex32_ndarray_conv_cuboid_backward_input_mec(
-    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride);
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long out_channel, long dpt_stride, long row_stride,
+    long col_stride);
 int owl_complex32_ndarray_conv_cuboid_backward_kernel_mec(
-    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride);
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long out_channel, long dpt_stride, long row_stride,
+    long col_stride);
 int owl_complex64_ndarray_conv_spatial_mec(
-    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
-    long input_cols, long input_rows, long in_channel, long kernel_cols,
-    long kernel_rows, long output_cols, long output_rows, long out_channel,
-    long row_stride, long col_stride, long padding, long row_in_stride,
-    long col_in_stride);
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel,
+    owlgpu_complex64 *output, long batches, long input_cols, long input_rows,
+    long in_channel, long kernel_cols, long kernel_rows, long output_cols,
+    long output_rows, long out_channel, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride);
 int owl_complex64_ndarray_conv_spatial_backward_input_mec(
-    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride);
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride);
 int owl_complex64_ndarray_conv_spatial_backward_kernel_mec(
-    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride);
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride);
 int owl_complex64_ndarray_conv_cuboid_mec(
-    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
-    long input_cols, long input_rows, long input_dpts, long in_channel,
-    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
-    long output_rows, long output_dpts, long out_channel, long dpt_stride,
-    long row_stride, long col_stride, long padding);
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel,
+    owlgpu_complex64 *output, long batches, long input_cols, long input_rows,
+    long input_dpts, long in_channel, long kernel_cols, long kernel_rows,
+    long kernel_dpts, long output_cols, long output_rows, long output_dpts,
+    long out_channel, long dpt_stride, long row_stride, long col_stride,
+    long padding);
 int owl_complex64_ndarray_conv_cuboid_backward_input_mec(
-    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride);
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long out_channel, long dpt_stride, long row_stride,
+    long col_stride);
 int owl_complex64_ndarray_conv_cuboid_backward_kernel_mec(
-    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride);
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long out_channel, long dpt_stride, long row_stride,
+    long col_stride);
 int owl_float32_ndarray_conv_spatial_naive(
     const float *input, const float *kernel, float *output, long batches,
     long input_cols, long input_rows, long in_channel, long kernel_cols,
@@ -1518,17 +1556,15 @@ int owl_float32_ndarray_conv_spatial_naive(
     long row_stride, long col_stride, long padding, long row_in_stride,
     long col_in_stride);
 int owl_float32_ndarray_conv_spatial_backward_input_naive(
-    float *input_grad, const float *kernel, const float *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride);
+    float *input_grad, const float *kernel, const float *output_grad, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long row_in_stride, long col_in_stride);
 int owl_float32_ndarray_conv_spatial_backward_kernel_naive(
-    const float *input, float *kernel_grad, const float *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride);
+    const float *input, float *kernel_grad, const float *output_grad, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long row_in_stride, long col_in_stride);
 int owl_float32_ndarray_conv_cuboid_naive(
     const float *input, const float *kernel, float *output, long batches,
     long input_cols, long input_rows, long input_dpts, long in_channel,
@@ -1536,17 +1572,17 @@ int owl_float32_ndarray_conv_cuboid_naive(
     long output_rows, long output_dpts, long out_channel, long dpt_stride,
     long row_stride, long col_stride, long padding);
 int owl_float32_ndarray_conv_cuboid_backward_input_naive(
-    float *input_grad, const float *kernel, const float *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride);
+    float *input_grad, const float *kernel, const float *output_grad, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride);
 int owl_float32_ndarray_conv_cuboid_backward_kernel_naive(
-    const float *input, float *kernel_grad, const float *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride);
+    const float *input, float *kernel_grad, const float *output_grad, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride);
 int owl_float64_ndarray_conv_spatial_naive(
     const double *input, const double *kernel, double *output, long batches,
     long input_cols, long input_rows, long in_channel, long kernel_cols,
@@ -1584,77 +1620,83 @@ int owl_float64_ndarray_conv_cuboid_backward_kernel_naive(
     long output_cols, long output_rows, long output_dpts, long out_channel,
     long dpt_stride, long row_stride, long col_stride);
 int owl_complex32_ndarray_conv_spatial_naive(
-    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
-    long input_cols, long input_rows, long in_channel, long kernel_cols,
-    long kernel_rows, long output_cols, long output_rows, long out_channel,
-    long row_stride, long col_stride, long padding, long row_in_stride,
-    long col_in_stride);
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel,
+    owlgpu_complex32 *output, long batches, long input_cols, long input_rows,
+    long in_channel, long kernel_cols, long kernel_rows, long output_cols,
+    long output_rows, long out_channel, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride);
 int owl_complex32_ndarray_conv_spatial_backward_input_naive(
-    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride);
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride);
 int owl_complex32_ndarray_conv_spatial_backward_kernel_naive(
-    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride);
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride);
 int owl_complex32_ndarray_conv_cuboid_naive(
-    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel, owlgpu_complex32 *output, long batches,
-    long input_cols, long input_rows, long input_dpts, long in_channel,
-    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
-    long output_rows, long output_dpts, long out_channel, long dpt_stride,
-    long row_stride, long col_stride, long padding);
+    const owlgpu_complex32 *input, const owlgpu_complex32 *kernel,
+    owlgpu_complex32 *output, long batches, long input_cols, long input_rows,
+    long input_dpts, long in_channel, long kernel_cols, long kernel_rows,
+    long kernel_dpts, long output_cols, long output_rows, long output_dpts,
+    long out_channel, long dpt_stride, long row_stride, long col_stride,
+    long padding);
 int owl_complex32_ndarray_conv_cuboid_backward_input_naive(
-    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride);
+    owlgpu_complex32 *input_grad, const owlgpu_complex32 *kernel,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long out_channel, long dpt_stride, long row_stride,
+    long col_stride);
 int owl_complex32_ndarray_conv_cuboid_backward_kernel_naive(
-    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad, const owlgpu_complex32 *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride);
+    const owlgpu_complex32 *input, owlgpu_complex32 *kernel_grad,
+    const owlgpu_complex32 *output_grad, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long out_channel, long dpt_stride, long row_stride,
+    long col_stride);
 int owl_complex64_ndarray_conv_spatial_naive(
-    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
-    long input_cols, long input_rows, long in_channel, long kernel_cols,
-    long kernel_rows, long output_cols, long output_rows, long out_channel,
-    long row_stride, long col_stride, long padding, long row_in_stride,
-    long col_in_stride);
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel,
+    owlgpu_complex64 *output, long batches, long input_cols, long input_rows,
+    long in_channel, long kernel_cols, long kernel_rows, long output_cols,
+    long output_rows, long out_channel, long row_stride, long col_stride,
+    long padding, long row_in_stride, long col_in_stride);
 int owl_complex64_ndarray_conv_spatial_backward_input_naive(
-    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride);
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride);
 int owl_complex64_ndarray_conv_spatial_backward_kernel_naive(
-    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long in_channel,
-    long kernel_cols, long kernel_rows, long output_cols, long output_rows,
-    long out_channel, long row_stride, long col_stride, long row_in_stride,
-    long col_in_stride);
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long in_channel, long kernel_cols, long kernel_rows,
+    long output_cols, long output_rows, long out_channel, long row_stride,
+    long col_stride, long row_in_stride, long col_in_stride);
 int owl_complex64_ndarray_conv_cuboid_naive(
-    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel, owlgpu_complex64 *output, long batches,
-    long input_cols, long input_rows, long input_dpts, long in_channel,
-    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
-    long output_rows, long output_dpts, long out_channel, long dpt_stride,
-    long row_stride, long col_stride, long padding);
+    const owlgpu_complex64 *input, const owlgpu_complex64 *kernel,
+    owlgpu_complex64 *output, long batches, long input_cols, long input_rows,
+    long input_dpts, long in_channel, long kernel_cols, long kernel_rows,
+    long kernel_dpts, long output_cols, long output_rows, long output_dpts,
+    long out_channel, long dpt_stride, long row_stride, long col_stride,
+    long padding);
 int owl_complex64_ndarray_conv_cuboid_backward_input_naive(
-    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride);
+    owlgpu_complex64 *input_grad, const owlgpu_complex64 *kernel,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long out_channel, long dpt_stride, long row_stride,
+    long col_stride);
 int owl_complex64_ndarray_conv_cuboid_backward_kernel_naive(
-    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad, const owlgpu_complex64 *output_grad,
-    long batches, long input_cols, long input_rows, long input_dpts,
-    long in_channel, long kernel_cols, long kernel_rows, long kernel_dpts,
-    long output_cols, long output_rows, long output_dpts, long out_channel,
-    long dpt_stride, long row_stride, long col_stride);
+    const owlgpu_complex64 *input, owlgpu_complex64 *kernel_grad,
+    const owlgpu_complex64 *output_grad, long batches, long input_cols,
+    long input_rows, long input_dpts, long in_channel, long kernel_cols,
+    long kernel_rows, long kernel_dpts, long output_cols, long output_rows,
+    long output_dpts, long out_channel, long dpt_stride, long row_stride,
+    long col_stride);
 
 /* ======================================================================
  * Allocation-free entry point.  No counterpart in the reference: Owl's C
