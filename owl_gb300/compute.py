@@ -431,7 +431,9 @@ def eval_graph(graph: Graph, device: Device):
 class CompiledGraph:
     """A planned graph captured once as a CUDA graph.  `run(inputs)` copies
     each input array into its variable's buffer and replays the captured
-    kernels; the outputs are the graph's output buffers."""
+    kernels; the outputs are the graph's output buffers (overwritten by the
+    next run).  Packed arrays (weights) are captured by address: update them
+    in place (`copy_`), not by rebinding the node to a new array."""
 
     def __init__(self, graph: Graph, device: Device):
         import torch

@@ -134,3 +134,19 @@ def test_unassigned_inputs_are_errors(oracle_nn):
         C.eval_graph(g, C.Device(oracle_nn))
     with pytest.raises(InvalidArgument):
         C.unpack_arr(y)
+
+
+def test_complex_graph(oracle_nn):
+    """Complex64 (Owl's Complex32) nodes plan and evaluate like real ones."""
+    rng = np.random.default_rng(75)
+    c = lambda s: (rng.uniform(-1, 1, s) + 1j * rng.uniform(-1, 1, s)).astype(np.complex64)  # noqa: E731
+    x = C.var_arr((2, 6, 6, 2), "x", np.complex64)
+    w = C.pack_arr(c((3, 3, 2, 3)))
+    y = C.avg_pool2d(C.conv2d(x, w, [1, 1]), [2, 2], [2, 2])
+    assert y.dtype == np.complex64 and y.shape == (2, 3, 3, 3)
+    g = C.make_graph([x], [y])
+    xv = c(x.shape)
+    C.assign_arr(x, xv)
+    (got,) = C.eval_graph(g, C.Device(oracle_nn))
+    ref = oracle_nn.avg_pool2d(oracle_nn.conv2d(xv, C.unpack_arr(w), [1, 1]), [2, 2], [2, 2])
+    assert np.array_equal(got, ref)
