@@ -406,7 +406,7 @@ def _like_dtype(like, dtype):
     if type(like).__module__.startswith("torch"):
         import torch
 
-        return {"float32": torch.float32, "float64": torch.float64}[str(dtype)]
+        return getattr(torch, str(dtype))  # float32, float64, complex64, complex128
     return dtype
 
 

@@ -150,3 +150,53 @@ def test_complex_graph(oracle_nn):
     (got,) = C.eval_graph(g, C.Device(oracle_nn))
     ref = oracle_nn.avg_pool2d(oracle_nn.conv2d(xv, C.unpack_arr(w), [1, 1]), [2, 2], [2, 2])
     assert np.array_equal(got, ref)
+
+
+class _TorchOracle:
+    """The oracle over torch CPU tensors (shared-memory numpy views), so the
+    engine's torch path (buffer allocation, element types) runs on the CPU."""
+
+    name = "torch-oracle"
+
+    def __init__(self, inner):
+        self.inner = inner
+
+    def stub(self, kind, op, *args):
+        import torch
+
+        self.inner.stub(kind, op, *[a.numpy() if isinstance(a, torch.Tensor) else a
+                                    for a in args])
+
+    def empty(self, like, shape, dtype=None):
+        import torch
+
+        return torch.empty(tuple(shape), dtype=dtype or like.dtype)
+
+    def shape(self, a):
+        return tuple(a.shape)
+
+    def reshape(self, a, shape):
+        return a.reshape(shape)
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.complex128])
+def test_graph_on_torch_tensors(oracle_nn, dt):
+    import torch
+
+    from owl_gb300.dense import NN
+
+    rng = np.random.default_rng(76)
+    u = lambda s: (rng.uniform(-1, 1, s) + (1j * rng.uniform(-1, 1, s) if dt == np.complex128
+                                             else 0)).astype(dt)  # noqa: E731
+    x = C.var_arr((2, 8, 8, 3), "x", dt)
+    w = C.pack_arr(torch.from_numpy(u((3, 3, 3, 4))))
+    y = C.avg_pool2d(C.conv2d(x, w, [1, 1]), [2, 2], [2, 2])
+    g = C.make_graph([x], [C.conv2d_backward_kernel(x, w, [1, 1], C.upsampling2d(y, [2, 2]))])
+    xv = u(x.shape)
+    C.assign_arr(x, torch.from_numpy(xv))
+    (got,) = C.eval_graph(g, C.Device(NN(_TorchOracle(oracle_nn.b))))
+    assert isinstance(got, torch.Tensor) and got.dtype == getattr(torch, np.dtype(dt).name)
+    wv = C.unpack_arr(w).numpy()
+    up = oracle_nn.upsampling2d(oracle_nn.avg_pool2d(oracle_nn.conv2d(xv, wv, [1, 1]), [2, 2],
+                                                     [2, 2]), [2, 2])
+    assert np.array_equal(got.numpy(), oracle_nn.conv2d_backward_kernel(xv, wv, [1, 1], up))
