@@ -164,6 +164,13 @@ static int make_conv(const char *fn, ConvGeom &g, long B, long IC, long IR, long
   return kOk;
 }
 
+// The pooling padding flag: 0 = SAME, 1 = VALID, as for the convolutions (Owl's
+// stubs read any value other than 1 as SAME; its OCaml layer passes only 0 or 1).
+static int check_pool_padding(const char *fn, long padding) {
+  if (padding != 0 && padding != 1) return invalid(fn, "padding must be 0 (SAME) or 1 (VALID)");
+  return kOk;
+}
+
 static int make_pool(const char *fn, PoolGeom &g, long B, long IC, long IR, long ID, long Ch,
                      long KC, long KR, long KD, long OC, long OR, long OD, long sc, long sr,
                      long sd) {
@@ -877,6 +884,7 @@ CONV_SPELLINGS_ALL(complex64, owlgpu_complex64)
                        kernel_cols, kernel_rows, 1, output_cols, output_rows, 1, col_stride,  \
                        row_stride, 1);                                                        \
     if (rc) return rc;                                                                        \
+    if (check_pool_padding(#WHICH, padding)) return kErrInvalid;                              \
     g.pr = fwd_pad(padding, row_stride, output_rows, kernel_rows, input_rows);                \
     g.pc = fwd_pad(padding, col_stride, output_cols, kernel_cols, input_cols);                \
     return pool_fwd_host<T>(MODE, g, input, output, nullptr);                                 \
@@ -892,6 +900,7 @@ CONV_SPELLINGS_ALL(complex64, owlgpu_complex64)
                        kernel_cols, kernel_rows, 1, output_cols, output_rows, 1, col_stride,  \
                        row_stride, 1);                                                        \
     if (rc) return rc;                                                                        \
+    if (check_pool_padding(#WHICH, padding)) return kErrInvalid;                              \
     g.pr = fwd_pad(padding, row_stride, output_rows, kernel_rows, input_rows);                \
     g.pc = fwd_pad(padding, col_stride, output_cols, kernel_cols, input_cols);                \
     return pool_fwd(dtype_of<T>(), MODE, g, input, output, nullptr, (cudaStream_t)stream);    \
@@ -939,6 +948,7 @@ CONV_SPELLINGS_ALL(complex64, owlgpu_complex64)
                        in_channel, kernel_cols, kernel_rows, kernel_dpts, output_cols,        \
                        output_rows, output_dpts, col_stride, row_stride, dpt_stride);         \
     if (rc) return rc;                                                                        \
+    if (check_pool_padding(#WHICH, padding)) return kErrInvalid;                              \
     g.pc = fwd_pad(padding, col_stride, output_cols, kernel_cols, input_cols);                \
     g.pr = fwd_pad(padding, row_stride, output_rows, kernel_rows, input_rows);                \
     g.pd = fwd_pad(padding, dpt_stride, output_dpts, kernel_dpts, input_dpts);                \
@@ -955,6 +965,7 @@ CONV_SPELLINGS_ALL(complex64, owlgpu_complex64)
                        in_channel, kernel_cols, kernel_rows, kernel_dpts, output_cols,        \
                        output_rows, output_dpts, col_stride, row_stride, dpt_stride);         \
     if (rc) return rc;                                                                        \
+    if (check_pool_padding(#WHICH, padding)) return kErrInvalid;                              \
     g.pc = fwd_pad(padding, col_stride, output_cols, kernel_cols, input_cols);                \
     g.pr = fwd_pad(padding, row_stride, output_rows, kernel_rows, input_rows);                \
     g.pd = fwd_pad(padding, dpt_stride, output_dpts, kernel_dpts, input_dpts);                \
@@ -971,6 +982,7 @@ CONV_SPELLINGS_ALL(complex64, owlgpu_complex64)
                        output_cols, output_rows, output_dpts, col_stride, row_stride,         \
                        dpt_stride);                                                           \
     if (rc) return rc;                                                                        \
+    if (check_pool_padding(#WHICH, padding)) return kErrInvalid;                              \
     g.pc = fwd_pad(padding, col_stride, output_cols, kernel_cols, input_cols);                \
     g.pr = fwd_pad(padding, row_stride, output_rows, kernel_rows, input_rows);                \
     g.pd = fwd_pad(padding, dpt_stride, output_dpts, kernel_dpts, input_dpts);                \
@@ -988,6 +1000,7 @@ CONV_SPELLINGS_ALL(complex64, owlgpu_complex64)
                        output_cols, output_rows, output_dpts, col_stride, row_stride,         \
                        dpt_stride);                                                           \
     if (rc) return rc;                                                                        \
+    if (check_pool_padding(#WHICH, padding)) return kErrInvalid;                              \
     g.pc = fwd_pad(padding, col_stride, output_cols, kernel_cols, input_cols);                \
     g.pr = fwd_pad(padding, row_stride, output_rows, kernel_rows, input_rows);                \
     g.pd = fwd_pad(padding, dpt_stride, output_dpts, kernel_dpts, input_dpts);                \

@@ -90,3 +90,39 @@ def test_python_layer_raises_like_owl(oracle_nn):
         oracle_nn.conv2d(x, np.zeros((3, 3, 3), np.float32), [1, 1])
     with pytest.raises(InvalidArgument):
         oracle_nn.max_pool2d(x, [2, 2], [2])
+
+
+
+def _probe_args(params, buf, value):
+    """Arguments for an entry point: every array the same small buffer, every
+    integer value(name)."""
+    import ctypes
+
+    return [ctypes.cast(buf, ctypes.c_void_p) if "*" in t else value(a) for t, a in params]
+
+
+def _is_stride(a):
+    return (a.endswith("stride") and "in_stride" not in a) or a.endswith("scale")
+
+
+def test_every_host_entry_point_rejects_bad_arguments_without_gpu():
+    """Every host drop-in (all kinds, all spellings) checks its arguments
+    before touching CUDA: a stride or scale below 1, and a padding flag other
+    than 0 (SAME) or 1 (VALID), return OWLGPU_ERR_INVALID with a message."""
+    import ctypes
+
+    from owl_gb300 import _lib
+
+    L = _lib.lib()
+    buf = (ctypes.c_double * 64)()
+    hosts = {n: p for n, (_, p) in _lib.PROTOS.items() if n.startswith("owl_")}
+    assert len(hosts) == 152
+    for name, params in hosts.items():
+        assert any(_is_stride(a) for _, a in params), name
+        args = _probe_args(params, buf, lambda a: -1 if _is_stride(a) else 1)
+        assert getattr(L, name)(*args) == -1, name
+        assert _lib.last_error(), name
+        if any(a == "padding" for _, a in params):
+            args = _probe_args(params, buf, lambda a: 7 if a == "padding" else 1)
+            assert getattr(L, name)(*args) == -1, name
+            assert "padding" in _lib.last_error(), name
