@@ -200,3 +200,16 @@ def test_graph_on_torch_tensors(oracle_nn, dt):
     up = oracle_nn.upsampling2d(oracle_nn.avg_pool2d(oracle_nn.conv2d(xv, wv, [1, 1]), [2, 2],
                                                      [2, 2]), [2, 2])
     assert np.array_equal(got.numpy(), oracle_nn.conv2d_backward_kernel(xv, wv, [1, 1], up))
+
+
+def test_graph_whose_output_is_an_input(oracle_nn):
+    """A variable listed as an output is returned as assigned; operator nodes
+    between it and the other outputs still run."""
+    x = C.var_arr((1, 4, 4, 2), "x")
+    y = C.avg_pool2d(x, [2, 2], [2, 2])
+    g = C.make_graph([x], [x, y])
+    xv = np.arange(32, dtype=np.float32).reshape(x.shape)
+    C.assign_arr(x, xv)
+    a, b = C.eval_graph(g, C.Device(oracle_nn))
+    assert a is xv and np.array_equal(b, oracle_nn.avg_pool2d(xv, [2, 2], [2, 2]))
+    assert g.buffers == 1
