@@ -105,6 +105,11 @@ struct TcParams {
   int TPS, NSL;                  // taps per weight slot; plan: slots of the longest segment
   int NH, NB;
   unsigned idesc, tmem_cols;
+  // Accumulator sets in TMEM: nbuf (1 or 2) buffers of acc_cols columns; a
+  // BF16X3 set holds the hi*hi sums at column 0 and the cross terms (hi*lo +
+  // lo*hi) at small_off, added in the epilogue.
+  int nbuf;
+  unsigned acc_cols, small_off;
   int vec_in;
   int nseg;
   Seg seg[kMaxSeg];
@@ -182,6 +187,13 @@ template <int KIND, bool MULTI>
 __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_constant__ TcParams p) {
   constexpr int EPC = (KIND == K_TF32) ? 4 : 8;  // channels per 16-byte chunk
   constexpr int PARTS = (KIND == K_BF16X3) ? 2 : 1;
+  // BF16X3 keeps the cross terms in an accumulator of their own: the tensor
+  // core rounds its FP32 accumulator toward zero after every MMA, and three
+  // MMAs per K step into one accumulator cost about three times the rounding
+  // of the hi*hi sums alone (up to 2e-5 of max|y| at K = 3456); in their own
+  // accumulator the cross terms, 2^-8 of the result, round at their own
+  // small magnitude.
+  constexpr bool SEP = (KIND == K_BF16X3);
   extern __shared__ __align__(1024) uint8_t smem[];
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -398,11 +410,12 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
         sc = MULTI ? seg_of(p, t, sc) : 0;
         const int nsl = p.seg[sc].NSL, ntap = p.seg[sc].T;
         const uint32_t *toffs = tap_off + p.seg[sc].toff;
-        const int abuf = tc & 1;
-        const uint32_t aph = (uint32_t)((tc >> 1) & 1);
+        const int abuf = p.nbuf == 2 ? (tc & 1) : 0;
+        const uint32_t aph = (uint32_t)((p.nbuf == 2 ? (tc >> 1) : tc) & 1);
         if (!wait_bar(smem_u32(&acc_empty[abuf]), aph ^ 1, abort_flag, p.status, p.spin_limit)) break;
         tc_fence_after();
-        const uint32_t d0 = tmem_base + (uint32_t)(abuf * p.NCT * p.MH * 128);
+        const uint32_t d0 = tmem_base + (uint32_t)abuf * p.acc_cols;
+        const uint32_t so = p.small_off;  // cross-term accumulators (BF16X3)
         const int nct = min(p.NCT, p.n_tiles - (int)(t % p.n_groups) * p.NCT);
         uint32_t acc = 0;
         bool ok = true;
@@ -437,8 +450,8 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
                   } else {
                     mma_bf16(d0, wd, xd, p.idesc, acc);
                     if (KIND == K_BF16X3) {
-                      mma_bf16(d0, wd + (uint64_t)wlo16, xd, p.idesc, 1);
-                      mma_bf16(d0, wd, xd + (uint64_t)xlo16, p.idesc, 1);
+                      mma_bf16(d0 + so, wd + (uint64_t)wlo16, xd, p.idesc, acc);
+                      mma_bf16(d0 + so, wd, xd + (uint64_t)xlo16, p.idesc, 1);
                     }
                   }
                   acc = 1;
@@ -460,10 +473,10 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
                     mma_bf16(d0, wa, xd, p.idesc, acc);
                     mma_bf16(d1, wb, xd, p.idesc, acc);
                     if (KIND == K_BF16X3) {
-                      mma_bf16(d0, wa + (uint64_t)wlo16, xd, p.idesc, 1);
-                      mma_bf16(d1, wb + (uint64_t)wlo16, xd, p.idesc, 1);
-                      mma_bf16(d0, wa, xd + (uint64_t)xlo16, p.idesc, 1);
-                      mma_bf16(d1, wb, xd + (uint64_t)xlo16, p.idesc, 1);
+                      mma_bf16(d0 + so, wa + (uint64_t)wlo16, xd, p.idesc, acc);
+                      mma_bf16(d1 + so, wb + (uint64_t)wlo16, xd, p.idesc, acc);
+                      mma_bf16(d0 + so, wa, xd + (uint64_t)xlo16, p.idesc, 1);
+                      mma_bf16(d1 + so, wb, xd + (uint64_t)xlo16, p.idesc, 1);
                     }
                   }
                   acc = 1;
@@ -547,8 +560,9 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
       sc = MULTI ? seg_of(p, t, sc) : 0;
       const Tile tl = decode_tile(p, t, sc);
       const Seg &sg = p.seg[sc];
-      const int abuf = tc & 1;
-      if (!wait_bar(smem_u32(&acc_full[abuf]), (uint32_t)((tc >> 1) & 1), abort_flag, p.status, p.spin_limit))
+      const int abuf = p.nbuf == 2 ? (tc & 1) : 0;
+      if (!wait_bar(smem_u32(&acc_full[abuf]), (uint32_t)((p.nbuf == 2 ? (tc >> 1) : tc) & 1),
+                    abort_flag, p.status, p.spin_limit))
         break;
       tc_fence_after();
       // TMEM lane = output channel, column = pixel (group g = col / 8, v = col % 8)
@@ -556,8 +570,8 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
       for (int ct = 0; ct < nct; ++ct) {
         const int co = (tl.nt * p.NCT + ct) * 128 + q * 32 + lane;
         const bool co_ok = co < p.Cout;
-        const uint32_t tcol = tmem_base + ((uint32_t)(q * 32) << 16) +
-                              (uint32_t)((abuf * p.NCT + ct) * p.MH * 128);
+        const uint32_t tcol = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)abuf * p.acc_cols +
+                              (uint32_t)(ct * p.MH * 128);
         // Few instructions per store: this warp (quadrant 0) shares a
         // scheduler with the MMA issuer.  Element (u, v) of the tile is at
         // ytile + (u - u0) * du + (v - v0) * dv.  Streaming stores: the
@@ -575,15 +589,30 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
                         (long long)tl.u0 * p.ysu + (long long)tl.v0 * p.ysv) * p.ych + cy;
         const long long du = p.ysu * (long long)p.ych, dv = p.ysv * (long long)p.ych;
         const int urows = min(p.MH * 16, sg.OU - tl.u0), vcols = min(8, sg.OV - tl.v0);
-        for (int c0 = 0; c0 < p.MH * 128; c0 += 64) {
-          uint32_t r[4][16];
+        // four 16-column loads per wait; BF16X3 loads two of the hi*hi sums
+        // and the two matching cross-term sums, and adds them
+        constexpr int LD = SEP ? 2 : 4;
+        for (int c0 = 0; c0 < p.MH * 128; c0 += 16 * LD) {
+          uint32_t r[LD][16];
 #pragma unroll
-          for (int k = 0; k < 4; ++k) tmem_ld16(tcol + (uint32_t)(c0 + 16 * k), r[k]);
-          tmem_ld_wait();
+          for (int k = 0; k < LD; ++k) tmem_ld16(tcol + (uint32_t)(c0 + 16 * k), r[k]);
+          if (SEP) {
+            uint32_t r2[LD][16];
+#pragma unroll
+            for (int k = 0; k < LD; ++k) tmem_ld16(tcol + p.small_off + (uint32_t)(c0 + 16 * k), r2[k]);
+            tmem_ld_wait();
+#pragma unroll
+            for (int k = 0; k < LD; ++k)
+#pragma unroll
+              for (int e = 0; e < 16; ++e)
+                r[k][e] = __float_as_uint(__uint_as_float(r[k][e]) + __uint_as_float(r2[k][e]));
+          } else {
+            tmem_ld_wait();
+          }
           // (the next tcgen05.ld is warp-collective: no lane leaves the loop)
           if (co_ok) {
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
+            for (int k = 0; k < LD; ++k) {
 #pragma unroll
               for (int h = 0; h < 2; ++h) {
                 const int ur = (c0 + 16 * k + 8 * h) >> 3;  // u row within the tile
@@ -792,15 +821,18 @@ bool plan(TcParams &p, const View &v, int kind, int t_slot, int t_table) {
   p.BN = 128;  // output channels per tile = the MMA's M
   p.n_tiles = (v.Cout + p.BN - 1) / p.BN;
   p.T = t_slot;
-  p.NH = 2;
   const int cb0 = std::min(128, (int)((v.Cin * EB + 31) / 32 * 32));
   bool found = false;
   TcParams best = p;
   long long best_score = -1;
+  // two halo stages (staging overlaps the MMAs); one only when two do not
+  // fit shared memory (wide strided halos in split-BF16)
+  for (int nh = 2; nh >= 1 && !found; --nh)
   for (int mh = (v.OU > 16 ? 2 : 1); mh >= 1 && !found; --mh) {
     for (int cb = cb0; cb >= 32; cb -= 32) {
       if (cb != cb0 && cb % 64 != 0 && cb != 32) continue;  // try cb0, then 64, 32
       TcParams q = p;
+      q.NH = nh;
       q.MH = mh;
       // 128-pixel tiles take two co tiles when there are two: the halo is
       // staged once for both and their MMAs alternate accumulators
@@ -832,9 +864,14 @@ bool plan(TcParams &p, const View &v, int kind, int t_slot, int t_table) {
       q.b_bytes = (unsigned)(q.NCT * q.TPS) * q.tile_bytes;
       q.NB = (int)std::min<long long>(4, room / ((long long)parts * q.b_bytes));
       if (q.NB < 2) continue;
+      // accumulator sets: double-buffered when they fit TMEM (the epilogue
+      // of one tile overlaps the next tile's MMAs), else one set
+      q.small_off = (unsigned)(q.NCT * q.MH * 128);
+      q.acc_cols = q.small_off * (unsigned)parts;
+      q.nbuf = q.acc_cols * 2 <= 512 ? 2 : 1;
+      if (q.acc_cols > 512) continue;
       q.tmem_cols = 32;
-      while (q.tmem_cols < (unsigned)(2 * q.NCT * q.MH * 128)) q.tmem_cols <<= 1;
-      if (q.tmem_cols > 512) continue;
+      while (q.tmem_cols < q.acc_cols * (unsigned)q.nbuf) q.tmem_cols <<= 1;
       const long long score = (long long)q.CB * 1000 + (long long)q.TPS * (q.NCH / 2);
       if (score > best_score) {
         best_score = score;

@@ -71,6 +71,7 @@ struct WgParams {
   unsigned x_bytes, y_bytes;  // per stage, per precision part
   int NS;
   unsigned idesc, tmem_cols;
+  unsigned small_off;  // BF16X3: TMEM column of the cross-term accumulators (TG * BN)
   int vec_x, vec_y;
   // Tap groups.  ordered: group g holds taps tap_order[gstart[g] ..
   // gstart[g+1]); else group g holds taps g*TG .. min(T, (g+1)*TG) - 1.
@@ -107,6 +108,11 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const __grid_cons
   constexpr int PARTS = (KIND == K_BF16X3) ? 2 : 1;
   constexpr int XPL = 128 * EB / 16;  // planes for 128 input channels
   constexpr int KSTEP_PIX = 32 / EB;  // pixels per MMA (K = 16 bf16 / 8 tf32)
+  // BF16X3: the cross terms (hi*lo + lo*hi) accumulate apart from the hi*hi
+  // sums and are added in the epilogue.  The tensor core rounds its FP32
+  // accumulator toward zero after every MMA; with all three MMAs of a K step
+  // in one accumulator that rounding is three times that of the hi*hi sums.
+  constexpr bool SEP = (KIND == K_BF16X3);
   extern __shared__ __align__(1024) uint8_t smem[];
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -261,7 +267,16 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const __grid_cons
           for (int c0 = 0; c0 < p.BN; c0 += 16) {
             uint32_t rr[16];
             tmem_ld16(tcol + (uint32_t)c0, rr);
-            tmem_ld_wait();
+            if (SEP) {
+              uint32_t r2[16];
+              tmem_ld16(tcol + p.small_off + (uint32_t)c0, r2);
+              tmem_ld_wait();
+#pragma unroll
+              for (int e = 0; e < 16; ++e)
+                rr[e] = __float_as_uint(__uint_as_float(rr[e]) + __uint_as_float(r2[e]));
+            } else {
+              tmem_ld_wait();
+            }
             if (ci < p.Ci) {
               const int n0 = nb * p.BN + c0;
               if (p.vec_y && n0 + 16 <= p.Co && ((uintptr_t)(out + c0) % 16 == 0)) {
@@ -326,8 +341,8 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const __grid_cons
                 } else {
                   mma_bf16(dc[i], ad, bd, p.idesc, acc);
                   if (KIND == K_BF16X3) {
-                    mma_bf16(dc[i], ad, bd + (uint64_t)ylo16, p.idesc, 1);
-                    mma_bf16(dc[i], ad + (uint64_t)xlo16, bd, p.idesc, 1);
+                    mma_bf16(dc[i] + p.small_off, ad, bd + (uint64_t)ylo16, p.idesc, acc);
+                    mma_bf16(dc[i] + p.small_off, ad + (uint64_t)xlo16, bd, p.idesc, 1);
                   }
                 }
               }
@@ -341,8 +356,8 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const __grid_cons
               } else {
                 mma_bf16(d, ad, bd, p.idesc, acc);
                 if (KIND == K_BF16X3) {
-                  mma_bf16(d, ad, bd + (uint64_t)ylo16, p.idesc, 1);
-                  mma_bf16(d, ad + (uint64_t)xlo16, bd, p.idesc, 1);
+                  mma_bf16(d + p.small_off, ad, bd + (uint64_t)ylo16, p.idesc, acc);
+                  mma_bf16(d + p.small_off, ad + (uint64_t)xlo16, bd, p.idesc, 1);
                 }
               }
             }
@@ -553,7 +568,8 @@ int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, c
     return maxHP;
   };
 
-  // Plan: BN (co block), TG (taps per CTA, TG*BN <= 512 TMEM columns), NS = 2.
+  // Plan: BN (co block), TG (taps per CTA, TG*BN <= 512 TMEM columns, or
+  // 2*TG*BN with split-BF16's separate cross-term accumulators), NS = 2.
   // Tile height TU (even, so that TU*8 pixels fill whole 16-pixel K steps),
   // tried in order of estimated cost: rows staged including padding plus a
   // fixed per-tile cost of about four rows; a tile taller than the number of
@@ -583,7 +599,8 @@ int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, c
   for (int bn : {256, 128, 64, 32, 16}) {
     if (planned) break;
     p.BN = std::min(bn, (p.Co + 15) / 16 * 16);
-    const int tg_max = std::min(p.T, std::min(16, 512 / p.BN));
+    const int tg_max = std::min(p.T, std::min(16, 512 / (parts * p.BN)));
+    if (tg_max < 1) continue;
     for (int ti = 0; ti < ntu && !planned; ++ti) {
       const int tu = tus[ti];
       p.TU = tu;
@@ -610,8 +627,9 @@ int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, c
   p.v_tiles = (p.OV + 7) / 8;
   p.total_tiles = (long long)p.B * p.OW * p.u_tiles * p.v_tiles;
   p.n_nb = (p.Co + p.BN - 1) / p.BN;
+  p.small_off = (unsigned)(p.TG * p.BN);
   p.tmem_cols = 32;
-  while (p.tmem_cols < (unsigned)(p.TG * p.BN)) p.tmem_cols <<= 1;
+  while (p.tmem_cols < (unsigned)(parts * p.TG * p.BN)) p.tmem_cols <<= 1;
   // pixel ranges: enough CTAs to fill the GPU once
   const long long units = (long long)p.n_tg * p.n_nb * p.n_mb;
   const int sms = sm_count();

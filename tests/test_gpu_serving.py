@@ -7,7 +7,8 @@ Each image is computed independently by the conv and pool kernels and the
 accumulation order of a convolution does not depend on the batch, so the
 results are expected to be identical; the bound stated is 1e-6 relative
 (float32 reassociation level), far below the BF16 error against float64
-(checked separately, bound 5e-2 after 21 BF16 convolutions)."""
+(checked separately: at most 1e-2 of max|y| after 21 BF16 convolutions, the
+accuracy bar the served results are reported at)."""
 
 import numpy as np
 import pytest
@@ -69,4 +70,4 @@ def test_bf16_error_against_float64(served):
         y64 = from_dev(s64.forward(r.pixels.double().cuda()))
         errs.append(rel(r.output, y64))
     print("BF16 serving error vs float64:", max(errs))
-    assert max(errs) <= 5e-2
+    assert max(errs) <= 1e-2
