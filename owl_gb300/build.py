@@ -82,12 +82,13 @@ def build(verbose: bool = False) -> Path:
     return LIB
 
 
-def build_oracle() -> None:
-    """Build the CPU oracle (test infrastructure) and, where the reference
-    sources are present, the compiled reference stubs used to pin it."""
+def build_oracle(ref_root: str | os.PathLike | None = None) -> None:
+    """Build the CPU oracle (test infrastructure) and, when an Owl source
+    checkout is named (``ref_root``, else the OWL_REF_ROOT environment
+    variable) and present, the compiled reference stubs used to pin it."""
     subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
-    ref_root = Path(os.environ.get("OWL_REF_ROOT", "/root/reference"))
-    if (ref_root / "src" / "owl" / "core").is_dir():
+    ref_root = ref_root or os.environ.get("OWL_REF_ROOT")
+    if ref_root and (Path(ref_root) / "src" / "owl" / "core").is_dir():
         subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "ref", f"REF_ROOT={ref_root}"],
                        check=False)
 

@@ -139,9 +139,9 @@ static int invalid(const char *fn, const char *what) {
 
 // Build a ConvGeom.  `bwd` selects the backward padding rule; `rates` are
 // (cols, rows, dpts) dilation rates, all 1 for the non-dilated stubs.
-static int make_conv(const char *fn, ConvGeom &g, long B, long IC, long IR, long ID, long Ci,
-                     long KC, long KR, long KD, long OC, long OR, long OD, long Co, long sc,
-                     long sr, long sd, long dc, long dr, long dd, bool bwd, long padding) {
+int make_conv(const char *fn, ConvGeom &g, long B, long IC, long IR, long ID, long Ci, long KC,
+              long KR, long KD, long OC, long OR, long OD, long Co, long sc, long sr, long sd,
+              long dc, long dr, long dd, bool bwd, long padding) {
   if (bad_dims({B, IC, IR, ID, Ci, KC, KR, KD, OC, OR, OD, Co}))
     return invalid(fn, "negative or oversized dimension");
   if (bad_pos({sc, sr, sd})) return invalid(fn, "stride must be >= 1");

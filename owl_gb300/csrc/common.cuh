@@ -186,6 +186,15 @@ int simt_conv_bwd_kernel(Dtype dt, const ConvGeom &g, const void *x, void *dw, c
 
 // backward_kernel (float32, SIMT) with split-K partials in a caller-provided
 // workspace of ws_elems floats; splits are capped to fit it.
+// A ConvGeom from Owl stub arguments, with the argument checks every conv
+// entry point applies (dimensions 0..2^30, strides and rates 1..2^20,
+// padding 0 or 1 for forward) and the stubs' padding rules (`bwd` selects
+// the backward rule).  Sets the error message and returns kErrInvalid on a
+// bad argument.
+int make_conv(const char *fn, ConvGeom &g, long B, long IC, long IR, long ID, long Ci, long KC,
+              long KR, long KD, long OC, long OR, long OD, long Co, long sc, long sr, long sd,
+              long dc, long dr, long dd, bool bwd, long padding);
+
 int simt_conv_bwd_kernel_f32_into(const ConvGeom &g, const float *x, float *dw,
                                   const float *dy, float *ws, int64_t ws_elems,
                                   cudaStream_t s);

@@ -22,7 +22,10 @@
 // stream capture.  All calls share the array: two calls whose kernels
 // overlap on the GPU (different streams, or different host threads) race on
 // it and produce wrong results; serialise them.  Each call writes every
-// partial it later reads, so no clearing is needed between calls.
+// partial it later reads, so no clearing is needed between calls.  The
+// array's address is kept per device for the life of the process, so
+// cudaDeviceReset is not supported while this library is loaded (a reset
+// reloads the module and may move the array).
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -61,11 +64,6 @@ int noalloc_scratch(float **out) {
   return kOk;
 }
 
-int bwd_pad(long stride, long out, long k, long in) {
-  long p = (stride * (out - 1) + k - in) / 2;
-  return (int)(p < 0 ? 0 : p);
-}
-
 }  // namespace
 }  // namespace owlgpu
 
@@ -76,38 +74,32 @@ extern "C" int owlgpu_float32_ndarray_conv_spatial_backward_kernel_noalloc(
     long input_cols, long input_rows, long in_channel, long kernel_cols, long kernel_rows,
     long output_cols, long output_rows, long out_channel, long row_stride, long col_stride,
     long row_in_stride, long col_in_stride, void *stream) {
+  // As in the regular backward-kernel stub, the in-strides are unused.
   (void)row_in_stride;
   (void)col_in_stride;
   const char *fn = "conv_spatial_backward_kernel_noalloc";
-  for (long d : {batches, input_cols, input_rows, in_channel, kernel_cols, kernel_rows,
-                 output_cols, output_rows, out_channel})
-    if (d < 0 || d > (1L << 30)) {
-      set_error(std::string(fn) + ": negative or oversized dimension");
+  // the same argument checks and padding rule as the regular entry point
+  ConvGeom g;
+  int rc = make_conv(fn, g, batches, input_cols, input_rows, 1, in_channel, kernel_cols,
+                     kernel_rows, 1, output_cols, output_rows, 1, out_channel, col_stride,
+                     row_stride, 1, 1, 1, 1, true, 0);
+  if (rc) return rc;
+  // kernel elements, multiplied out only while they stay within the limit
+  // (each factor is at most 2^30, so the running product cannot overflow)
+  int64_t kernel_elems = 1;
+  for (long d : {kernel_cols, kernel_rows, in_channel, out_channel}) {
+    kernel_elems *= d;
+    if (kernel_elems > kNoallocScratchFloats) {
+      set_error(std::string(fn) + ": the kernel has more than " +
+                std::to_string(kNoallocScratchFloats) +
+                " elements, the most this entry point handles (its fixed 16 MiB device "
+                "scratch); use the allocating entry point");
       return kErrInvalid;
     }
-  if (row_stride < 1 || col_stride < 1) {
-    set_error(std::string(fn) + ": stride must be >= 1");
-    return kErrInvalid;
+    if (kernel_elems == 0) break;
   }
-  const int64_t kernel_elems = (int64_t)kernel_cols * kernel_rows * in_channel * out_channel;
-  if (kernel_elems > kNoallocScratchFloats) {
-    set_error(std::string(fn) + ": kernel has " + std::to_string(kernel_elems) +
-              " elements; this entry point handles at most " +
-              std::to_string(kNoallocScratchFloats) +
-              " (its fixed 16 MiB device scratch); use the allocating entry point");
-    return kErrInvalid;
-  }
-  ConvGeom g;
-  g.B = batches; g.IC = input_cols; g.IR = input_rows; g.ID = 1; g.Ci = in_channel;
-  g.KC = kernel_cols; g.KR = kernel_rows; g.KD = 1;
-  g.OC = output_cols; g.OR = output_rows; g.OD = 1; g.Co = out_channel;
-  g.sc = (int)col_stride; g.sr = (int)row_stride; g.sd = 1;
-  g.dc = g.dr = g.dd = 1;
-  g.pc = bwd_pad(col_stride, output_cols, kernel_cols, input_cols);
-  g.pr = bwd_pad(row_stride, output_rows, kernel_rows, input_rows);
-  g.pd = 0;
   float *ws = nullptr;
-  int rc = noalloc_scratch(&ws);
+  rc = noalloc_scratch(&ws);
   if (rc) return rc;
   return simt_conv_bwd_kernel_f32_into(g, input, kernel_grad, output_grad, ws,
                                        kNoallocScratchFloats, (cudaStream_t)stream);

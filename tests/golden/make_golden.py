@@ -1,8 +1,14 @@
 """Extract Owl's conv/pool known-answer tests into tests/golden/owl_golden.json.
 
-Run where the Owl sources are checked out:
+Run where the Owl sources are checked out, naming the checkout with --ref
+or the OWL_REF_ROOT environment variable:
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref <owl checkout>
+
+It also records, in tests/golden/owl_externals.json, the number of arguments
+of every `external` in Owl's conv, pool and upsampling bindings
+(src/owl/core/owl_ndarray_{conv,pool,upsampling}.ml), which the OCaml
+binding test checks the generated externals against.
 
 It reads the alcotest files listed in FILES, finds every
 ``let funNN () = ... verify_value <helper> <shapes..> PAD expected`` (or
@@ -19,6 +25,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import os
 import re
 from pathlib import Path
 
@@ -157,11 +164,32 @@ def parse_upsampling(path: Path) -> list[dict]:
     return cases
 
 
+EXTERNAL_FILES = ["owl_ndarray_conv.ml", "owl_ndarray_pool.ml", "owl_ndarray_upsampling.ml"]
+
+
+def external_arities(core: Path) -> dict:
+    """{external name: number of arguments} over Owl's conv/pool/upsampling
+    bindings (a leading underscore dropped, as the generated externals do)."""
+    out = {}
+    for f in EXTERNAL_FILES:
+        text = (core / f).read_text()
+        for m in re.finditer(r"external\s+(\w+)\s*:(.*?)=\s*\"", text, flags=re.S):
+            out[m.group(1).lstrip("_")] = m.group(2).count("->")
+    return dict(sorted(out.items()))
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("OWL_REF_ROOT"),
+                    help="Owl source checkout (default: $OWL_REF_ROOT)")
     ap.add_argument("--out", default=str(Path(__file__).with_name("owl_golden.json")))
     a = ap.parse_args()
+    if not a.ref:
+        ap.error("name the Owl checkout with --ref or OWL_REF_ROOT")
+    ext = external_arities(Path(a.ref) / "src" / "owl" / "core")
+    ext_out = Path(a.out).with_name("owl_externals.json")
+    ext_out.write_text(json.dumps({"source": "src/owl/core/" + ",".join(EXTERNAL_FILES),
+                                   "arities": ext}, indent=0) + "\n")
     tdir = Path(a.ref) / "test"
     cases = []
     for f in FILES:
@@ -174,7 +202,8 @@ def main() -> None:
     head = json.dumps({k: v for k, v in doc.items() if k != "cases"}, separators=(",", ":"))
     Path(a.out).write_text(head[:-1] + ',"cases":[\n' + lines + '\n],"upsampling_cases":[\n' +
                            up_lines + "\n]}\n")
-    print(f"{len(cases)} cases + {len(up)} upsampling cases -> {a.out}")
+    print(f"{len(cases)} cases + {len(up)} upsampling cases -> {a.out}; "
+          f"{len(ext)} external arities -> {ext_out}")
 
 
 if __name__ == "__main__":

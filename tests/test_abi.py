@@ -126,3 +126,29 @@ def test_every_host_entry_point_rejects_bad_arguments_without_gpu():
             args = _probe_args(params, buf, lambda a: 7 if a == "padding" else 1)
             assert getattr(L, name)(*args) == -1, name
             assert "padding" in _lib.last_error(), name
+
+
+def test_noalloc_entry_point_checks_like_the_regular_one_without_gpu():
+    """The allocation-free backward_kernel applies the regular entry point's
+    argument checks (strides 1..2^20, dimensions 0..2^30) and rejects kernels
+    beyond its fixed scratch, all before touching CUDA -- including kernels
+    whose element count would overflow a 64-bit product."""
+    import ctypes
+
+    from owl_gb300 import _lib
+
+    L = _lib.lib()
+    buf = (ctypes.c_float * 16)()
+    f = L.owlgpu_float32_ndarray_conv_spatial_backward_kernel_noalloc
+    # x, dW, dY, B, IC, IR, Ci, KC, KR, OC, OR, Co, row_s, col_s, row_in, col_in, stream
+    ok = [buf, buf, buf, 1, 2, 2, 1, 1, 1, 2, 2, 1, 1, 1, 1, 1, None]
+    for i, v in [(12, 0), (13, -1), (12, (1 << 20) + 1), (13, 1 << 40), (4, 1 << 31), (6, -2)]:
+        args = list(ok)
+        args[i] = v
+        assert f(*args) == -1, (i, v)
+        assert _lib.last_error()
+    big = list(ok)
+    big[6:9] = [1 << 30, 1 << 30, 1 << 30]  # Ci, KC, KR: 2^90 kernel elements
+    big[11] = 1 << 30
+    assert f(*big) == -1
+    assert "16 MiB" in _lib.last_error()

@@ -6,6 +6,7 @@ ints, Bigarray descriptors) releases the runtime lock around the call and
 raises Failure with the library's message on a bad argument."""
 
 import ctypes
+import json
 import re
 import subprocess
 import sys
@@ -15,7 +16,8 @@ import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
 OCAML = ROOT / "owl_gb300" / "ocaml"
-REF_CORE = Path("/root/reference/src/owl/core")
+# Owl's external arities, recorded from its sources by tests/golden/make_golden.py
+OWL_EXTERNALS = ROOT / "tests" / "golden" / "owl_externals.json"
 
 sys.path.insert(0, str(OCAML))
 
@@ -78,12 +80,9 @@ def test_externals_match_stub_arities():
         assert ours[name] == len(params), name
 
 
-@pytest.mark.skipif(not REF_CORE.exists(), reason="reference sources not on this machine")
 def test_externals_have_owls_arities():
     ours = _externals((OCAML / "owlgpu_externals.ml").read_text())
-    owl = {}
-    for f in ("owl_ndarray_conv.ml", "owl_ndarray_pool.ml", "owl_ndarray_upsampling.ml"):
-        owl.update(_externals((REF_CORE / f).read_text()))
+    owl = json.loads(OWL_EXTERNALS.read_text())["arities"]
     shared = [n for n in ours if n in owl]
     # every Owl conv/pool/upsampling external has a drop-in of the same name
     # (Owl's argmax external is spelled maxpool_argmax_spatial, as here)

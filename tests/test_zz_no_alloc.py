@@ -38,6 +38,11 @@ def _args(x, dy, w_shape, stride):
 @pytest.mark.parametrize("shape", [
     ((4, 20, 20, 32), (3, 3, 32, 48), (1, 1)),
     ((2, 15, 15, 64), (3, 3, 64, 128), (2, 2)),
+    # a wide kernel over few pixels: the split count the pixels would allow
+    # (4) is cut to the 3 partials of 1,179,648 elements that fit the scratch
+    ((1, 16, 16, 256), (3, 3, 256, 512), (1, 1)),
+    # exactly the element limit: one split, written straight into dW
+    ((1, 8, 8, 512), (4, 4, 512, 512), (1, 1)),
 ])
 def test_noalloc_matches_allocating_entry_point(gpu_lib, shape):
     import torch
@@ -83,4 +88,4 @@ def test_noalloc_rejects_kernels_beyond_its_scratch(gpu_lib):
         x.data_ptr(), x.data_ptr(), x.data_ptr(), 1, 4, 4, 1024, 3, 3, 4, 4, 1024, 1, 1, 1, 1,
         torch.cuda.current_stream().cuda_stream)
     assert rc == -1
-    assert "at most" in _lib.last_error()
+    assert "16 MiB" in _lib.last_error()
