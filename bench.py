@@ -673,9 +673,11 @@ def bench_algodiff(precision: str, steps: int = 10):
             del g
         except Exception as e:  # report, never lose the bench line
             out[prec]["graph"] = {"error": f"{type(e).__name__}: {e}"[:200]}
-    out["note"] = ("batch 256; conv/pool through libowlgpu, dense layers and softmax in torch "
-                   "(cuBLAS); gradients checked against float64 finite differences and the "
-                   "oracle in tests/test_gpu_algodiff.py")
+    out["note"] = ("batch 256; every kernel of the step is libowlgpu's: conv + bias + ReLU "
+                   "(epilogue-fused), pools, the dense layers' GEMM (tcgen05 at BF16), the "
+                   "bias/ReLU backward, softmax cross-entropy and the SGD update; gradients "
+                   "checked against float64 finite differences and the oracle in "
+                   "tests/test_gpu_algodiff.py")
     return out
 
 

@@ -1699,6 +1699,106 @@ int owl_complex64_ndarray_conv_cuboid_backward_kernel_naive(
     long col_stride);
 
 /* ======================================================================
+ * Extensions: the layers around the convolutions.  No counterpart among
+ * Owl's C stubs: in Owl these are OCaml compositions of ndarray operations
+ * inside the neural-network layers (src/base/neural/owl_neural_neuron.ml)
+ * and the optimiser (src/base/optimise/owl_optimise_generic.ml).  They let
+ * a training or serving step stay on the device in this library's own
+ * kernels.  Device pointers, asynchronous on `stream`; every reduction sums
+ * in a fixed order, so results repeat bit for bit.
+ * ====================================================================== */
+
+#define OWLGPU_ACT_NONE 0
+#define OWLGPU_ACT_RELU 1 /* x > 0 ? x : 0, Owl's Activation Relu */
+
+/* Conv2D / Conv3D neuron forward with its bias and activation:
+ * output = act(conv(input, kernel) + bias[out_channel]), as Conv2D.run
+ * (owl_neural_neuron.ml:1253, conv2d x w s + b) followed by an Activation
+ * neuron.  Arguments of owlgpu_<kind>_ndarray_conv_spatial /
+ * _conv_cuboid_im2col, then `bias` (out_channel values, or NULL for none)
+ * and `act`.  On the tensor cores the bias and activation are applied in
+ * the convolution's epilogue; the CUDA-core kernels apply them in a second
+ * pass. */
+int owlgpu_float32_ndarray_conv_spatial_bias_act(
+    const float *input, const float *kernel, float *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride, const float *bias, int act OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_ndarray_conv_spatial_bias_act(
+    const double *input, const double *kernel, double *output, long batches,
+    long input_cols, long input_rows, long in_channel, long kernel_cols,
+    long kernel_rows, long output_cols, long output_rows, long out_channel,
+    long row_stride, long col_stride, long padding, long row_in_stride,
+    long col_in_stride, const double *bias, int act OWLGPU_DEVICE_ARGS);
+int owlgpu_float32_ndarray_conv_cuboid_bias_act(
+    const float *input, const float *kernel, float *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long padding, const float *bias,
+    int act OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_ndarray_conv_cuboid_bias_act(
+    const double *input, const double *kernel, double *output, long batches,
+    long input_cols, long input_rows, long input_dpts, long in_channel,
+    long kernel_cols, long kernel_rows, long kernel_dpts, long output_cols,
+    long output_rows, long output_dpts, long out_channel, long dpt_stride,
+    long row_stride, long col_stride, long padding, const double *bias,
+    int act OWLGPU_DEVICE_ARGS);
+
+/* Backward of output = act(z + bias): pre_grad = output_grad * act'(z),
+ * read from the layer's output (for ReLU, output > 0 exactly where z > 0),
+ * and bias_grad[c] = the sum over pixels of pre_grad[p][c].  Arrays are
+ * [pixels][channels]; pre_grad may alias output_grad; pre_grad or bias_grad
+ * may be NULL (not written).  The backward of Owl's bias add and Relu
+ * (owl_algodiff_ops.ml: add's adjoint summed over the broadcast axes,
+ * relu's adjoint masked by x > 0). */
+int owlgpu_float32_bias_act_backward(const float *output, const float *output_grad,
+                                     float *pre_grad, float *bias_grad, long pixels,
+                                     long channels, int act, void *stream);
+int owlgpu_float64_bias_act_backward(const double *output, const double *output_grad,
+                                     double *pre_grad, double *bias_grad, long pixels,
+                                     long channels, int act, void *stream);
+
+/* The dense layer's matrix product and the two products of its backward
+ * pass (FullyConnected.run, owl_neural_neuron.ml:1907: (x *@ w) + b; Owl's
+ * `dot` is cblas_?gemm): c[m][n] = act(sum over k of op(a)[m][k] op(b)[k][n]
+ * + bias[n]), row-major.  op(a) = a stored [m][k], or with trans_a its
+ * transpose (a stored [k][m]); op(b) = b stored [k][n], or with trans_b its
+ * transpose (b stored [n][k]).  Both transposed is rejected.  bias: n
+ * values or NULL.  float32 at BF16 / BF16X3 runs the tcgen05 GEMM (split-K,
+ * partials summed in order); FP32 / TF32 and float64 run the CUDA-core
+ * kernels (precision is ignored for float64). */
+int owlgpu_float32_dot(const float *a, const float *b, float *c, long m, long n, long k,
+                       int trans_a, int trans_b, const float *bias,
+                       int act OWLGPU_DEVICE_ARGS);
+int owlgpu_float64_dot(const double *a, const double *b, double *c, long m, long n, long k,
+                       int trans_a, int trans_b, const double *bias,
+                       int act OWLGPU_DEVICE_ARGS);
+
+/* Softmax cross-entropy of a classifier's training step: loss = -sum over
+ * rows and classes of labels * log softmax(logits), divided by rows (Owl's
+ * Loss Cross_entropy, owl_optimise_generic.ml:172, cross_entropy
+ * owl_algodiff_ops.ml:1392, softmax :918-922, and the batch mean of
+ * owl_optimise_generic.ml:646-649); dlogits = (softmax(logits) - labels) *
+ * dloss / rows.  logits, labels, dlogits: [rows][classes]; loss: one value;
+ * dloss: the loss's adjoint on the device (one value) or NULL for 1;
+ * loss or dlogits may be NULL (not written). */
+int owlgpu_float32_softmax_cross_entropy(const float *logits, const float *labels,
+                                         float *loss, float *dlogits, const float *dloss,
+                                         long rows, long classes, void *stream);
+int owlgpu_float64_softmax_cross_entropy(const double *logits, const double *labels,
+                                         double *loss, double *dlogits, const double *dloss,
+                                         long rows, long classes, void *stream);
+
+/* Gradient-descent update weight -= lr * grad over n elements (Owl's
+ * optimiser with a constant learning rate and no momentum). */
+int owlgpu_float32_sgd_update(float *weight, const float *grad, long n, double lr,
+                              void *stream);
+int owlgpu_float64_sgd_update(double *weight, const double *grad, long n, double lr,
+                              void *stream);
+
+/* ======================================================================
  * Allocation-free entry point.  No counterpart in the reference: Owl's C
  * stubs allocate their own scratch with malloc.  This is the float32 2-D
  * conv backward_kernel (same arguments and results as

@@ -55,7 +55,7 @@ def _ctype(t: str):
         return ctypes.c_void_p
     t = t.replace("const", "").strip()
     return {"long": ctypes.c_long, "long long": ctypes.c_longlong, "int": ctypes.c_int,
-            "uint64_t": ctypes.c_uint64}[t]
+            "uint64_t": ctypes.c_uint64, "double": ctypes.c_double}[t]
 
 
 RESTYPE = {"int": ctypes.c_int, "long long": ctypes.c_longlong, "uint64_t": ctypes.c_uint64,

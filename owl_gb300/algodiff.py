@@ -35,6 +35,7 @@ import numpy as np
 
 from .dense import NN as _NN
 from .dense import SAME
+from .layers import ACT_NONE, ACT_RELU, Layers
 
 # ---- array helpers (numpy for the oracle, torch for the GPU) ----------------
 
@@ -296,10 +297,71 @@ class Maths:
 
 class _NNOps:
     """Owl's ``Algodiff.NN`` conv/pool functions bound to one stub provider
-    (owl_algodiff_ops.ml:2260-2900)."""
+    (owl_algodiff_ops.ml:2260-2900), and the layers around them
+    (:mod:`owl_gb300.layers`) as differentiable ops."""
 
     def __init__(self, g: _NN):
         self.g = g
+        self.layers = Layers(g)
+
+    # ---- layers (owl_neural_neuron.ml), each one tape node -------------------
+
+    def conv2d_bias_act(self, a, w, b, s, padding=SAME, act=ACT_RELU):
+        """act(conv2d a w s + b): Owl's Conv2D neuron (owl_neural_neuron.ml:1253)
+        and the Activation after it, one fused forward.  Reverse: the ReLU
+        mask and bias gradient in one pass, then the convolution's
+        backward_input / backward_kernel on the masked adjoint."""
+        L, g = self.layers, self.g
+        ap, wp, bp = primal(a), primal(w), primal(b)
+        cp = L.conv2d_bias_act(ap, wp, bp, s, padding, act)
+        if not (_tracked(a) or _tracked(w) or _tracked(b)):
+            return cp
+
+        def back(ca):
+            dz, db = L.bias_act_backward(cp, ca, act, bias_grad=_tracked(b))
+            dx = g.conv2d_backward_input(ap, wp, s, dz) if _tracked(a) else None
+            dw = g.conv2d_backward_kernel(ap, wp, s, dz) if _tracked(w) else None
+            return dx, dw, db
+
+        return Node(cp, (a, w, b), back, "conv2d_bias_act")
+
+    def fully_connected(self, a, w, b, act=ACT_NONE):
+        """act(a *@ w + b): Owl's FullyConnected neuron (owl_neural_neuron.ml:1907)
+        with an optional ReLU, on the library's GEMM.  Reverse: dz = the
+        activation-masked adjoint, da = dz w^T, dw = a^T dz, db = sum of dz."""
+        L = self.layers
+        ap, wp, bp = primal(a), primal(w), primal(b)
+        cp = L.dot(ap, wp, bias=bp, act=act)
+        if not (_tracked(a) or _tracked(w) or _tracked(b)):
+            return cp
+
+        def back(ca):
+            if act == ACT_NONE and not _tracked(b):
+                dz, db = ca, None
+            else:
+                dz, db = L.bias_act_backward(cp, ca, act, bias_grad=_tracked(b))
+            da = L.dot(dz, wp, trans_b=True) if _tracked(a) else None
+            dw = L.dot(ap, dz, trans_a=True) if _tracked(w) else None
+            return da, dw, db
+
+        return Node(cp, (a, w, b), back, "fully_connected")
+
+    def softmax_cross_entropy(self, logits, labels):
+        """Batch-mean cross-entropy of softmax(logits) against `labels`
+        (owl_optimise_generic.ml:172 and :646-649); reverse: (softmax -
+        labels) * adjoint / batch."""
+        L = self.layers
+        zp = primal(logits)
+        loss, _ = L.softmax_cross_entropy(zp, labels, want_loss=True)
+        if not _tracked(logits):
+            return loss
+
+        def back(g):
+            _, dz = L.softmax_cross_entropy(zp, labels, dloss=g, want_loss=False,
+                                            want_grad=True)
+            return (dz,)
+
+        return Node(loss, (logits,), back, "softmax_cross_entropy")
 
     # conv family: ff_bb = forward stub, dr_a = backward_input, dr_b = backward_kernel
     def _conv(self, label, fwd, bwd_i, bwd_k, a, b):
@@ -421,6 +483,7 @@ class Algodiff:
     def __init__(self, nn: _NN):
         self.nn = nn
         self.NN = _NNOps(nn)
+        self._one = {}
         self.Maths = Maths
         self.make_reverse = make_reverse
         self.reverse_prop = reverse_prop
@@ -483,9 +546,25 @@ def init_mnist_cnn(seed: int = 0, dtype=np.float32) -> dict:
 
 
 def mnist_cnn_loss(ad: Algodiff, p: dict, x, onehot):
-    """conv 5x5x1x32 SAME, ReLU, max_pool 2x2, conv 5x5x32x64 SAME, ReLU,
-    max_pool 2x2, dense 3136->1024 ReLU, dense 1024->10, softmax
-    cross-entropy (mean over the batch)."""
+    """conv 5x5x1x32 SAME + bias, ReLU, max_pool 2x2, conv 5x5x32x64 SAME +
+    bias, ReLU, max_pool 2x2, dense 3136->1024 + bias, ReLU, dense 1024->10 +
+    bias, softmax cross-entropy (mean over the batch).  Each conv + bias +
+    ReLU and each dense layer is one fused op of the library."""
+    M, N = ad.Maths, ad.NN
+    h = N.conv2d_bias_act(x, p["w1"], p["b1"], [1, 1], SAME, ACT_RELU)
+    h = N.max_pool2d(SAME, h, [2, 2], [2, 2])
+    h = N.conv2d_bias_act(h, p["w2"], p["b2"], [1, 1], SAME, ACT_RELU)
+    h = N.max_pool2d(SAME, h, [2, 2], [2, 2])
+    h = M.reshape(h, (primal(h).shape[0], 3136))
+    h = N.fully_connected(h, p["w3"], p["b3"], ACT_RELU)
+    z = N.fully_connected(h, p["w4"], p["b4"], ACT_NONE)
+    return N.softmax_cross_entropy(z, onehot)
+
+
+def mnist_cnn_loss_composed(ad: Algodiff, p: dict, x, onehot):
+    """The same network from Owl's separate operations (conv2d, add, relu,
+    dot, softmax cross-entropy), as Owl's neurons compose them: the
+    reference the fused ops are checked against."""
     M, N = ad.Maths, ad.NN
     h = M.relu(M.add(N.conv2d(x, p["w1"], [1, 1], SAME), p["b1"]))
     h = N.max_pool2d(SAME, h, [2, 2], [2, 2])
@@ -497,17 +576,30 @@ def mnist_cnn_loss(ad: Algodiff, p: dict, x, onehot):
     return M.softmax_cross_entropy(z, onehot)
 
 
+def _seed(ad: Algodiff, loss):
+    """The loss adjoint 1.  On the device: one cached value, so that a
+    captured step launches no fill kernel."""
+    if ad.NN.layers.gpu and _is_torch(loss):
+        key = (loss.dtype, loss.device)
+        one = ad._one.get(key)
+        if one is None:
+            one = ad._one[key] = _ones_like(loss)
+        return one
+    return _ones_like(loss)
+
+
 def loss_and_grads(ad: Algodiff, params: dict, x, onehot, model=mnist_cnn_loss):
     """One reverse sweep: (loss value, {name: gradient})."""
     nodes = {k: make_reverse(v, k) for k, v in params.items()}
     loss = model(ad, nodes, x, onehot)
-    reverse_prop(_ones_like(loss.p), loss)
+    reverse_prop(_seed(ad, loss.p), loss)
     return loss.p, {k: n.adj for k, n in nodes.items()}
 
 
 def sgd_step(ad: Algodiff, params: dict, x, onehot, lr: float = 0.01, model=mnist_cnn_loss):
-    """A training step: loss, gradients, and in-place SGD update."""
+    """A training step: loss, gradients, and in-place SGD update (the
+    library's update kernel on the device)."""
     loss, grads = loss_and_grads(ad, params, x, onehot, model)
     for k, g in grads.items():
-        params[k] -= lr * g
+        ad.NN.layers.sgd_update(params[k], g, lr)
     return loss, grads

@@ -70,16 +70,19 @@ static thread_local int t_last_path = -1;
 // otherwise it runs on the FP32 CUDA-core kernels, which are at least as
 // accurate.  The path taken is visible through owlgpu_last_conv_path().
 int conv_fwd(Dtype dt, int prec, const ConvGeom &g, const void *x, const void *w, void *y,
-             cudaStream_t s) {
+             cudaStream_t s, const void *bias, int act) {
   if (tc_requested(dt, prec)) {
-    int rc = tc_conv_fwd(prec, g, (const float *)x, (const float *)w, (float *)y, s);
+    int rc = tc_conv_fwd(prec, g, (const float *)x, (const float *)w, (float *)y, s,
+                         (const float *)bias, act);
     if (rc != kErrUnsupported) {
       t_last_path = 1;
       return rc;
     }
   }
   t_last_path = 0;
-  return simt_conv_fwd(dt, g, x, w, y, s);
+  int rc = simt_conv_fwd(dt, g, x, w, y, s);
+  if (rc || (!bias && act == OWLGPU_ACT_NONE)) return rc;
+  return bias_act_inplace(dt, y, bias, g.y_elems(), g.Co, act, s);
 }
 
 int conv_bwd_input(Dtype dt, int prec, const ConvGeom &g, void *dx, const void *w,
@@ -1101,5 +1104,48 @@ UPSAMPLE(float32, float)
 UPSAMPLE(float64, double)
 UPSAMPLE(complex32, owlgpu_complex32)
 UPSAMPLE(complex64, owlgpu_complex64)
+
+// ---- forward convolution with bias and activation (Conv2D / Conv3D neuron
+// followed by an Activation neuron), no Owl stub ---------------------------
+
+#define CONV_BIAS_ACT(KIND, T)                                                                  \
+  int owlgpu_##KIND##_ndarray_conv_spatial_bias_act(                                           \
+      const T *input, const T *kernel, T *output, long batches, long input_cols,               \
+      long input_rows, long in_channel, long kernel_cols, long kernel_rows, long output_cols,   \
+      long output_rows, long out_channel, long row_stride, long col_stride, long padding,      \
+      long row_in_stride, long col_in_stride, const T *bias, int act, int precision,           \
+      void *stream) {                                                                          \
+    (void)row_in_stride;                                                                       \
+    (void)col_in_stride;                                                                       \
+    ConvGeom g;                                                                                \
+    int rc = make_conv("conv_spatial_bias_act", g, batches, input_cols, input_rows, 1,        \
+                       in_channel, kernel_cols, kernel_rows, 1, output_cols, output_rows, 1,   \
+                       out_channel, col_stride, row_stride, 1, 1, 1, 1, false, padding);       \
+    if (rc) return rc;                                                                         \
+    if (act != OWLGPU_ACT_NONE && act != OWLGPU_ACT_RELU)                                      \
+      return invalid("conv_spatial_bias_act", "unknown activation");                          \
+    return conv_fwd(dtype_of<T>(), precision, g, input, kernel, output, (cudaStream_t)stream, \
+                    bias, act);                                                                \
+  }                                                                                            \
+  int owlgpu_##KIND##_ndarray_conv_cuboid_bias_act(                                            \
+      const T *input, const T *kernel, T *output, long batches, long input_cols,               \
+      long input_rows, long input_dpts, long in_channel, long kernel_cols, long kernel_rows,   \
+      long kernel_dpts, long output_cols, long output_rows, long output_dpts,                  \
+      long out_channel, long dpt_stride, long row_stride, long col_stride, long padding,       \
+      const T *bias, int act, int precision, void *stream) {                                   \
+    ConvGeom g;                                                                                \
+    int rc = make_conv("conv_cuboid_bias_act", g, batches, input_cols, input_rows, input_dpts,\
+                       in_channel, kernel_cols, kernel_rows, kernel_dpts, output_cols,         \
+                       output_rows, output_dpts, out_channel, col_stride, row_stride,          \
+                       dpt_stride, 1, 1, 1, false, padding);                                   \
+    if (rc) return rc;                                                                         \
+    if (act != OWLGPU_ACT_NONE && act != OWLGPU_ACT_RELU)                                      \
+      return invalid("conv_cuboid_bias_act", "unknown activation");                           \
+    return conv_fwd(dtype_of<T>(), precision, g, input, kernel, output, (cudaStream_t)stream, \
+                    bias, act);                                                                \
+  }
+
+CONV_BIAS_ACT(float32, float)
+CONV_BIAS_ACT(float64, double)
 
 }  // extern "C"

@@ -159,8 +159,14 @@ int scratch_alloc(void **p, size_t bytes, cudaStream_t s);
 void scratch_free(void *p, cudaStream_t s);
 
 // ---- compute entry points (device pointers, asynchronous) --------------
+// Forward convolution; with `bias` (per output channel, or null) and `act`
+// (OWLGPU_ACT_*), y = act(conv + bias): in the tensor-core epilogue, or by a
+// second pass after the CUDA-core kernel.
 int conv_fwd(Dtype dt, int prec, const ConvGeom &g, const void *x, const void *w, void *y,
-             cudaStream_t s);
+             cudaStream_t s, const void *bias = nullptr, int act = 0);
+// y[i] = act(y[i] + bias[i % C]) over n elements (real kinds).
+int bias_act_inplace(Dtype dt, void *y, const void *bias, long long n, long long C, int act,
+                     cudaStream_t s);
 int conv_bwd_input(Dtype dt, int prec, const ConvGeom &g, void *dx, const void *w,
                    const void *dy, cudaStream_t s);
 int conv_bwd_kernel(Dtype dt, int prec, const ConvGeom &g, const void *x, void *dw,
@@ -184,6 +190,12 @@ int simt_conv_bwd_input(Dtype dt, const ConvGeom &g, void *dx, const void *w, co
 int simt_conv_bwd_kernel(Dtype dt, const ConvGeom &g, const void *x, void *dw, const void *dy,
                          cudaStream_t s);
 
+// A pass of a 1x1 geometry on the CUDA cores as a split-K GEMM (partials
+// summed in order): mode 0 forward (a = x, b = w, c = y), 1 backward_input
+// (a = dy, b = w, c = dx), 2 backward_kernel (a = x, b = dy, c = dw).
+int simt_gemm(Dtype dt, int mode, const ConvGeom &g, const void *a, const void *b, void *c,
+              cudaStream_t s);
+
 // backward_kernel (float32, SIMT) with split-K partials in a caller-provided
 // workspace of ws_elems floats; splits are capped to fit it.
 // A ConvGeom from Owl stub arguments, with the argument checks every conv
@@ -203,7 +215,7 @@ int simt_conv_bwd_kernel_f32_into(const ConvGeom &g, const float *x, float *dw,
 // kErrUnsupported when a geometry is outside what the kernels handle, in
 // which case the caller reports the error (there is no silent fallback).
 int tc_conv_fwd(int prec, const ConvGeom &g, const float *x, const float *w, float *y,
-                cudaStream_t s);
+                cudaStream_t s, const float *bias = nullptr, int act = 0);
 int tc_conv_bwd_input(int prec, const ConvGeom &g, float *dx, const float *w, const float *dy,
                       cudaStream_t s);
 int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, const float *dy,
@@ -218,6 +230,7 @@ long long set_wait_limit(long long cycles);
 // Read (and clear) the tensor-core kernels' device error word on stream s.
 int tc_read_status(int *out, cudaStream_t s);
 int *tc_wgrad_status_word();  // device address of the weight-gradient kernel's status word
+int *tc_gemm_status_word();   // device address of the tensor-core GEMM's status word
 // out[i] = sum over r = 0 .. R-1 of part[r * n + i], in that order.
 int sum_partials_f32(const float *part, float *out, long long n, int R, cudaStream_t s);
 // The calling thread launched a tensor-core kernel (whose watchdog status the

@@ -278,7 +278,8 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
   }
 
   // ---- epilogue --------------------------------------------------------
-  T *Cz = C + (MODE == BWDK ? (int64_t)blockIdx.z * g.M * g.N : 0);
+  // split z of a split-K launch writes its own partial (z = 0 otherwise)
+  T *Cz = C + (int64_t)blockIdx.z * g.M * g.N;
 #pragma unroll
   for (int i = 0; i < TM; ++i) {
     int64_t m = m0 + ty * TM + i;
@@ -373,15 +374,18 @@ int bwdi_t(const ConvGeom &g, T *dx, const T *w, const T *dy, cudaStream_t s) {
   return launch_any<T, BWDI>(d, dy, w, dx, 1, d.K, s);
 }
 
-template <typename T>
-int bwdk_t(const ConvGeom &g, const T *x, T *dw, const T *dy, cudaStream_t s) {
-  Dev d = make_dev(g, BWDK);
+// The GEMM view of one pass with its reduction split across CTAs: each
+// split writes a partial, summed in split order by a second kernel
+// (deterministic).  A/B are the pass's operands in launch_any's order.
+template <typename T, int MODE>
+int splitk_t(const ConvGeom &g, const T *A, const T *B, T *C, cudaStream_t s) {
+  Dev d = make_dev(g, MODE);
   if (d.M == 0 || d.N == 0) return kOk;
   if (d.K == 0) {
-    OWL_CUDA(cudaMemsetAsync(dw, 0, sizeof(T) * d.M * d.N, s));
+    OWL_CUDA(cudaMemsetAsync(C, 0, sizeof(T) * d.M * d.N, s));
     return kOk;
   }
-  // Split the pixel reduction so that ~4 waves of CTAs cover 152 SMs, with
+  // Split the reduction so that ~4 waves of CTAs cover 152 SMs, with
   // each split at least 8 K-tiles deep.
   int64_t tiles = ceil_div(d.M, tile_m<T>(d)) * ceil_div(d.N, tile_n<T>(d));
   int64_t want = ceil_div(4 * 152, tiles);
@@ -389,22 +393,27 @@ int bwdk_t(const ConvGeom &g, const T *x, T *dw, const T *dy, cudaStream_t s) {
   int splits = (int)std::max<int64_t>(1, std::min<int64_t>(want, std::min<int64_t>(max_by_k, 256)));
   int64_t kps = ceil_div(ceil_div(d.K, splits), 8) * 8;
   splits = (int)ceil_div(d.K, kps);
-  if (splits == 1) return launch_any<T, BWDK>(d, x, dy, dw, 1, kps, s);
+  if (splits == 1) return launch_any<T, MODE>(d, A, B, C, 1, kps, s);
   void *ws = nullptr;
   size_t bytes = sizeof(T) * (size_t)splits * d.M * d.N;
   int rc = scratch_alloc(&ws, bytes, s);
   if (rc) return rc;
-  rc = launch_any<T, BWDK>(d, x, dy, (T *)ws, splits, kps, s);
+  rc = launch_any<T, MODE>(d, A, B, (T *)ws, splits, kps, s);
   if (rc == kOk) {
     int64_t n = d.M * d.N;
     int blocks = (int)std::min<int64_t>(ceil_div(n, 256), 4 * 152);
-    splitk_reduce_kernel<T><<<blocks, 256, 0, s>>>((const T *)ws, dw, n, splits);
+    splitk_reduce_kernel<T><<<blocks, 256, 0, s>>>((const T *)ws, C, n, splits);
     cudaError_t e = cudaGetLastError();
     note_launch();
     if (e != cudaSuccess) rc = cuda_fail(e, "splitk_reduce_kernel");
   }
   scratch_free(ws, s);
   return rc;
+}
+
+template <typename T>
+int bwdk_t(const ConvGeom &g, const T *x, T *dw, const T *dy, cudaStream_t s) {
+  return splitk_t<T, BWDK>(g, x, dy, dw, s);
 }
 
 // backward_kernel, float32, with the split-K partials written into a
@@ -473,6 +482,23 @@ int simt_conv_bwd_input(Dtype dt, const ConvGeom &g, void *dx, const void *w, co
   return by_dtype(dt, [&](auto *tag) {
     using T = std::remove_pointer_t<decltype(tag)>;
     return bwdi_t<T>(g, (T *)dx, (const T *)w, (const T *)dy, s);
+  });
+}
+
+// A pass of a 1x1 geometry as a split-K GEMM (the dense layer's products on
+// the CUDA cores): mode 0 forward (a = x, b = w, c = y), 1 backward_input
+// (a = dy, b = w, c = dx), 2 backward_kernel (a = x, b = dy, c = dw).
+int simt_gemm(Dtype dt, int mode, const ConvGeom &g, const void *a, const void *b, void *c,
+              cudaStream_t s) {
+  if (dt != F32 && dt != F64) {
+    set_error("simt_gemm: real element kinds only");
+    return kErrInvalid;
+  }
+  return by_dtype(dt, [&](auto *tag) {
+    using T = std::remove_pointer_t<decltype(tag)>;
+    if (mode == FWD) return splitk_t<T, FWD>(g, (const T *)a, (const T *)b, (T *)c, s);
+    if (mode == BWDI) return splitk_t<T, BWDI>(g, (const T *)a, (const T *)b, (T *)c, s);
+    return splitk_t<T, BWDK>(g, (const T *)a, (const T *)b, (T *)c, s);
   });
 }
 

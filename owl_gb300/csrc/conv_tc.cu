@@ -120,6 +120,10 @@ struct TcParams {
   // (a depth-to-space epilogue; one staged input tile serves all classes).
   int ych, fuse_n;
   long long fuse_yoff[kMaxSeg];
+  // forward only: y = act(conv + bias[co]) in the epilogue (bias may be
+  // null; act OWLGPU_ACT_NONE or OWLGPU_ACT_RELU)
+  const float *bias;
+  int act;
   long long spin_limit;  // cycles a pipeline wait polls before the CTA gives up
 };
 
@@ -577,6 +581,8 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
         // ytile + (u - u0) * du + (v - v0) * dv.  Streaming stores: the
         // output is not read again here, so it should not displace the
         // input halo lines the producers still read from L2.
+        const float bco = (p.bias && co_ok) ? __ldg(p.bias + co) : 0.f;
+        const bool epi = p.bias != nullptr || p.act != 0;
         int cy = co;
         long long yo = sg.yoff;
         if (p.fuse_n > 0) {
@@ -608,6 +614,16 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
                 r[k][e] = __float_as_uint(__uint_as_float(r[k][e]) + __uint_as_float(r2[k][e]));
           } else {
             tmem_ld_wait();
+          }
+          if (epi) {
+#pragma unroll
+            for (int k = 0; k < LD; ++k)
+#pragma unroll
+              for (int e = 0; e < 16; ++e) {
+                float v = __uint_as_float(r[k][e]) + bco;
+                if (p.act == OWLGPU_ACT_RELU) v = v > 0.f ? v : 0.f;
+                r[k][e] = __float_as_uint(v);
+              }
           }
           // (the next tcgen05.ld is warp-collective: no lane leaves the loop)
           if (co_ok) {
@@ -932,7 +948,8 @@ struct SegSpec {
 // extents and pads; they run as a single segment with fuse * nseg output
 // channels and a depth-to-space epilogue (sp[0].v.Cout must be fuse).
 int run_segs(int prec, int nseg_in, const SegSpec *sp, bool bwd_input, int Ci, int Co,
-             const float *x, const float *w, float *y, cudaStream_t s, int fuse = 0) {
+             const float *x, const float *w, float *y, cudaStream_t s, int fuse = 0,
+             const float *bias = nullptr, int act = 0) {
   const int kind = prec == OWLGPU_PREC_TF32 ? K_TF32 : (prec == OWLGPU_PREC_BF16X3 ? K_BF16X3 : K_BF16);
   // segments with work, and the union of their halo extents
   int idx[kMaxSeg], nseg = 0, spw = 0, spu = 0, spv = 0, t_slot = 0, t_table = 0;
@@ -974,6 +991,8 @@ int run_segs(int prec, int nseg_in, const SegSpec *sp, bool bwd_input, int Ci, i
   p.Cin = pv.Cin; p.Cout = pv.Cout;
   p.ych = fuse_n ? fuse_n : pv.Cout;
   p.fuse_n = fuse_n;
+  p.bias = bias;
+  p.act = act;
   for (int k = 0; k < kMaxSeg; ++k) p.fuse_yoff[k] = fuse_yoff[k];
   p.nseg = nseg;
   long long tiles = 0;
@@ -1061,15 +1080,16 @@ int run_segs(int prec, int nseg_in, const SegSpec *sp, bool bwd_input, int Ci, i
 }
 
 int run_view(int prec, const View &v, const TapMap &tm, bool bwd_input, int Ci, int Co,
-             const float *x, const float *w, float *y, cudaStream_t s) {
+             const float *x, const float *w, float *y, cudaStream_t s,
+             const float *bias = nullptr, int act = 0) {
   SegSpec sp{v, tm, 0};
-  return run_segs(prec, 1, &sp, bwd_input, Ci, Co, x, w, y, s);
+  return run_segs(prec, 1, &sp, bwd_input, Ci, Co, x, w, y, s, 0, bias, act);
 }
 
 // The whole kernel over a geometry: forward, or stride-1 backward-input
 // (a forward convolution of dY with the flipped, channel-exchanged kernel).
 int run(int prec, const ConvGeom &g, bool bwd_input, const float *x, const float *w, float *y,
-        cudaStream_t s) {
+        cudaStream_t s, const float *bias = nullptr, int act = 0) {
   if (bwd_input && (g.sc != 1 || g.sr != 1 || g.sd != 1)) return kErrUnsupported;
   if (g.sc > 8 || g.sr > 8 || g.sd > 8) return kErrUnsupported;
   const View v = make_view(g, bwd_input);
@@ -1081,7 +1101,7 @@ int run(int prec, const ConvGeom &g, bool bwd_input, const float *x, const float
     tm.base[a] = bwd_input ? KO[a] - 1 : 0;
     tm.mul[a] = bwd_input ? -1 : 1;
   }
-  return run_view(prec, v, tm, bwd_input, (int)g.Ci, (int)g.Co, x, w, y, s);
+  return run_view(prec, v, tm, bwd_input, (int)g.Ci, (int)g.Co, x, w, y, s, bias, act);
 }
 
 // Strided backward-input by residue classes.  With forward x index
@@ -1190,8 +1210,8 @@ int run_bwd_input_strided(int prec, const ConvGeom &g, float *dx, const float *w
 }  // namespace
 
 int tc_conv_fwd(int prec, const ConvGeom &g, const float *x, const float *w, float *y,
-                cudaStream_t s) {
-  return run(prec, g, false, x, w, y, s);
+                cudaStream_t s, const float *bias, int act) {
+  return run(prec, g, false, x, w, y, s, bias, act);
 }
 
 int tc_conv_bwd_input(int prec, const ConvGeom &g, float *dx, const float *w, const float *dy,
@@ -1201,18 +1221,18 @@ int tc_conv_bwd_input(int prec, const ConvGeom &g, float *dx, const float *w, co
   return run_bwd_input_strided(prec, g, dx, w, dy, s);
 }
 
-// Both tensor-core kernels' status words, read with one synchronisation and
-// cleared when set.
+// The tensor-core kernels' status words (convolution, weight gradient,
+// GEMM), read with one synchronisation and cleared when set.
 int tc_read_status(int *out, cudaStream_t s) {
-  int *p = status_ptr(), *pw = tc_wgrad_status_word();
-  if (!p || !pw) return kErrCuda;
-  int v[2] = {0, 0};
-  OWL_CUDA(cudaMemcpyAsync(&v[0], p, sizeof(int), cudaMemcpyDeviceToHost, s));
-  OWL_CUDA(cudaMemcpyAsync(&v[1], pw, sizeof(int), cudaMemcpyDeviceToHost, s));
+  int *w[3] = {status_ptr(), tc_wgrad_status_word(), tc_gemm_status_word()};
+  if (!w[0] || !w[1] || !w[2]) return kErrCuda;
+  int v[3] = {0, 0, 0};
+  for (int i = 0; i < 3; ++i)
+    OWL_CUDA(cudaMemcpyAsync(&v[i], w[i], sizeof(int), cudaMemcpyDeviceToHost, s));
   OWL_CUDA(cudaStreamSynchronize(s));
-  if (v[0]) OWL_CUDA(cudaMemsetAsync(p, 0, sizeof(int), s));
-  if (v[1]) OWL_CUDA(cudaMemsetAsync(pw, 0, sizeof(int), s));
-  *out = v[0] | v[1];
+  for (int i = 0; i < 3; ++i)
+    if (v[i]) OWL_CUDA(cudaMemsetAsync(w[i], 0, sizeof(int), s));
+  *out = v[0] | v[1] | v[2];
   return kOk;
 }
 

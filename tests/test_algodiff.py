@@ -187,3 +187,63 @@ def test_fan_in_adjoints_add(ad):
     reverse_prop(np.ones(primal(y).shape), y)
     one = ad.nn.conv2d_backward_input(x, w, [1, 1], np.ones(primal(y).shape))
     assert np.allclose(nx.adj, 2 * one, rtol=0, atol=1e-12)
+
+
+# ---- the fused layers (owl_gb300.layers) as tape ops ------------------------
+
+
+def _small_cnn_fused(ad, p, x, onehot):
+    """_small_cnn with each conv + bias + ReLU, the dense layer and the loss
+    as the library's fused ops."""
+    M, N = ad.Maths, ad.NN
+    h = N.conv2d_bias_act(x, p["w1"], p["b1"], [1, 1], SAME, 1)
+    h = N.max_pool2d(SAME, h, [2, 2], [2, 2])
+    h = N.conv2d_bias_act(h, p["w2"], p["b2"], [1, 1], SAME, 1)
+    h = N.avg_pool2d(VALID, h, [2, 2], [2, 2])
+    h = M.reshape(h, (primal(h).shape[0], 3 * 3 * 6))
+    z = N.fully_connected(h, p["w3"], p["b3"], 0)
+    return N.softmax_cross_entropy(z, onehot)
+
+
+def test_fused_layers_equal_owls_composition(ad):
+    """conv2d_bias_act / fully_connected / softmax_cross_entropy give the
+    loss and gradients of Owl's separate operations (conv2d, add, relu, dot,
+    softmax, cross_entropy) to float64 rounding."""
+    rng = np.random.default_rng(37)
+    params = _small_params(rng)
+    x = rng.uniform(0, 1, (4, 12, 12, 1))
+    onehot = np.eye(10)[rng.integers(0, 10, 4)]
+    la, ga = loss_and_grads(ad, params, x, onehot, model=_small_cnn_fused)
+    lb, gb = loss_and_grads(ad, params, x, onehot, model=_small_cnn)
+    assert abs(float(la) - float(lb)) <= 1e-13 * abs(float(lb))
+    for k in ga:
+        assert np.max(np.abs(ga[k] - gb[k])) <= 1e-12 * max(np.max(np.abs(gb[k])), 1e-300), k
+
+
+def test_fused_layers_match_finite_differences(ad):
+    rng = np.random.default_rng(38)
+    params = _small_params(rng)
+    x = rng.uniform(0, 1, (3, 12, 12, 1))
+    onehot = np.eye(10)[rng.integers(0, 10, 3)]
+    _, grads = loss_and_grads(ad, params, x, onehot, model=_small_cnn_fused)
+
+    def loss(p):
+        return _small_cnn_fused(ad, p, x, onehot)
+
+    for name in params:
+        idx = rng.choice(params[name].size, size=min(8, params[name].size), replace=False)
+        err, _ = check_grad(loss, params, grads, name, idx, EPS)
+        assert err <= TOL, (name, err)
+
+
+def test_fully_connected_with_relu_and_untracked_inputs(ad):
+    """A ReLU dense layer with only some inputs tracked: the adjoints of the
+    tracked ones, against FD."""
+    rng = np.random.default_rng(39)
+    a = rng.standard_normal((5, 7))
+    w = rng.standard_normal((7, 4))
+    b = rng.standard_normal(4)
+    for tracked in ("a", "w", "b"):
+        _fd_check_op(lambda *t: ad.NN.fully_connected(
+            t[0] if tracked == "a" else a, t[0] if tracked == "w" else w,
+            t[0] if tracked == "b" else b, 1), [{"a": a, "w": w, "b": b}[tracked]], rng)
