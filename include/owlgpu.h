@@ -81,8 +81,26 @@ int owlgpu_last_conv_path(void);
 int owlgpu_device_status(void);
 /* Device ordinal used by the host drop-in entry points (default 0). */
 int owlgpu_set_device(int device);
-/* Release cached device/pinned staging memory held by the host drop-in. */
+/* Release cached device/pinned staging memory held by the host drop-in,
+ * and every cached weight image (below). */
 int owlgpu_trim(void);
+/* Weight-image cache (no counterpart in Owl, whose stubs re-pack their
+ * kernel operand on every call too).  The tensor-core convolutions re-lay
+ * the kernel tensor out into the image of its shared-memory tiles on every
+ * call.  A caller whose kernel tensors stay unchanged across calls -- a
+ * serving loop -- declares their contents with a version; later calls on
+ * the current device whose kernel pointer has a declared version reuse the
+ * images built for that version (one per layout the call's geometry needs),
+ * so a captured forward pass launches no re-layout.  An image is built by
+ * the first call that needs it outside stream capture, which synchronises
+ * its stream once; calls made while their stream is capturing and finding
+ * no image re-lay the tensor out per call as usual.  The caller declares a
+ * new version whenever it changes the tensor's contents, and forgets the
+ * pointer before freeing it (images are keyed by device address); both drop
+ * the pointer's images after synchronising the device, and neither may race
+ * with calls that use the pointer. */
+int owlgpu_weights_declare(const void *kernel, uint64_t version);
+int owlgpu_weights_forget(const void *kernel);
 
 /* ======================================================================
  * Convolution.  Owl kernel families: GEBP `spatial*` for 2-D

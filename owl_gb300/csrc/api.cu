@@ -599,8 +599,16 @@ int owlgpu_trim(void) {
   OWL_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
   OWL_CUDA(cudaDeviceSynchronize());
   OWL_CUDA(cudaMemPoolTrimTo(pool, 0));
-  return kOk;
+  return weights_drop_all();
 }
+int owlgpu_weights_declare(const void *kernel, uint64_t version) {
+  if (!kernel) {
+    set_error("owlgpu_weights_declare: null kernel pointer");
+    return kErrInvalid;
+  }
+  return weights_declare(kernel, version);
+}
+int owlgpu_weights_forget(const void *kernel) { return weights_forget(kernel); }
 
 // ---- 2-D conv (GEBP spatial family and its im2col / dilated spellings) ----
 

@@ -221,6 +221,14 @@ int tc_conv_bwd_input(int prec, const ConvGeom &g, float *dx, const float *w, co
 int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, const float *dy,
                        cudaStream_t s);
 
+// Weight-image cache of the tensor-core convolutions: declare a kernel
+// tensor's contents version (its cached images are dropped when the version
+// changes), forget a pointer, or drop every image.  Dropping synchronises
+// the device first.
+int weights_declare(const void *w, uint64_t version);
+int weights_forget(const void *w);
+int weights_drop_all();
+
 // Cycles a tensor-core pipeline wait polls before its CTA gives up and sets
 // the device error word (default about 2 s; shorter for a watchdog or for
 // exercising the give-up path).

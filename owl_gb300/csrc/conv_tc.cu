@@ -38,6 +38,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cstring>
 #include <mutex>
 #include <vector>
 
@@ -901,8 +902,69 @@ bool plan(TcParams &p, const View &v, int kind, int t_slot, int t_table) {
   return true;
 }
 
+// ---- weight-image cache ------------------------------------------------------
+// A caller that keeps a kernel tensor unchanged across calls declares its
+// contents with a version (owlgpu_weights_declare); calls whose kernel
+// pointer has a declared version reuse the B-tile images built for that
+// version, one per layout (the plan and tap maps a geometry needs), instead
+// of re-laying the tensor out on every call.
+
+struct WeightKey {
+  int dev, kind, bwd_input, BN, CB, NCB, n_tiles, nseg, Ci, Co;
+  const float *w;
+  PrepSegs ps;  // zero-initialised before it is filled: compared bytewise
+};
+
+struct WeightImage {
+  WeightKey key;
+  uint64_t version;
+  uint8_t *buf;
+  size_t bytes;
+  bool ready;  // built and synchronised (calls meanwhile use per-call scratch)
+};
+
+std::mutex g_wmu;
+std::vector<std::pair<std::pair<int, const void *>, uint64_t>> g_declared;
+std::vector<WeightImage> g_images;
+
+bool same_key(const WeightKey &a, const WeightKey &b) {
+  return std::memcmp(&a, &b, sizeof(WeightKey)) == 0;
+}
+
+// The declared version of (device, pointer); false when none.
+bool declared_version(int dev, const void *w, uint64_t *v) {
+  for (const auto &d : g_declared)
+    if (d.first.first == dev && d.first.second == w) {
+      *v = d.second;
+      return true;
+    }
+  return false;
+}
+
+// Free the images of (device, pointer), or all of them, after the device
+// has finished every queued kernel (they may still be reading them).
+// Caller holds g_wmu.
+int drop_images(int dev, const void *w, bool all) {
+  bool any = false;
+  for (const auto &im : g_images)
+    if (all || (im.key.dev == dev && im.key.w == w)) any = true;
+  if (!any) return kOk;
+  OWL_CUDA(cudaDeviceSynchronize());
+  for (size_t i = 0; i < g_images.size();) {
+    WeightImage &im = g_images[i];
+    if (all || (im.key.dev == dev && im.key.w == w)) {
+      cudaFree(im.buf);
+      g_images[i] = g_images.back();
+      g_images.pop_back();
+    } else {
+      ++i;
+    }
+  }
+  return kOk;
+}
+
 template <int KIND, bool MULTI>
-int launch(const TcParams &p, size_t smem, cudaStream_t s) {
+int launch(const TcParams &p, size_t smem, cudaStream_t s, bool after_prep) {
   static bool attr_set[64] = {false};
   int dev = 0;
   cudaGetDevice(&dev);
@@ -922,7 +984,9 @@ int launch(const TcParams &p, size_t smem, cudaStream_t s) {
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  // a cached weight image has no prep_weights launch before the kernel:
+  // then it is an ordinary launch, ordered after everything on the stream
+  cfg.numAttrs = after_prep ? 1 : 0;
   cudaError_t e = cudaLaunchKernelEx(&cfg, conv_tc_kernel<KIND, MULTI>, p);
   note_launch();
   note_tc_launch();
@@ -1028,25 +1092,65 @@ int run_segs(int prec, int nseg_in, const SegSpec *sp, bool bwd_input, int Ci, i
   }
   const int parts = kind == K_BF16X3 ? 2 : 1;
   const size_t wt_bytes = woff;
-  void *wt = nullptr;
-  int rc = scratch_alloc(&wt, wt_bytes * parts, s);
-  if (rc) return rc;
+  // the images of every segment (blockIdx.y of prep_weights = segment)
+  PrepSegs ps;
+  std::memset(&ps, 0, sizeof(ps));
+  for (int k = 0; k < nseg; ++k) {
+    ps.T[k] = p.seg[k].T;
+    ps.off[k] = p.seg[k].woff;
+    ps.tm[k] = sp[idx[k]].tm;
+  }
+  if (fuse_n) {
+    ps.fuse_n = fuse_n;
+    // channels past the last class (tile padding) read no weight; their
+    // map entry is any valid one
+    for (int k = 0; k < kMaxSeg; ++k) ps.tm[k] = fuse_tm[k < nclass ? k : 0];
+  }
+  // a declared kernel tensor: reuse (or build, outside stream capture) its
+  // cached images; otherwise re-lay it out into per-call scratch
+  WeightKey key;
+  std::memset(&key, 0, sizeof(key));
+  cudaGetDevice(&key.dev);
+  key.kind = kind; key.bwd_input = bwd_input ? 1 : 0; key.BN = p.BN; key.CB = p.CB;
+  key.NCB = p.NCB; key.n_tiles = p.n_tiles; key.nseg = nseg; key.Ci = Ci; key.Co = Co;
+  key.w = w;
+  key.ps = ps;
+  uint8_t *cached = nullptr;
+  bool build_cached = false;
+  {
+    std::lock_guard<std::mutex> lk(g_wmu);
+    uint64_t ver = 0;
+    if (declared_version(key.dev, w, &ver)) {
+      bool present = false;
+      for (const WeightImage &im : g_images)
+        if (im.version == ver && same_key(im.key, key)) {
+          present = true;
+          if (im.ready) cached = im.buf;
+        }
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      if (!present && cudaStreamIsCapturing(s, &cs) == cudaSuccess &&
+          cs == cudaStreamCaptureStatusNone) {
+        void *buf = nullptr;
+        if (cudaMalloc(&buf, wt_bytes * parts) == cudaSuccess) {
+          g_images.push_back({key, ver, (uint8_t *)buf, wt_bytes * parts, false});
+          cached = (uint8_t *)buf;
+          build_cached = true;
+        } else {
+          cudaGetLastError();  // no room for an image: per-call scratch instead
+        }
+      }
+    }
+  }
+  void *wt = cached;
+  int rc = kOk;
+  if (!cached) {
+    rc = scratch_alloc(&wt, wt_bytes * parts, s);
+    if (rc) return rc;
+  }
   p.wt_hi = (const uint8_t *)wt;
   p.wt_lo = parts == 2 ? (const uint8_t *)wt + wt_bytes : nullptr;
-  {
-    // one launch for every segment's images (blockIdx.y = segment)
-    PrepSegs ps{};
-    for (int k = 0; k < nseg; ++k) {
-      ps.T[k] = p.seg[k].T;
-      ps.off[k] = p.seg[k].woff;
-      ps.tm[k] = sp[idx[k]].tm;
-    }
-    if (fuse_n) {
-      ps.fuse_n = fuse_n;
-      // channels past the last class (tile padding) read no weight; their
-      // map entry is any valid one
-      for (int k = 0; k < kMaxSeg; ++k) ps.tm[k] = fuse_tm[k < nclass ? k : 0];
-    }
+  const bool prep = !cached || build_cached;
+  if (prep) {
     uint8_t *hi = (uint8_t *)wt;
     uint8_t *lo = parts == 2 ? (uint8_t *)wt + wt_bytes : nullptr;
     const long long n = (long long)p.n_tiles * p.NCB * t_slot * p.NCH * p.BN;
@@ -1064,18 +1168,27 @@ int run_segs(int prec, int nseg_in, const SegSpec *sp, bool bwd_input, int Ci, i
     cudaError_t e = cudaGetLastError();
     note_launch();
     if (e != cudaSuccess) {
-      scratch_free(wt, s);
+      if (!cached) scratch_free(wt, s);
       return cuda_fail(e, "prep_weights");
+    }
+    if (build_cached) {
+      // the image is complete before any call, on any stream, reads it
+      OWL_CUDA(cudaStreamSynchronize(s));
+      std::lock_guard<std::mutex> lk(g_wmu);
+      for (WeightImage &im : g_images)
+        if (im.buf == wt) im.ready = true;
     }
   }
   const size_t smem = (size_t)p.NH * parts * p.halo_bytes + (size_t)p.NB * parts * p.b_bytes +
                       (2 * p.NH + 2 * p.NB + 5) * 8 + 16 + 4 * (size_t)t_table;
   const bool multi = p.nseg > 1;
-  if (kind == K_TF32) rc = multi ? launch<K_TF32, true>(p, smem, s) : launch<K_TF32, false>(p, smem, s);
+  const bool pdl = prep && !build_cached;
+  if (kind == K_TF32)
+    rc = multi ? launch<K_TF32, true>(p, smem, s, pdl) : launch<K_TF32, false>(p, smem, s, pdl);
   else if (kind == K_BF16X3)
-    rc = multi ? launch<K_BF16X3, true>(p, smem, s) : launch<K_BF16X3, false>(p, smem, s);
-  else rc = multi ? launch<K_BF16, true>(p, smem, s) : launch<K_BF16, false>(p, smem, s);
-  scratch_free(wt, s);
+    rc = multi ? launch<K_BF16X3, true>(p, smem, s, pdl) : launch<K_BF16X3, false>(p, smem, s, pdl);
+  else rc = multi ? launch<K_BF16, true>(p, smem, s, pdl) : launch<K_BF16, false>(p, smem, s, pdl);
+  if (!cached) scratch_free(wt, s);
   return rc;
 }
 
@@ -1208,6 +1321,38 @@ int run_bwd_input_strided(int prec, const ConvGeom &g, float *dx, const float *w
 }
 
 }  // namespace
+
+int weights_declare(const void *w, uint64_t version) {
+  int dev = 0;
+  OWL_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_wmu);
+  for (auto &d : g_declared)
+    if (d.first.first == dev && d.first.second == w) {
+      if (d.second == version) return kOk;
+      d.second = version;
+      return drop_images(dev, w, false);
+    }
+  g_declared.push_back({{dev, w}, version});
+  return kOk;
+}
+
+int weights_forget(const void *w) {
+  int dev = 0;
+  OWL_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_wmu);
+  for (size_t i = 0; i < g_declared.size(); ++i)
+    if (g_declared[i].first.first == dev && g_declared[i].first.second == w) {
+      g_declared[i] = g_declared.back();
+      g_declared.pop_back();
+      break;
+    }
+  return drop_images(dev, w, false);
+}
+
+int weights_drop_all() {
+  std::lock_guard<std::mutex> lk(g_wmu);
+  return drop_images(0, nullptr, true);
+}
 
 int tc_conv_fwd(int prec, const ConvGeom &g, const float *x, const float *w, float *y,
                 cudaStream_t s, const float *bias, int act) {

@@ -147,26 +147,64 @@ def stack_flops(side: int, batch: int = 1) -> float:
 
 
 class ResidualStack:
-    """Forward pass of the stack over one NN function set (GPU or oracle);
-    elementwise ReLU and residual sums are plain array ops."""
+    """Forward pass of the stack over one NN function set (GPU or oracle).
+    A convolution followed by ReLU runs as one call with the ReLU in the
+    convolution's epilogue (owl_gb300.layers); residual sums are plain array
+    ops.  On the GPU the stack declares its kernel tensors to the library's
+    weight-image cache (they never change), so a forward pass re-lays no
+    weights out and a captured one launches only the convolution and pooling
+    kernels."""
 
     def __init__(self, weights: dict, nn: NN):
+        from .layers import Layers
+
         self.w = weights
         self.nn = nn
+        self.layers = Layers(nn)
+        self._declared = []
+        if self.layers.gpu:
+            from . import _lib
+
+            for t in weights.values():
+                if type(t).__module__.startswith("torch") and t.is_cuda:
+                    _lib.call("owlgpu_weights_declare", t.data_ptr(), 0)
+                    self._declared.append(t)
+
+    def release(self) -> None:
+        """Forget the declared kernel tensors.  Call it before the weights
+        are freed: the library keys its images by device address, and a
+        freed address may be reused by another tensor."""
+        if self._declared:
+            from . import _lib
+
+            for t in self._declared:
+                _lib.call("owlgpu_weights_forget", t.data_ptr())
+            self._declared = []
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
 
     @staticmethod
     def _relu(a):
         return a.clamp_min(0) if type(a).__module__.startswith("torch") else np.maximum(a, 0)
 
+    def _conv_relu(self, x, w, s):
+        from .layers import ACT_RELU
+
+        return self.layers.conv2d_bias_act(x, w, None, [s, s], SAME, ACT_RELU)
+
     def forward(self, x):
         nn, w, relu = self.nn, self.w, self._relu
-        h = relu(nn.conv2d(x, w["stem"], [2, 2], SAME))
+        h = self._conv_relu(x, w["stem"], 2)
         h = nn.max_pool2d(h, [2, 2], [2, 2], SAME)
         for si, (cout, stride) in enumerate(STAGES):
             for bi in range(2):
                 s = stride if bi == 0 else 1
                 pre = f"s{si}b{bi}"
-                y = relu(nn.conv2d(h, w[pre + "c1"], [s, s], SAME))
+                y = self._conv_relu(h, w[pre + "c1"], s)
                 y = nn.conv2d(y, w[pre + "c2"], [1, 1], SAME)
                 sc = nn.conv2d(h, w[pre + "proj"], [s, s], SAME) if pre + "proj" in w else h
                 h = relu(y + sc)

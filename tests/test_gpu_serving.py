@@ -34,7 +34,8 @@ def served(gpu_lib):
     sch = Scheduler(ex, hbm_budget=8 << 30, max_group=48)
     st = sch.run(reqs)
     sch.close()
-    return stack, reqs, st
+    yield stack, reqs, st
+    stack.release()
 
 
 def test_every_request_served(served):
@@ -69,5 +70,6 @@ def test_bf16_error_against_float64(served):
     for r in reqs[:6]:
         y64 = from_dev(s64.forward(r.pixels.double().cuda()))
         errs.append(rel(r.output, y64))
+    s64.release()
     print("BF16 serving error vs float64:", max(errs))
     assert max(errs) <= 1e-2
