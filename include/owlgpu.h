@@ -102,6 +102,23 @@ int owlgpu_trim(void);
 int owlgpu_weights_declare(const void *kernel, uint64_t version);
 int owlgpu_weights_forget(const void *kernel);
 
+/* Device buffers and streams for a caller that does not link the CUDA
+ * runtime itself -- the OCaml binding's custom blocks (owl_gb300/ocaml/
+ * owlgpu_device_stubs.c), which hold the pointers the device-resident entry
+ * points take.  No counterpart in Owl, whose arrays live in host memory.
+ * Streams are created on the device of owlgpu_set_device, blocking with
+ * respect to the legacy default stream (NULL).  Allocation and free are
+ * stream-ordered: a buffer freed on the legacy default stream is released
+ * after all earlier work on every such stream.  The copies return when the
+ * bytes have arrived. */
+int owlgpu_stream_create(void **stream);
+int owlgpu_stream_destroy(void *stream);
+int owlgpu_stream_synchronize(void *stream);
+int owlgpu_device_alloc(void **ptr, uint64_t bytes, void *stream);
+int owlgpu_device_free(void *ptr, void *stream);
+int owlgpu_copy_to_device(void *dst, const void *src, uint64_t bytes, void *stream);
+int owlgpu_copy_to_host(void *dst, const void *src, uint64_t bytes, void *stream);
+
 /* ======================================================================
  * Convolution.  Owl kernel families: GEBP `spatial*` for 2-D
  * (owl_ndarray_conv.ml:257-282), `cuboid_*_im2col` for 3-D

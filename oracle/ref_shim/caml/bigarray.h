@@ -11,4 +11,7 @@ struct caml_ba_array {
 };
 #define Caml_ba_array_val(v) ((struct caml_ba_array *)(v))
 #define Caml_ba_data_val(v) (Caml_ba_array_val(v)->data)
+#define CAML_BA_KIND_MASK 0xFF
+/* bytes of the array's data (element kind in flags & CAML_BA_KIND_MASK) */
+uintnat caml_ba_byte_size(struct caml_ba_array *b);
 #endif

@@ -7,3 +7,4 @@
 #define CAMLparam3(a, b, c) ((void)(a), (void)(b), (void)(c))
 #define CAMLparam4(a, b, c, d) ((void)(a), (void)(b), (void)(c), (void)(d))
 #define CAMLreturn(v) return (v)
+#define CAMLlocal1(a) value a = 0

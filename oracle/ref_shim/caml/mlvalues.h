@@ -27,4 +27,6 @@ typedef unsigned int tag_t;
 #define Store_double_field(v, i, d) (((double *)(v))[i] = (d))
 #define Double_field(v, i) (((double *)(v))[i])
 #define Wosize_val(v) 0
+#define Is_long(x) (((x) & 1) != 0)
+#define Is_block(x) (((x) & 1) == 0)
 #endif

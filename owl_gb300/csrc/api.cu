@@ -610,6 +610,53 @@ int owlgpu_weights_declare(const void *kernel, uint64_t version) {
 }
 int owlgpu_weights_forget(const void *kernel) { return weights_forget(kernel); }
 
+// ---- device buffers and streams for callers without the CUDA runtime --------
+
+int owlgpu_stream_create(void **stream) {
+  if (!stream) {
+    set_error("owlgpu_stream_create: null result pointer");
+    return kErrInvalid;
+  }
+  cudaStream_t s = nullptr;
+  OWL_CUDA(cudaSetDevice(g_device.load()));
+  OWL_CUDA(cudaStreamCreate(&s));
+  *stream = (void *)s;
+  return kOk;
+}
+int owlgpu_stream_destroy(void *stream) {
+  if (stream) OWL_CUDA(cudaStreamDestroy((cudaStream_t)stream));
+  return kOk;
+}
+int owlgpu_stream_synchronize(void *stream) {
+  OWL_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  return kOk;
+}
+int owlgpu_device_alloc(void **ptr, uint64_t bytes, void *stream) {
+  if (!ptr) {
+    set_error("owlgpu_device_alloc: null result pointer");
+    return kErrInvalid;
+  }
+  *ptr = nullptr;
+  OWL_CUDA(cudaSetDevice(g_device.load()));
+  return scratch_alloc(ptr, (size_t)bytes, (cudaStream_t)stream);
+}
+int owlgpu_device_free(void *ptr, void *stream) {
+  if (ptr) OWL_CUDA(cudaFreeAsync(ptr, (cudaStream_t)stream));
+  return kOk;
+}
+int owlgpu_copy_to_device(void *dst, const void *src, uint64_t bytes, void *stream) {
+  if (bytes == 0) return kOk;
+  OWL_CUDA(cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyHostToDevice, (cudaStream_t)stream));
+  OWL_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  return kOk;
+}
+int owlgpu_copy_to_host(void *dst, const void *src, uint64_t bytes, void *stream) {
+  if (bytes == 0) return kOk;
+  OWL_CUDA(cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  OWL_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  return kOk;
+}
+
 // ---- 2-D conv (GEBP spatial family and its im2col / dilated spellings) ----
 
 #define CONV2D_FWD(KIND, T, NAME, DIL)                                                        \

@@ -3,7 +3,12 @@ externals are current, the stubs compile warning-free against OCaml's header
 interface and link against libowlgpu, every external has the arity of Owl's
 external of the same name, and a stub called the way OCaml calls it (tagged
 ints, Bigarray descriptors) releases the runtime lock around the call and
-raises Failure with the library's message on a bad argument."""
+raises Failure with the library's message on a bad argument.
+
+The device-resident binding (owlgpu_device_stubs.c, owlgpu_device.ml): a
+stub per device entry point with the C function's arity, custom blocks for
+buffers and streams with finalisers and no compare / hash / serialise, and
+its argument checks, all without a GPU."""
 
 import ctypes
 import json
@@ -29,7 +34,8 @@ def build_stubs(out_dir: Path) -> Path:
     lib_dir = ROOT / "owl_gb300"
     cmd = ["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-O1", "-fPIC", "-shared",
            "-I", str(ROOT / "oracle" / "ref_shim"), "-I", str(ROOT / "include"),
-           str(OCAML / "owlgpu_stubs.c"), str(ROOT / "tests" / "ocaml_runtime_shim.c"),
+           str(OCAML / "owlgpu_stubs.c"), str(OCAML / "owlgpu_device_stubs.c"),
+           str(ROOT / "tests" / "ocaml_runtime_shim.c"),
            "-L", str(lib_dir), "-lowlgpu", f"-Wl,-rpath,{lib_dir}", "-o", str(so)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
@@ -53,6 +59,10 @@ def test_generated_files_are_current():
     assert (OCAML / "owlgpu_stubs.c").read_text() == c
     assert (OCAML / "owlgpu_externals.ml").read_text() == ml
     assert n == 152
+    dc, dml, dn = make_stubs.render_device()
+    assert (OCAML / "owlgpu_device_stubs.c").read_text() == dc
+    assert (OCAML / "owlgpu_device.ml").read_text() == dml
+    assert dn == 105
 
 
 def test_every_entry_point_has_a_stub_pair(stubs):
@@ -121,3 +131,49 @@ def test_bad_argument_raises_failure_around_a_released_lock(stubs):
     stubs.shim_reset()
     stubs.owlgpu_stub_float32_ndarray_conv_spatial_bytecode(argv, 17)
     assert b"stride" in stubs.shim_last_failure()
+
+
+# ---- the device-resident binding ---------------------------------------------
+
+
+def test_every_device_entry_point_has_its_stubs_and_arity(stubs):
+    import make_stubs
+
+    ours = _externals((OCAML / "owlgpu_device.ml").read_text())
+    eps = make_stubs.device_entry_points()
+    assert len(eps) == 105
+    for name, params in eps:
+        short = name[len("owlgpu_"):]
+        assert ours[short] == len(params), name
+        stub = "owlgpu_dstub_" + short
+        assert getattr(stubs, stub + "_native") is not None
+        if len(params) > 5:
+            assert getattr(stubs, stub + "_bytecode") is not None
+    for fixed in ("stream_create", "stream_default", "stream_sync", "buf_create", "buf_bytes",
+                  "buf_free", "buf_upload", "buf_download"):
+        assert getattr(stubs, "owlgpu_dstub_" + fixed) is not None
+    text = (OCAML / "owlgpu_device.ml").read_text()
+    assert "type buf" in text and "type stream" in text
+    # nullable pointer arguments are options: the dense layer's bias
+    assert "-> buf option" in text
+
+
+def test_custom_blocks_without_gpu(stubs):
+    """The default-stream block: identifier, a finaliser that leaves the
+    legacy stream alone; a negative buffer size raises Failure before any
+    CUDA call."""
+    f = stubs.owlgpu_dstub_stream_default
+    f.restype = ctypes.c_void_p
+    v = f(_tag(0))
+    stubs.shim_custom_id.restype = ctypes.c_char_p
+    assert stubs.shim_custom_id(ctypes.c_void_p(v)) == b"owlgpu.stream"
+    stubs.shim_finalize(ctypes.c_void_p(v))
+    stubs.shim_reset()
+    b = stubs.owlgpu_dstub_buf_create
+    b.restype = ctypes.c_void_p
+    b(_tag(-8), ctypes.c_void_p(v))
+    assert b"negative size" in stubs.shim_last_failure()
+    src = (OCAML / "owlgpu_device_stubs.c").read_text()
+    # no equality, hashing or serialisation of device memory
+    for op in ("custom_compare_default", "custom_hash_default", "custom_serialize_default"):
+        assert src.count(op) == 2
