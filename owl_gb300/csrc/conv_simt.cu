@@ -15,6 +15,7 @@
 //                by a second kernel in a fixed order (deterministic).
 #include "common.cuh"
 
+#include <algorithm>
 #include <type_traits>
 
 namespace owlgpu {
@@ -26,6 +27,11 @@ struct Dev {
   int64_t B, IC, IR, ID, Ci, KC, KR, KD, OC, OR, OD, Co;
   int sc, sr, sd, dc, dr, dd, pc, pr, pd;
   int64_t M, N, K;  // GEMM view sizes
+  // FWD only, ystrided: output pixel (b, oc, or, od) is written at pixel
+  // yoff + b*ysb + oc*ysc + or*ysr + od*ysd of the output array (one
+  // residue class of a backward_input); otherwise the output is dense.
+  int ystrided;
+  int64_t yoff, ysb, ysc, ysr, ysd;
 };
 
 template <typename T, int MODE, int BM, int BN, int BK, int TM, int TN>
@@ -46,6 +52,25 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
 
   const int tid = threadIdx.x;
   const int64_t m0 = (int64_t)blockIdx.x * BM;
+  // BWDK: a thread's A elements all sit in row m0 + tid % BM (NT is a
+  // multiple of BM), so its tap and channel are decoded once.
+  static_assert(MODE != BWDK || NT % BM == 0, "BWDK row decode needs NT % BM == 0");
+  int a_dc = 0, a_dr = 0, a_dd = 0, a_ci = 0;
+  bool a_mval = false;
+  if (MODE == BWDK) {
+    const int64_t m = m0 + tid % BM;
+    a_mval = m < g.M;
+    if (a_mval) {
+      int64_t tap = m / g.Ci;
+      a_ci = (int)(m - tap * g.Ci);
+      const int kd = (int)(tap % g.KD);
+      tap /= g.KD;
+      const int kr = (int)(tap % g.KR), kc = (int)(tap / g.KR);
+      a_dc = kc * g.dc;
+      a_dr = kr * g.dr;
+      a_dd = kd * g.dd;
+    }
+  }
   const int64_t n0 = (int64_t)blockIdx.y * BN;
   const int64_t k_begin = (int64_t)blockIdx.z * k_per_split;
   const int64_t k_end = min(g.K, k_begin + k_per_split);
@@ -175,20 +200,13 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
       // BWDK: A[m=(tap,ci)][k=pixel] = X[gather], m fastest across threads.
 #pragma unroll
       for (int i = 0; i < A_PER; ++i) {
-        int e = tid + i * NT;
-        int mm = e % BM, kk = e / BM;
-        int64_t m = m0 + mm;
+        const int kk = (tid + i * NT) / BM;
         T v = T(0);
-        int64_t base = s_base[buf][kk];
-        if (m < g.M && base >= 0) {
-          int64_t tap = m / g.Ci;
-          int ci = (int)(m - tap * g.Ci);
-          int kd = (int)(tap % g.KD); tap /= g.KD;
-          int kr = (int)(tap % g.KR), kc = (int)(tap / g.KR);
-          int c = s_c[buf][kk] + kc * g.dc, r = s_r[buf][kk] + kr * g.dr,
-              d = s_d[buf][kk] + kd * g.dd;
+        const int64_t base = s_base[buf][kk];
+        if (a_mval && base >= 0) {
+          const int c = s_c[buf][kk] + a_dc, r = s_r[buf][kk] + a_dr, d = s_d[buf][kk] + a_dd;
           if (c >= 0 && c < g.IC && r >= 0 && r < g.IR && d >= 0 && d < g.ID)
-            v = A0[((base + ((int64_t)c * g.IR + r) * g.ID + d) * g.Ci) + ci];
+            v = A0[((base + ((int64_t)c * g.IR + r) * g.ID + d) * g.Ci) + a_ci];
         }
         a_reg[i] = v;
       }
@@ -284,10 +302,20 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
   for (int i = 0; i < TM; ++i) {
     int64_t m = m0 + ty * TM + i;
     if (m >= g.M) continue;
+    int64_t row = m;
+    if (MODE == FWD && g.ystrided) {
+      int64_t t = m;
+      const int64_t od = t % g.OD;
+      t /= g.OD;
+      const int64_t orr = t % g.OR;
+      t /= g.OR;
+      const int64_t oc = t % g.OC, b = t / g.OC;
+      row = g.yoff + b * g.ysb + oc * g.ysc + orr * g.ysr + od * g.ysd;
+    }
 #pragma unroll
     for (int j = 0; j < TN; ++j) {
       int64_t n = n0 + tx * TN + j;
-      if (n < g.N) Cz[m * g.N + n] = acc[i][j];
+      if (n < g.N) Cz[row * g.N + n] = acc[i][j];
     }
   }
 }
@@ -313,6 +341,9 @@ Dev make_dev(const ConvGeom &g, int mode) {
   d.sc = g.sc; d.sr = g.sr; d.sd = g.sd;
   d.dc = g.dc; d.dr = g.dr; d.dd = g.dd;
   d.pc = g.pc; d.pr = g.pr; d.pd = g.pd;
+  d.ystrided = 0;
+  d.yoff = 0;
+  d.ysb = g.OC * g.OR * g.OD; d.ysc = g.OR * g.OD; d.ysr = g.OD; d.ysd = 1;
   if (mode == FWD) { d.M = g.out_pixels(); d.N = g.Co; d.K = g.taps() * g.Ci; }
   else if (mode == BWDI) { d.M = g.in_pixels(); d.N = g.Ci; d.K = g.taps() * g.Co; }
   else { d.M = g.taps() * g.Ci; d.N = g.Co; d.K = g.out_pixels(); }
@@ -363,15 +394,109 @@ int fwd_t(const ConvGeom &g, const T *x, const T *w, T *y, cudaStream_t s) {
   return launch_any<T, FWD>(d, x, w, y, 1, d.K, s);
 }
 
+// The kernel of one residue class of backward_input, laid out as the kernel
+// of a forward convolution of dY: w2[t'][co][ci] = w[orig(t')][ci][co], t' =
+// (a, b, c) over the class's taps, orig = (base + mul * t') per axis.
+template <typename T>
+__global__ void bwdi_class_weights(const T *__restrict__ w, T *__restrict__ w2, int Ka, int Kb,
+                                   int Kc, int base_a, int base_b, int base_c, int mul_a,
+                                   int mul_b, int mul_c, int KR, int KD, int64_t Ci,
+                                   int64_t Co) {
+  const int64_t total = (int64_t)Ka * Kb * Kc * Co * Ci;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ci = i % Ci;
+    int64_t r = i / Ci;
+    const int64_t co = r % Co;
+    r /= Co;
+    const int c = (int)(r % Kc), b = (int)((r / Kc) % Kb), a = (int)(r / ((int64_t)Kc * Kb));
+    const int64_t orig = ((int64_t)(base_a + mul_a * a) * KR + (base_b + mul_b * b)) * KD +
+                         (base_c + mul_c * c);
+    w2[i] = w[(orig * Ci + ci) * Co + co];
+  }
+}
+
+// backward_input as forward convolutions over the residue classes of dX.
+// With forward index s*o - p + t*d, element i = s*a + r of dX receives
+// dY[o] W[t] for the taps with (r + p - t*d) divisible by s, at
+// o = a + (r + p - t*d)/s.  Those taps, largest first, spaced s/g apart
+// (g = gcd(s, d)), form a stride-1 convolution of dY with dilation d/g and
+// leading pad -(r + p - tmax*d)/s, whose output is the sub-grid i = s*a + r
+// of dX: every multiply-add is a useful one (no tap is tested and masked).
+// Classes that no tap reaches are zero; dX is cleared first when there are
+// any.  Stride 1 is one class: dY against the flipped, channel-exchanged
+// kernel.
 template <typename T>
 int bwdi_t(const ConvGeom &g, T *dx, const T *w, const T *dy, cudaStream_t s) {
-  Dev d = make_dev(g, BWDI);
-  if (d.M == 0 || d.N == 0) return kOk;
-  if (d.K == 0) {
-    OWL_CUDA(cudaMemsetAsync(dx, 0, sizeof(T) * d.M * d.N, s));
-    return kOk;
-  }
-  return launch_any<T, BWDI>(d, dy, w, dx, 1, d.K, s);
+  if (g.in_pixels() == 0 || g.Ci == 0) return kOk;
+  const int S[3] = {g.sc, g.sr, g.sd}, D[3] = {g.dc, g.dr, g.dd}, P[3] = {g.pc, g.pr, g.pd};
+  const int64_t K[3] = {g.KC, g.KR, g.KD}, I[3] = {g.IC, g.IR, g.ID};
+  struct Axis {
+    int n, base, mul, dil, pad;
+    int64_t out;
+  };
+  auto axis_class = [&](int ax, int r) {
+    Axis a{0, 0, 0, 1, 0, 0};
+    int tmax = -1;
+    for (int t = 0; t < (int)K[ax]; ++t)
+      if ((((r + P[ax] - t * D[ax]) % S[ax]) + S[ax]) % S[ax] == 0) {
+        tmax = t > tmax ? t : tmax;
+        ++a.n;
+      }
+    int gg = S[ax], dd = D[ax];
+    while (dd) { const int t = gg % dd; gg = dd; dd = t; }
+    a.base = tmax;
+    a.mul = -(S[ax] / gg);
+    a.dil = D[ax] / gg;
+    a.pad = a.n ? -((r + P[ax] - tmax * D[ax]) / S[ax]) : 0;
+    a.out = I[ax] > r ? (I[ax] - r + S[ax] - 1) / S[ax] : 0;
+    return a;
+  };
+  bool any_empty = g.Co == 0 || g.out_pixels() == 0;
+  for (int ax = 0; ax < 3; ++ax)
+    for (int r = 0; r < S[ax]; ++r) {
+      const Axis a = axis_class(ax, r);
+      if (a.n == 0 && a.out > 0) any_empty = true;
+    }
+  if (any_empty) OWL_CUDA(cudaMemsetAsync(dx, 0, sizeof(T) * (size_t)g.x_elems(), s));
+  if (g.Co == 0 || g.out_pixels() == 0) return kOk;
+  T *w2 = nullptr;
+  int rc = scratch_alloc((void **)&w2, sizeof(T) * (size_t)g.w_elems(), s);
+  if (rc) return rc;
+  for (int r0 = 0; r0 < S[0] && rc == kOk; ++r0)
+    for (int r1 = 0; r1 < S[1] && rc == kOk; ++r1)
+      for (int r2 = 0; r2 < S[2] && rc == kOk; ++r2) {
+        const Axis a = axis_class(0, r0), b = axis_class(1, r1), c = axis_class(2, r2);
+        if (a.n == 0 || b.n == 0 || c.n == 0 || a.out * b.out * c.out == 0) continue;
+        const int64_t nw = (int64_t)a.n * b.n * c.n * g.Co * g.Ci;
+        bwdi_class_weights<T><<<(unsigned)std::min<int64_t>(ceil_div(nw, 256), 1024), 256, 0, s>>>(
+            w, w2, a.n, b.n, c.n, a.base, b.base, c.base, a.mul, b.mul, c.mul, (int)g.KR,
+            (int)g.KD, g.Ci, g.Co);
+        cudaError_t e = cudaGetLastError();
+        note_launch();
+        if (e != cudaSuccess) {
+          rc = cuda_fail(e, "bwdi_class_weights");
+          break;
+        }
+        ConvGeom gc{};
+        gc.B = g.B;
+        gc.IC = g.OC; gc.IR = g.OR; gc.ID = g.OD; gc.Ci = g.Co;
+        gc.KC = a.n; gc.KR = b.n; gc.KD = c.n;
+        gc.OC = a.out; gc.OR = b.out; gc.OD = c.out; gc.Co = g.Ci;
+        gc.sc = gc.sr = gc.sd = 1;
+        gc.dc = a.dil; gc.dr = b.dil; gc.dd = c.dil;
+        gc.pc = a.pad; gc.pr = b.pad; gc.pd = c.pad;
+        Dev d = make_dev(gc, FWD);
+        d.ystrided = 1;
+        d.ysb = g.IC * g.IR * g.ID;
+        d.ysc = (int64_t)S[0] * g.IR * g.ID;
+        d.ysr = (int64_t)S[1] * g.ID;
+        d.ysd = S[2];
+        d.yoff = ((int64_t)r0 * g.IR + r1) * g.ID + r2;
+        rc = launch_any<T, FWD>(d, dy, w2, dx, 1, d.K, s);
+      }
+  scratch_free(w2, s);
+  return rc;
 }
 
 // The GEMM view of one pass with its reduction split across CTAs: each
