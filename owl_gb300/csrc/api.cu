@@ -71,6 +71,15 @@ static thread_local int t_last_path = -1;
 // accurate.  The path taken is visible through owlgpu_last_conv_path().
 int conv_fwd(Dtype dt, int prec, const ConvGeom &g, const void *x, const void *w, void *y,
              cudaStream_t s, const void *bias, int act) {
+  if (tc_requested(dt, prec) && prec != OWLGPU_PREC_TF32) {
+    // kernel = stride: a GEMM over the windows
+    int rc = tc_conv_s2d(prec, false, g, (const float *)x, (const float *)w, (float *)y,
+                         (const float *)bias, act, s);
+    if (rc != kErrUnsupported) {
+      t_last_path = 1;
+      return rc;
+    }
+  }
   if (tc_requested(dt, prec)) {
     int rc = tc_conv_fwd(prec, g, (const float *)x, (const float *)w, (float *)y, s,
                          (const float *)bias, act);
@@ -100,6 +109,15 @@ int conv_bwd_input(Dtype dt, int prec, const ConvGeom &g, void *dx, const void *
 
 int conv_bwd_kernel(Dtype dt, int prec, const ConvGeom &g, const void *x, void *dw,
                     const void *dy, cudaStream_t s) {
+  if (tc_requested(dt, prec)) {
+    // kernel = stride: a GEMM over the windows
+    int rc = tc_conv_s2d(prec, true, g, (const float *)x, (const float *)dy, (float *)dw,
+                         nullptr, 0, s);
+    if (rc != kErrUnsupported) {
+      t_last_path = 1;
+      return rc;
+    }
+  }
   if (tc_requested(dt, prec)) {
     int rc = tc_conv_bwd_kernel(prec, g, (const float *)x, (float *)dw, (const float *)dy, s);
     if (rc != kErrUnsupported) {

@@ -229,6 +229,13 @@ int weights_declare(const void *w, uint64_t version);
 int weights_forget(const void *w);
 int weights_drop_all();
 
+// A convolution whose kernel equals its stride (no dilation or padding,
+// windows tiling the input): forward (bwd_kernel false: x, w -> out = y) or
+// backward_kernel (x, dy -> out = dw) as a tcgen05 GEMM over the windows.
+// kErrUnsupported for any other geometry or precision.
+int tc_conv_s2d(int prec, bool bwd_kernel, const ConvGeom &g, const float *x,
+                const float *w_or_dy, float *out, const float *bias, int act, cudaStream_t s);
+
 // Cycles a tensor-core pipeline wait polls before its CTA gives up and sets
 // the device error word (default about 2 s; shorter for a watchdog or for
 // exercising the give-up path).

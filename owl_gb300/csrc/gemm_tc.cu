@@ -41,7 +41,38 @@ constexpr int kBK = 64;   // k per pipeline stage (four K = 16 MMAs)
 constexpr int kSmemMax = 232448;
 constexpr long long kSpinLimit = 4000000000LL;
 
+// Operand A gathered from an array by non-overlapping windows (a
+// convolution whose kernel equals its stride): the A element of pixel p and
+// combined index tc = (tap, channel) is X[b][oc*KC + tcol][or*KR + tr]
+// [od*KD + td][c], p = ((b*OC + oc)*OR + or)*OD + od over the window grid.
+// Pixel counts and (tap, channel) counts are below 2^31 (checked on the
+// host), so the decodes divide in 32 bits; the offset is formed in 64.
+struct S2D {
+  int on;
+  unsigned C;            // channels of the array
+  unsigned KC, KR, KD;   // window = stride
+  unsigned OC, OR, OD;   // window grid
+  long long IC, IR, ID;  // array extents
+};
+
+__device__ __forceinline__ long long s2d_off(const S2D &g, long long p, long long tc) {
+  unsigned t = (unsigned)tc / g.C;
+  const unsigned c = (unsigned)tc - t * g.C;
+  const unsigned td = t % g.KD;
+  t /= g.KD;
+  const unsigned tr = t % g.KR, tcl = t / g.KR;
+  unsigned q = (unsigned)p;
+  const unsigned od = q % g.OD;
+  q /= g.OD;
+  const unsigned orr = q % g.OR;
+  q /= g.OR;
+  const unsigned oc = q % g.OC, b = q / g.OC;
+  return ((((long long)b * g.IC + (long long)oc * g.KC + tcl) * g.IR +
+           (long long)orr * g.KR + tr) * g.ID + (long long)od * g.KD + td) * g.C + c;
+}
+
 struct GemmParams {
+  S2D s2d;  // operand A gathered by windows (s2d.on), else by its strides
   const float *a, *b;
   float *c;           // the result (splits == 1) or partials [split][M][N]
   const float *bias;  // per column, or null; applied when splits == 1
@@ -79,71 +110,160 @@ __device__ __forceinline__ float apply_act(float v, int act) {
   return act == OWLGPU_ACT_RELU ? (v > 0.f ? v : 0.f) : v;
 }
 
-// Stage one operand's k block [k0, k0 + kBK) of rows [row0, row0 + R) into
-// `dst` (bf16, or bf16 hi + lo planes lo_off apart), zero outside the
-// matrix.  Element (row, k) is at src[row*s_row + k] when kmaj (k
-// contiguous), else at src[k*s_k + row].  K-major layout: chunk c of row r at
-// (c*R + r)*16; MN-major: k of row chunk j at (j*kBK + k)*16.  Consecutive threads take consecutive
-// 16-byte destinations (no bank conflicts); each thread reads 8 contiguous
-// floats.  Four slots per thread are loaded before any is converted.
-template <int KIND>
-__device__ __forceinline__ void stage_operand(uint8_t *dst, uint32_t lo_off, const float *src,
-                                              long long s_row, long long s_k, int kmaj,
-                                              long long row0, long long rows, int R, long long k0,
-                                              long long kend, int tid) {
-  constexpr int Q = 4;
-  const int total = 8 * R;  // slots: R rows x 8 chunks, or R/8 row chunks x 64 k
-  for (int base = tid; base < total; base += Q * kProducerThreads) {
-    float v[Q][8];
-    int off[Q];
+// One operand's part of a stage: rows [row0, row0 + R) of k block
+// [k0, k0 + kBK), zero outside the matrix.  Element (row, k) is at
+// src[row*s_row + k] when kmaj (k contiguous), else at src[k*s_k + row], or
+// where the window gather `g` puts it.  Slot sl (0 .. 8R-1) is one 16-byte
+// destination and 8 contiguous source floats.
+//   K-major: slot sl = chunk c (sl % 8) of row r (sl / 8), at
+//   (c*(R+1) + r)*16: 8 consecutive lanes read one row's 256 contiguous
+//   bytes, and the planes' stride of R+1 chunks (1 mod 8) puts the 8
+//   chunks of a row in 8 different bank groups.
+//   MN-major: slot sl = row chunk j (sl % (R/8)) at k (sl / (R/8)), at
+//   (j*(kBK+1) + k)*16: consecutive lanes read consecutive row chunks of one
+//   k (contiguous), the plane stride kBK+1 keeps them in distinct banks.
+// Each warp-wide load therefore touches whole lines, not one line per lane.
+struct Operand {
+  const float *src;
+  long long s_row, s_k, row0, rows;
+  int kmaj, R;
+  uint32_t dst;  // byte offset of the operand's hi part in the stage
+};
+
+__device__ __forceinline__ void load_slot(const Operand &o, int sl, long long k0, long long kend,
+                                          const S2D &g, float (&v)[8], int &off) {
 #pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      const int sl = base + q * kProducerThreads;
+  for (int e = 0; e < 8; ++e) v[e] = 0.f;
+  const float *p = nullptr;
+  bool vec = false;
+  if (o.kmaj) {
+    const int c = sl & 7, r = sl >> 3;
+    off = (int)o.dst + (c * (o.R + 1) + r) * 16;
+    const long long row = o.row0 + r, k = k0 + 8 * c;
+    if (row < o.rows && k < kend) {
+      p = o.src + (g.on ? s2d_off(g, row, k) : row * o.s_row + k);
+      vec = k + 8 <= kend;
+      if (!vec)
+        for (int e = 0; e < 8; ++e)
+          if (k + e < kend) v[e] = __ldg(p + e);
+    }
+  } else {
+    const int nj = o.R >> 3;
+    const int kk = sl / nj, j = sl - kk * nj;
+    off = (int)o.dst + (j * (kBK + 1) + kk) * 16;
+    const long long k = k0 + kk, row = o.row0 + 8 * j;
+    if (k < kend && row < o.rows) {
+      p = o.src + (g.on ? s2d_off(g, k, row) : k * o.s_k + row);
+      vec = row + 8 <= o.rows;
+      if (!vec)
+        for (int e = 0; e < 8; ++e)
+          if (row + e < o.rows) v[e] = __ldg(p + e);
+    }
+  }
+  if (vec) {
+    if (((uintptr_t)p & 15) == 0) {
+      const float4 x0 = __ldg(reinterpret_cast<const float4 *>(p));
+      const float4 x1 = __ldg(reinterpret_cast<const float4 *>(p) + 1);
+      v[0] = x0.x; v[1] = x0.y; v[2] = x0.z; v[3] = x0.w;
+      v[4] = x1.x; v[5] = x1.y; v[6] = x1.z; v[7] = x1.w;
+    } else {
 #pragma unroll
-      for (int e = 0; e < 8; ++e) v[q][e] = 0.f;
-      off[q] = -1;
-      if (sl < total) {
-        if (kmaj) {
-          const int c = sl / R, r = sl - c * R;
-          off[q] = sl * 16;
-          const long long row = row0 + r, k = k0 + 8 * c;
-          if (row < rows && k < kend) {
-            const float *p = src + row * s_row + k;
-            if (k + 8 <= kend && ((uintptr_t)p & 15) == 0) {
-              const float4 x0 = __ldg(reinterpret_cast<const float4 *>(p));
-              const float4 x1 = __ldg(reinterpret_cast<const float4 *>(p) + 1);
-              v[q][0] = x0.x; v[q][1] = x0.y; v[q][2] = x0.z; v[q][3] = x0.w;
-              v[q][4] = x1.x; v[q][5] = x1.y; v[q][6] = x1.z; v[q][7] = x1.w;
-            } else {
+      for (int e = 0; e < 8; ++e) v[e] = __ldg(p + e);
+    }
+  }
+}
+
+// A whole stage (both operands) in one round per thread: every load of the
+// stage is issued first (up to kQ slots per thread, 2 x 16-byte loads
+// each), then `ready()` waits for the stage's buffer to be free, then the
+// values are converted and stored.  The loads' latency overlaps the wait.
+// slots per thread per stage: (8*128 + 8*256) / 480 producer threads <= 7
+constexpr int kQ = 7;
+static_assert(kQ * kProducerThreads >= 8 * (kBM + 256), "a stage must fit one round");
+
+// A thread's slots, resolved once per tile: where slot q's 8 floats of the
+// first k block are, how far they move per k block, and its destination.
+// A slot whose row lies outside the matrix has base == nullptr (zeros).
+struct Slots {
+  const float *base[kQ];
+  int off[kQ];
+  long long step_a, step_b;  // per k block, operand A's slots and B's
+};
+
+__device__ __forceinline__ long long slot_step(const Operand &o) {
+  return o.kmaj ? (long long)kBK : (long long)kBK * o.s_k;
+}
+
+__device__ __forceinline__ void slot_plan(const Operand &o, int sl, long long k_begin,
+                                          const float *&base, int &off) {
+  base = nullptr;
+  if (o.kmaj) {
+    const int c = sl & 7, r = sl >> 3;
+    off = (int)o.dst + (c * (o.R + 1) + r) * 16;
+    const long long row = o.row0 + r;
+    if (row < o.rows) base = o.src + row * o.s_row + k_begin + 8 * c;
+  } else {
+    const int nj = o.R >> 3;
+    const int kk = sl / nj, j = sl - kk * nj;
+    off = (int)o.dst + (j * (kBK + 1) + kk) * 16;
+    const long long row = o.row0 + 8 * j;
+    if (row + 8 <= o.rows) base = o.src + (k_begin + kk) * o.s_k + row;
+  }
+}
+
+// A whole stage (both operands) in one round per thread: every load of the
+// stage is issued first (up to kQ slots per thread, 2 x 16-byte loads
+// each), then `ready()` waits for the stage's buffer to be free, then the
+// values are converted and stored.  The loads' latency overlaps the wait.
+// `fast`: the k block lies wholly inside the matrix, the operands are read
+// through their strides and every source is 16-byte aligned, so each slot
+// is two vector loads at base + i*step; otherwise each slot is resolved in
+// full (matrix edges, the window gather).
+template <int KIND, class Ready>
+__device__ __forceinline__ bool stage_round(uint8_t *stage, uint32_t lo_a, uint32_t lo_b,
+                                            const Operand &A, const Operand &B, long long k0,
+                                            long long kend, const S2D &g, int tid,
+                                            const Slots &sp, bool fast, long long i, Ready ready) {
+  const int na = 8 * A.R, total = na + 8 * B.R;
+  const S2D none{};
+  float v[kQ][8];
+  int off[kQ];
+  if (fast) {
 #pragma unroll
-              for (int e = 0; e < 8; ++e)
-                if (k + e < kend) v[q][e] = __ldg(p + e);
-            }
-          }
-        } else {
-          const int j = sl / kBK, kk = sl - j * kBK;
-          off[q] = sl * 16;
-          const long long k = k0 + kk, row = row0 + 8 * j;
-          if (k < kend && row < rows) {
-            const float *p = src + k * s_k + row;
-            if (row + 8 <= rows && ((uintptr_t)p & 15) == 0) {
-              const float4 x0 = __ldg(reinterpret_cast<const float4 *>(p));
-              const float4 x1 = __ldg(reinterpret_cast<const float4 *>(p) + 1);
-              v[q][0] = x0.x; v[q][1] = x0.y; v[q][2] = x0.z; v[q][3] = x0.w;
-              v[q][4] = x1.x; v[q][5] = x1.y; v[q][6] = x1.z; v[q][7] = x1.w;
-            } else {
+    for (int q = 0; q < kQ; ++q) {
+      const int sl = tid + q * kProducerThreads;
+      off[q] = sl < total ? sp.off[q] : -1;
+      if (off[q] >= 0 && sp.base[q]) {
+        const float4 *p4 = reinterpret_cast<const float4 *>(
+            sp.base[q] + i * (sl < na ? sp.step_a : sp.step_b));
+        const float4 x0 = __ldg(p4), x1 = __ldg(p4 + 1);
+        v[q][0] = x0.x; v[q][1] = x0.y; v[q][2] = x0.z; v[q][3] = x0.w;
+        v[q][4] = x1.x; v[q][5] = x1.y; v[q][6] = x1.z; v[q][7] = x1.w;
+      } else {
 #pragma unroll
-              for (int e = 0; e < 8; ++e)
-                if (row + e < rows) v[q][e] = __ldg(p + e);
-            }
-          }
-        }
+        for (int e = 0; e < 8; ++e) v[q][e] = 0.f;
       }
     }
+  } else {
 #pragma unroll
-    for (int q = 0; q < Q; ++q)
-      if (off[q] >= 0) stage::put_chunk<KIND, 8>(dst + off[q], lo_off, v[q]);
+    for (int q = 0; q < kQ; ++q) {
+      const int sl = tid + q * kProducerThreads;
+      off[q] = -1;
+      if (sl < na) {
+        load_slot(A, sl, k0, kend, g, v[q], off[q]);
+      } else if (sl < total) {
+        load_slot(B, sl - na, k0, kend, none, v[q], off[q]);
+      }
+    }
   }
+  if (!ready()) return false;
+#pragma unroll
+  for (int q = 0; q < kQ; ++q)
+    if (off[q] >= 0) {
+      const uint32_t lo = off[q] < (int)B.dst ? lo_a : lo_b;
+      stage::put_chunk<KIND, 8>(stage + off[q], lo, v[q]);
+    }
+  return true;
 }
 
 template <int KIND>
@@ -190,20 +310,38 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(const __grid_const
     // ===================== producers =====================
     const int tid = threadIdx.x - 32;
     bool staged = true;
+    // the stage: A hi [, A lo], B hi [, B lo]
+    const Operand A{p.a, p.a_sm, p.a_sk, m0, p.M, p.a_kmaj, kBM, 0u};
+    const Operand B{p.b, p.b_sn, p.b_sk, n0, p.N, p.b_kmaj, p.BN, PARTS * p.a_bytes};
+    Slots sp;
+    const int na = 8 * kBM, total = na + 8 * p.BN;
+    sp.step_a = slot_step(A);
+    sp.step_b = slot_step(B);
+#pragma unroll
+    for (int q = 0; q < kQ; ++q) {
+      const int sl = tid + q * kProducerThreads;
+      sp.base[q] = nullptr;
+      sp.off[q] = -1;
+      if (sl < na) slot_plan(A, sl, k_begin, sp.base[q], sp.off[q]);
+      else if (sl < total) slot_plan(B, sl - na, k_begin, sp.base[q], sp.off[q]);
+    }
+    // plain strided operands whose rows start 16-byte aligned (the fast path)
+    const bool aligned = !p.s2d.on && ((uintptr_t)p.a & 15) == 0 && ((uintptr_t)p.b & 15) == 0 &&
+                         (p.a_kmaj ? p.a_sm % 4 == 0 : p.a_sk % 4 == 0) &&
+                         (p.b_kmaj ? p.b_sn % 4 == 0 : p.b_sk % 4 == 0);
     for (int i = 0; i < nkb; ++i) {
       const int st = i % p.NS;
-      if (!wait_bar(smem_u32(&empty[st]), (uint32_t)(((i / p.NS) & 1) ^ 1), abort_flag, p.status,
-                    p.spin_limit)) {
+      uint8_t *stg = smem + (size_t)st * stage_bytes;
+      const long long k0 = k_begin + (long long)i * kBK;
+      const bool fast = aligned && k0 + kBK <= k_end;
+      if (!stage_round<KIND>(stg, p.a_bytes, p.b_bytes, A, B, k0, k_end, p.s2d, tid, sp, fast, i,
+                             [&] {
+            return wait_bar(smem_u32(&empty[st]), (uint32_t)(((i / p.NS) & 1) ^ 1), abort_flag,
+                            p.status, p.spin_limit);
+          })) {
         staged = false;
         break;
       }
-      uint8_t *sa = smem + (size_t)st * stage_bytes;
-      uint8_t *sb = sa + PARTS * p.a_bytes;
-      const long long k0 = k_begin + (long long)i * kBK;
-      stage_operand<KIND>(sa, p.a_bytes, p.a, p.a_sm, p.a_sk, p.a_kmaj, m0, p.M, kBM, k0, k_end,
-                          tid);
-      stage_operand<KIND>(sb, p.b_bytes, p.b, p.b_sn, p.b_sk, p.b_kmaj, n0, p.N, p.BN, k0, k_end,
-                          tid);
       fence_proxy_async();
       mbar_arrive(smem_u32(&full[st]));
     }
@@ -257,12 +395,15 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(const __grid_const
   } else if (lane == 0) {
     // ===================== MMA issuer =====================
     const uint32_t s0 = smem_u32(smem);
-    // K-major: core matrices along k are R*16 bytes apart, along rows 128;
-    // MN-major: along k 128 bytes apart, along rows kBK*16.  One K = 16 step
-    // is two k chunks (K-major) or 16 k rows (MN-major), in 16-byte units.
-    const uint32_t a_lbo = p.a_kmaj ? kBM * 16 : 128, a_sbo = p.a_kmaj ? 128 : kBK * 16;
-    const uint32_t b_lbo = p.b_kmaj ? (uint32_t)p.BN * 16 : 128, b_sbo = p.b_kmaj ? 128 : kBK * 16;
-    const uint32_t a_step = p.a_kmaj ? 2 * kBM : 16, b_step = p.b_kmaj ? 2 * (uint32_t)p.BN : 16;
+    // K-major: core matrices along k are (R+1)*16 bytes apart, along rows
+    // 128; MN-major: along k 128 bytes apart, along rows (kBK+1)*16.  One
+    // K = 16 step is two k chunks (K-major) or 16 k rows (MN-major), in
+    // 16-byte units.
+    const uint32_t a_lbo = p.a_kmaj ? (kBM + 1) * 16 : 128, a_sbo = p.a_kmaj ? 128 : (kBK + 1) * 16;
+    const uint32_t b_lbo = p.b_kmaj ? (uint32_t)(p.BN + 1) * 16 : 128,
+                   b_sbo = p.b_kmaj ? 128 : (kBK + 1) * 16;
+    const uint32_t a_step = p.a_kmaj ? 2 * (kBM + 1) : 16,
+                   b_step = p.b_kmaj ? 2 * (uint32_t)(p.BN + 1) : 16;
     const uint32_t alo = p.a_bytes >> 4, blo = p.b_bytes >> 4;
     const uint32_t d = tmem_base, ds = tmem_base + p.small_off;
     uint32_t acc = 0;
@@ -358,28 +499,21 @@ int launch(const GemmParams &p, size_t smem, dim3 grid, cudaStream_t s) {
 
 int *tc_gemm_status_word() { return gemm_status_word(); }
 
-int tc_gemm(int prec, bool trans_a, bool trans_b, long long M, long long N, long long K,
-            const float *a, const float *b, float *c, const float *bias, int act,
-            cudaStream_t s) {
-  if (prec != OWLGPU_PREC_BF16 && prec != OWLGPU_PREC_BF16X3) return kErrUnsupported;
-  if (M == 0 || N == 0) return kOk;
-  if (K == 0) return kErrUnsupported;  // the caller fills act(bias)
+namespace {
+
+// Tiles, pipeline depth and split of a GEMM whose operands `p` describes
+// (a, b, strides, majorness, M, N, K, bias, act, s2d), then the launch and
+// the fixed-order sum of the splits into c.
+int gemm_run(int prec, GemmParams p, float *c, cudaStream_t s) {
+  const long long M = p.M, N = p.N, K = p.K;
+  const float *bias = p.bias;
+  const int act = p.act;
   const int kind = prec == OWLGPU_PREC_BF16X3 ? stage::K_BF16X3 : stage::K_BF16;
   const int parts = kind == stage::K_BF16X3 ? 2 : 1;
-  GemmParams p{};
-  p.a = a; p.b = b; p.bias = bias; p.act = act;
-  p.M = M; p.N = N; p.K = K;
-  // op(A) is M x K: stored [M][K] (k contiguous) or, transposed, [K][M]
-  p.a_kmaj = trans_a ? 0 : 1;
-  p.a_sm = trans_a ? 1 : K;
-  p.a_sk = trans_a ? M : 1;
-  // op(B) is K x N: stored [K][N] (n contiguous) or, transposed, [N][K]
-  p.b_kmaj = trans_b ? 1 : 0;
-  p.b_sn = trans_b ? K : 1;
-  p.b_sk = trans_b ? 1 : N;
   p.BN = N >= 256 ? 256 : (int)std::max<long long>(16, (N + 15) / 16 * 16);
-  p.a_bytes = (unsigned)(kBM * kBK * 2);
-  p.b_bytes = (unsigned)(p.BN * kBK * 2);
+  // one padded plane per k chunk (K-major) or per row chunk (MN-major)
+  p.a_bytes = (unsigned)(p.a_kmaj ? 8 * (kBM + 1) * 16 : (kBM / 8) * (kBK + 1) * 16);
+  p.b_bytes = (unsigned)(p.b_kmaj ? 8 * (p.BN + 1) * 16 : (p.BN / 8) * (kBK + 1) * 16);
   const size_t stage_bytes = (size_t)parts * (p.a_bytes + p.b_bytes);
   p.NS = (int)std::min<size_t>(4, (kSmemMax - 256) / stage_bytes);
   if (p.NS < 2) return kErrUnsupported;
@@ -426,6 +560,69 @@ int tc_gemm(int prec, bool trans_a, bool trans_b, long long M, long long N, long
   }
   if (part) scratch_free(part, s);
   return rc;
+}
+
+}  // namespace
+
+int tc_gemm(int prec, bool trans_a, bool trans_b, long long M, long long N, long long K,
+            const float *a, const float *b, float *c, const float *bias, int act,
+            cudaStream_t s) {
+  if (prec != OWLGPU_PREC_BF16 && prec != OWLGPU_PREC_BF16X3) return kErrUnsupported;
+  if (M == 0 || N == 0) return kOk;
+  if (K == 0) return kErrUnsupported;  // the caller fills act(bias)
+  GemmParams p{};
+  p.a = a; p.b = b; p.bias = bias; p.act = act;
+  p.M = M; p.N = N; p.K = K;
+  // op(A) is M x K: stored [M][K] (k contiguous) or, transposed, [K][M]
+  p.a_kmaj = trans_a ? 0 : 1;
+  p.a_sm = trans_a ? 1 : K;
+  p.a_sk = trans_a ? M : 1;
+  // op(B) is K x N: stored [K][N] (n contiguous) or, transposed, [N][K]
+  p.b_kmaj = trans_b ? 1 : 0;
+  p.b_sn = trans_b ? K : 1;
+  p.b_sk = trans_b ? 1 : N;
+  return gemm_run(prec, p, c, s);
+}
+
+// A convolution whose kernel equals its stride, without dilation or
+// padding, its windows tiling the input exactly (a transpose convolution's
+// backward passes with kernel = stride, patchify layers): forward and
+// backward_kernel are GEMMs over the windows, with operand A gathered from
+// the activation window by window (no im2col copy).
+//   forward:         y[p][co]        = sum_(t,ci) X[win(p) + t][ci] * W[t][ci][co]
+//   backward_kernel: dW[(t,ci)][co]  = sum_p      X[win(p) + t][ci] * dY[p][co]
+// Channel chunks of 8 must not straddle taps (Ci % 8 == 0).  TF32 runs the
+// split-BF16 GEMM, which is at least as accurate.
+int tc_conv_s2d(int prec, bool bwd_kernel, const ConvGeom &g, const float *x,
+                const float *w_or_dy, float *out, const float *bias, int act, cudaStream_t s) {
+  if (prec == OWLGPU_PREC_TF32) prec = OWLGPU_PREC_BF16X3;
+  if (prec != OWLGPU_PREC_BF16 && prec != OWLGPU_PREC_BF16X3) return kErrUnsupported;
+  const bool win = g.KC == g.sc && g.KR == g.sr && g.KD == g.sd && g.dc == 1 && g.dr == 1 &&
+                   g.dd == 1 && g.pc == 0 && g.pr == 0 && g.pd == 0 && g.IC == g.OC * g.sc &&
+                   g.IR == g.OR * g.sr && g.ID == g.OD * g.sd && g.taps() > 1 && g.Ci % 8 == 0;
+  if (!win) return kErrUnsupported;
+  if (g.out_pixels() == 0 || g.Ci == 0 || g.Co == 0) return kErrUnsupported;
+  if (g.out_pixels() >= (1LL << 31) || g.taps() * g.Ci >= (1LL << 31)) return kErrUnsupported;
+  GemmParams p{};
+  p.s2d.on = 1;
+  p.s2d.C = (unsigned)g.Ci;
+  p.s2d.KC = (unsigned)g.KC; p.s2d.KR = (unsigned)g.KR; p.s2d.KD = (unsigned)g.KD;
+  p.s2d.OC = (unsigned)g.OC; p.s2d.OR = (unsigned)g.OR; p.s2d.OD = (unsigned)g.OD;
+  p.s2d.IC = g.IC; p.s2d.IR = g.IR; p.s2d.ID = g.ID;
+  p.a = x;
+  p.b = w_or_dy;
+  p.N = g.Co;
+  // B is [K][N] row-major in both: W[(t,ci)][co] or dY[p][co]
+  p.b_kmaj = 0; p.b_sn = 1; p.b_sk = g.Co;
+  if (!bwd_kernel) {
+    p.M = g.out_pixels(); p.K = g.taps() * g.Ci;
+    p.a_kmaj = 1;  // rows = pixels, k = (tap, channel), 8 channels contiguous
+    p.bias = bias; p.act = act;
+  } else {
+    p.M = g.taps() * g.Ci; p.K = g.out_pixels();
+    p.a_kmaj = 0;  // rows = (tap, channel), 8 contiguous; k = pixels
+  }
+  return gemm_run(prec, p, out, s);
 }
 
 }  // namespace owlgpu

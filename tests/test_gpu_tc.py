@@ -275,3 +275,36 @@ def test_transpose_conv_tc(gpu_lib, f64_nn, prec, case):
     assert _path() == 1
     dw64 = getattr(f64_nn, f + "_backward_kernel")(x64, w64, list(st), dy.astype(np.float64))
     assert rel(dw, dw64) <= TOL[prec]
+
+
+# convolutions whose kernel equals their stride (non-overlapping windows,
+# the backward passes of a kernel = stride transpose convolution): forward
+# and backward_kernel run as a tcgen05 GEMM over the windows
+PATCH = [
+    ((2, 16, 16, 32), (4, 4, 32, 64), (4, 4), VALID),
+    ((3, 12, 10, 16), (2, 2, 16, 40), (2, 2), SAME),
+    ((1, 8, 6, 4, 24), (2, 2, 2, 24, 16), (2, 2, 2), VALID),
+]
+
+
+@pytest.mark.parametrize("prec", ["bf16", "tf32", "bf16x3"])
+@pytest.mark.parametrize("case", PATCH)
+def test_kernel_equals_stride_tc(gpu_lib, f64_nn, prec, case):
+    xs, ks, st, pad = case
+    rng = np.random.default_rng(28)
+    x = rng.uniform(-1, 1, xs).astype(np.float32)
+    w = (rng.standard_normal(ks) * 0.1).astype(np.float32)
+    G = _nn(prec)
+    f = "conv3d" if len(xs) == 5 else "conv2d"
+    x64, w64 = x.astype(np.float64), w.astype(np.float64)
+    y64 = getattr(f64_nn, f)(x64, w64, list(st), pad)
+    dy = rng.standard_normal(y64.shape).astype(np.float32)
+    dw = from_dev(getattr(G, f + "_backward_kernel")(to_dev(x), to_dev(w), list(st), to_dev(dy)))
+    assert _path() == 1
+    assert rel(dw, getattr(f64_nn, f + "_backward_kernel")(x64, w64, list(st),
+                                                            dy.astype(np.float64))) <= TOL[prec]
+    if prec == "tf32":
+        return  # a TF32 forward runs the convolution kernel (kind::tf32), tested above
+    y = from_dev(getattr(G, f)(to_dev(x), to_dev(w), list(st), pad))
+    assert _path() == 1
+    assert rel(y, y64) <= TOL[prec]
