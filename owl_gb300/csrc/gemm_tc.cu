@@ -181,6 +181,15 @@ __device__ __forceinline__ void load_slot(const Operand &o, int sl, long long k0
 constexpr int kQ = 7;
 static_assert(kQ * kProducerThreads >= 8 * (kBM + 256), "a stage must fit one round");
 
+// 8 floats in one 32-byte load (p 32-byte aligned), through the read-only
+// path: one L1 wavefront per lane instead of two 16-byte loads' two.
+__device__ __forceinline__ void ld8(const float *p, float (&v)[8]) {
+  asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]),
+                 "=f"(v[6]), "=f"(v[7])
+               : "l"(p));
+}
+
 // A thread's slots, resolved once per tile: where slot q's 8 floats of the
 // first k block are, how far they move per k block, and its destination.
 // A slot whose row lies outside the matrix has base == nullptr (zeros).
@@ -223,7 +232,8 @@ template <int KIND, class Ready>
 __device__ __forceinline__ bool stage_round(uint8_t *stage, uint32_t lo_a, uint32_t lo_b,
                                             const Operand &A, const Operand &B, long long k0,
                                             long long kend, const S2D &g, int tid,
-                                            const Slots &sp, bool fast, long long i, Ready ready) {
+                                            const Slots &sp, bool fast, bool wide, long long i,
+                                            Ready ready) {
   const int na = 8 * A.R, total = na + 8 * B.R;
   const S2D none{};
   float v[kQ][8];
@@ -234,11 +244,15 @@ __device__ __forceinline__ bool stage_round(uint8_t *stage, uint32_t lo_a, uint3
       const int sl = tid + q * kProducerThreads;
       off[q] = sl < total ? sp.off[q] : -1;
       if (off[q] >= 0 && sp.base[q]) {
-        const float4 *p4 = reinterpret_cast<const float4 *>(
-            sp.base[q] + i * (sl < na ? sp.step_a : sp.step_b));
-        const float4 x0 = __ldg(p4), x1 = __ldg(p4 + 1);
-        v[q][0] = x0.x; v[q][1] = x0.y; v[q][2] = x0.z; v[q][3] = x0.w;
-        v[q][4] = x1.x; v[q][5] = x1.y; v[q][6] = x1.z; v[q][7] = x1.w;
+        const float *src = sp.base[q] + i * (sl < na ? sp.step_a : sp.step_b);
+        if (wide) {
+          ld8(src, v[q]);
+        } else {
+          const float4 *p4 = reinterpret_cast<const float4 *>(src);
+          const float4 x0 = __ldg(p4), x1 = __ldg(p4 + 1);
+          v[q][0] = x0.x; v[q][1] = x0.y; v[q][2] = x0.z; v[q][3] = x0.w;
+          v[q][4] = x1.x; v[q][5] = x1.y; v[q][6] = x1.z; v[q][7] = x1.w;
+        }
       } else {
 #pragma unroll
         for (int e = 0; e < 8; ++e) v[q][e] = 0.f;
@@ -329,12 +343,17 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(const __grid_const
     const bool aligned = !p.s2d.on && ((uintptr_t)p.a & 15) == 0 && ((uintptr_t)p.b & 15) == 0 &&
                          (p.a_kmaj ? p.a_sm % 4 == 0 : p.a_sk % 4 == 0) &&
                          (p.b_kmaj ? p.b_sn % 4 == 0 : p.b_sk % 4 == 0);
+    // ... and 32-byte aligned: one 32-byte load per slot
+    const bool wide = aligned && ((uintptr_t)p.a & 31) == 0 && ((uintptr_t)p.b & 31) == 0 &&
+                      (p.a_kmaj ? p.a_sm % 8 == 0 : p.a_sk % 8 == 0) &&
+                      (p.b_kmaj ? p.b_sn % 8 == 0 : p.b_sk % 8 == 0);
     for (int i = 0; i < nkb; ++i) {
       const int st = i % p.NS;
       uint8_t *stg = smem + (size_t)st * stage_bytes;
       const long long k0 = k_begin + (long long)i * kBK;
       const bool fast = aligned && k0 + kBK <= k_end;
-      if (!stage_round<KIND>(stg, p.a_bytes, p.b_bytes, A, B, k0, k_end, p.s2d, tid, sp, fast, i,
+      if (!stage_round<KIND>(stg, p.a_bytes, p.b_bytes, A, B, k0, k_end, p.s2d, tid, sp, fast,
+                             wide, i,
                              [&] {
             return wait_bar(smem_u32(&empty[st]), (uint32_t)(((i / p.NS) & 1) ^ 1), abort_flag,
                             p.status, p.spin_limit);

@@ -74,14 +74,25 @@ __global__ void bias_act_bwd_kernel(const T *__restrict__ y, const T *__restrict
   }
 }
 
+// out[c] = sum over chunks of partial[chunk][c]: block (32, 32), x = channel
+// of a 32-channel tile, y = one of 32 interleaved chunk sets (y, y + 32,
+// ...) summed in order, then the 32 set sums added in order (a fixed order
+// whatever the run).
 template <typename T>
 __global__ void sum_chunks_kernel(const T *__restrict__ partial, T *__restrict__ out, long long C,
                                   int chunks) {
-  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < C;
-       c += (long long)gridDim.x * blockDim.x) {
-    T s = partial[c];
-    for (int k = 1; k < chunks; ++k) s += partial[(long long)k * C + c];
-    out[c] = s;
+  __shared__ T red[32][33];
+  const long long c = (long long)blockIdx.x * 32 + threadIdx.x;
+  T s = T(0);
+  if (c < C)
+    for (int k = threadIdx.y; k < chunks; k += 32) s += partial[(long long)k * C + c];
+  red[threadIdx.y][threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.y == 0 && c < C) {
+    T t = red[0][threadIdx.x];
+#pragma unroll 8
+    for (int r = 1; r < 32; ++r) t += red[r][threadIdx.x];
+    out[c] = t;
   }
 }
 
@@ -255,7 +266,7 @@ int bias_act_bwd_t(const char *fn, const T *y, const T *dy, T *dz, T *db, long P
   note_launch();
   int rc = e == cudaSuccess ? kOk : cuda_fail(e, "bias_act_bwd_kernel");
   if (rc == kOk && db) {
-    sum_chunks_kernel<T><<<grid_for(C, 256), 256, 0, s>>>(part, db, C, (int)chunks);
+    sum_chunks_kernel<T><<<(unsigned)ctiles, dim3(32, 32), 0, s>>>(part, db, C, (int)chunks);
     e = cudaGetLastError();
     note_launch();
     if (e != cudaSuccess) rc = cuda_fail(e, "sum_chunks_kernel");
