@@ -45,6 +45,7 @@
 #include "../../include/owlgpu.h"
 #include "common.cuh"
 #include "tc_ptx.cuh"
+#include "tc_stage.cuh"
 
 namespace owlgpu {
 namespace {
@@ -306,12 +307,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
                 if (row_ok && iv >= 0 && iv < p.IV && c < p.Cin) {
                   const float *src = rowp + hc * vstep + j * EPC;
                   if (p.vec_in && c + EPC <= p.Cin) {
-#pragma unroll
-                    for (int e = 0; e < EPC; e += 4) {
-                      float4 f = __ldg(reinterpret_cast<const float4 *>(src + e));
-                      v[rr][q][e] = f.x; v[rr][q][e + 1] = f.y;
-                      v[rr][q][e + 2] = f.z; v[rr][q][e + 3] = f.w;
-                    }
+                    stage::load_vec<EPC>(src, p.vec_in, v[rr][q]);
                   } else {
 #pragma unroll
                     for (int e = 0; e < EPC; ++e)
@@ -1083,7 +1079,10 @@ int run_segs(int prec, int nseg_in, const SegSpec *sp, bool bwd_input, int Ci, i
   }
   p.total_tiles = tiles;
   p.idesc = instr_desc(kind == K_TF32 ? 2u : 1u, (uint32_t)(128 * p.MH));
-  p.vec_in = ((uintptr_t)x % 16 == 0) && (pv.Cin % 4 == 0);
+  // 1: 16-byte vector loads; 2: 32-byte aligned chunks (one load per chunk)
+  p.vec_in = ((uintptr_t)x % 32 == 0 && pv.Cin % 8 == 0)
+                 ? 2
+                 : (((uintptr_t)x % 16 == 0) && (pv.Cin % 4 == 0) ? 1 : 0);
   p.spin_limit = wait_limit();
   p.status = status_ptr();
   if (!p.status) {

@@ -241,14 +241,14 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const __grid_cons
         // at most one row of each per warp: both rows in one pass
         stage::RowSet sx{xd, p.x_bytes, (uint32_t)p.PS * 16, xrows, HVR, XPL, p.Ci - xcb};
         stage::RowSet sy{yd, p.y_bytes, (uint32_t)p.YPS * 16, p.TU, 8, YPL, p.Co - ycb};
-        stage::stage_rows2<KIND, EPC, 5, 4>(sx, xrow, sy, yrow, p.vec_x != 0 && p.vec_y != 0,
+        stage::stage_rows2<KIND, EPC, 5, 4>(sx, xrow, sy, yrow, min(p.vec_x, p.vec_y),
                                             pidx, kProducerWarps, lane);
       } else {
         stage::stage_rows<KIND, EPC, 6>(xd, p.x_bytes, (uint32_t)p.PS * 16, xrows, HVR, XPL,
-                                        p.Ci - xcb, p.vec_x != 0, pidx, kProducerWarps, lane,
+                                        p.Ci - xcb, p.vec_x, pidx, kProducerWarps, lane,
                                         xrow);
         stage::stage_rows<KIND, EPC, 4>(yd, p.y_bytes, (uint32_t)p.YPS * 16, p.TU, 8, YPL,
-                                        p.Co - ycb, p.vec_y != 0, pidx, kProducerWarps, lane,
+                                        p.Co - ycb, p.vec_y, pidx, kProducerWarps, lane,
                                         yrow);
       }
       fence_proxy_async();
@@ -641,8 +641,13 @@ int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, c
   uint32_t idesc = instr_desc(kind == K_TF32 ? 2u : 1u, (uint32_t)p.BN);
   idesc |= (1u << 15) | (1u << 16);  // A and B MN-major
   p.idesc = idesc;
-  p.vec_x = ((uintptr_t)x % 16 == 0) && (p.Ci % 4 == 0);
-  p.vec_y = ((uintptr_t)dy % 16 == 0) && (p.Co % 4 == 0);
+  // 1: 16-byte vector loads; 2: 32-byte aligned chunks (one load per chunk)
+  auto vec_of = [](const float *a, long long ch) {
+    if ((uintptr_t)a % 32 == 0 && ch % 8 == 0) return 2;
+    return ((uintptr_t)a % 16 == 0 && ch % 4 == 0) ? 1 : 0;
+  };
+  p.vec_x = vec_of(x, p.Ci);
+  p.vec_y = vec_of(dy, p.Co);
   p.spin_limit = wait_limit();
   p.status = status_word();
   if (!p.status) {

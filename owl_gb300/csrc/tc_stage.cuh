@@ -25,6 +25,30 @@ __device__ __forceinline__ uint32_t to_tf32(float a) {
   return r;
 }
 
+// 8 floats in one 32-byte load through the read-only path (p 32-byte
+// aligned): one L1 wavefront per lane where two 16-byte loads take two.
+__device__ __forceinline__ void ld8(const float *p, float *v) {
+  asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]),
+                 "=f"(v[6]), "=f"(v[7])
+               : "l"(p));
+}
+
+// EPC floats from src: vec 2 = 32-byte aligned (one 32-byte load when EPC
+// is 8), else 16-byte vector loads.
+template <int EPC>
+__device__ __forceinline__ void load_vec(const float *src, int vec, float *v) {
+  if (EPC == 8 && vec >= 2) {
+    ld8(src, v);
+  } else {
+#pragma unroll
+    for (int e = 0; e < EPC; e += 4) {
+      float4 f = __ldg(reinterpret_cast<const float4 *>(src + e));
+      v[e] = f.x; v[e + 1] = f.y; v[e + 2] = f.z; v[e + 3] = f.w;
+    }
+  }
+}
+
 template <int KIND, int EPC>
 __device__ __forceinline__ void put_chunk(uint8_t *dst, uint32_t lo_off, const float (&v)[EPC]) {
   uint4 hi;
@@ -61,7 +85,7 @@ struct Row {
 // requests in flight.
 template <int KIND, int EPC, int BATCH, class RowFn>
 __device__ __forceinline__ void stage_rows(uint8_t *dst, uint32_t lo_off, uint32_t plane_bytes,
-                                           int nrows, int npix, int nch, int clim, bool vec,
+                                           int nrows, int npix, int nch, int clim, int vec,
                                            int warp, int nwarps, int lane, RowFn rowfn) {
   const int S = npix * nch;
   const int nsh = (nch & (nch - 1)) == 0 ? __ffs(nch) - 1 : -1;
@@ -85,11 +109,7 @@ __device__ __forceinline__ void stage_rows(uint8_t *dst, uint32_t lo_off, uint32
           if (row.ok && vv >= 0 && vv < row.vlim && c < clim) {
             const float *src = row.rowp + (long long)i * row.pstep + c;
             if (vec && c + EPC <= clim) {
-#pragma unroll
-              for (int e = 0; e < EPC; e += 4) {
-                float4 f = __ldg(reinterpret_cast<const float4 *>(src + e));
-                v[q][e] = f.x; v[q][e + 1] = f.y; v[q][e + 2] = f.z; v[q][e + 3] = f.w;
-              }
+load_vec<EPC>(src, vec, v[q]);
             } else {
 #pragma unroll
               for (int e = 0; e < EPC; ++e)
@@ -125,7 +145,7 @@ struct RowSet {
 // single round trip to memory.
 template <int KIND, int EPC, int BA, int BB, class FnA, class FnB>
 __device__ __forceinline__ void stage_rows2(const RowSet &A, FnA rowa, const RowSet &Bs,
-                                            FnB rowb, bool vec, int warp, int nwarps,
+                                            FnB rowb, int vec, int warp, int nwarps,
                                             int lane) {
   const int SA = A.npix * A.nch, SB = Bs.npix * Bs.nch;
   const int nshA = (A.nch & (A.nch - 1)) == 0 ? __ffs(A.nch) - 1 : -1;
@@ -156,11 +176,7 @@ __device__ __forceinline__ void stage_rows2(const RowSet &A, FnA rowa, const Row
           if (ra.ok && vv >= 0 && vv < ra.vlim && c < A.clim) {
             const float *src = ra.rowp + (long long)i * ra.pstep + c;
             if (vec && c + EPC <= A.clim) {
-#pragma unroll
-              for (int e = 0; e < EPC; e += 4) {
-                float4 f = __ldg(reinterpret_cast<const float4 *>(src + e));
-                va[q][e] = f.x; va[q][e + 1] = f.y; va[q][e + 2] = f.z; va[q][e + 3] = f.w;
-              }
+load_vec<EPC>(src, vec, va[q]);
             } else {
 #pragma unroll
               for (int e = 0; e < EPC; ++e)
@@ -183,11 +199,7 @@ __device__ __forceinline__ void stage_rows2(const RowSet &A, FnA rowa, const Row
           if (rb.ok && vv >= 0 && vv < rb.vlim && c < Bs.clim) {
             const float *src = rb.rowp + (long long)i * rb.pstep + c;
             if (vec && c + EPC <= Bs.clim) {
-#pragma unroll
-              for (int e = 0; e < EPC; e += 4) {
-                float4 f = __ldg(reinterpret_cast<const float4 *>(src + e));
-                vb[q][e] = f.x; vb[q][e + 1] = f.y; vb[q][e + 2] = f.z; vb[q][e + 3] = f.w;
-              }
+load_vec<EPC>(src, vec, vb[q]);
             } else {
 #pragma unroll
               for (int e = 0; e < EPC; ++e)
