@@ -178,3 +178,15 @@ def test_sgd_update(gpu_lib):
     wd = to_dev(w)
     _layers().sgd_update(wd, to_dev(g), 0.01)
     assert np.array_equal(from_dev(wd), w - np.float32(0.01) * g)
+
+
+def test_bias_act_backward_ragged_channels(gpu_lib):
+    """Channel counts off the 32-channel tile and few pixels (one chunk)."""
+    rng = np.random.default_rng(59)
+    for shape in [(3, 70), (1000, 33), (5, 1)]:
+        y = np.maximum(rng.standard_normal(shape), 0).astype(np.float32)
+        dy = rng.standard_normal(shape).astype(np.float32)
+        dz, db = _layers().bias_act_backward(to_dev(y), to_dev(dy), 1)
+        assert np.array_equal(from_dev(dz), dy * (y > 0))
+        ref = (dy * (y > 0)).astype(np.float64).sum(axis=0)
+        assert np.max(np.abs(from_dev(db) - ref)) <= 1e-5 * max(np.max(np.abs(ref)), 1.0)

@@ -308,3 +308,17 @@ def test_kernel_equals_stride_tc(gpu_lib, f64_nn, prec, case):
     y = from_dev(getattr(G, f)(to_dev(x), to_dev(w), list(st), pad))
     assert _path() == 1
     assert rel(y, y64) <= TOL[prec]
+
+
+def test_kernel_equals_stride_with_channels_off_the_chunk_runs_the_conv_kernel(gpu_lib, f64_nn):
+    """Channels that are not a multiple of 8 cannot be gathered window by
+    window in whole chunks: the convolution kernel runs instead, still on
+    the tensor cores, with the same results."""
+    rng = np.random.default_rng(29)
+    x = rng.uniform(-1, 1, (3, 8, 8, 12)).astype(np.float32)
+    w = (rng.standard_normal((2, 2, 12, 20)) * 0.2).astype(np.float32)
+    G = _nn("bf16")
+    y = from_dev(G.conv2d(to_dev(x), to_dev(w), [2, 2], VALID))
+    assert _path() == 1
+    assert rel(y, f64_nn.conv2d(x.astype(np.float64), w.astype(np.float64), [2, 2],
+                                VALID)) <= TOL["bf16"]

@@ -94,3 +94,27 @@ def test_captured_call_launches_no_relayout(declared):
     g.replay()
     assert np.array_equal(from_dev(y), ref)
     del g
+
+
+@pytest.mark.parametrize("case", ["strided", "transpose"])
+def test_cached_multi_segment_layouts(declared, case):
+    """Layouts with several segments: a stride-2 backward_input (one
+    segment per residue class) and a kernel = stride transpose convolution
+    (classes fused into one launch): cached images give the per-call
+    results bit for bit."""
+    rng = np.random.default_rng(64)
+    G = _nn()
+    if case == "strided":
+        x = to_dev(rng.uniform(-1, 1, (2, 15, 15, 32)).astype(np.float32))
+        w_np = (rng.standard_normal((3, 3, 32, 64)) * 0.08).astype(np.float32)
+        dy = to_dev(rng.standard_normal((2, 7, 7, 64)).astype(np.float32))
+        run = lambda w: G.conv2d_backward_input(x, w, [2, 2], dy)
+    else:
+        x = to_dev(rng.uniform(-1, 1, (2, 7, 9, 48)).astype(np.float32))
+        w_np = (rng.standard_normal((2, 2, 48, 40)) * 0.2).astype(np.float32)
+        run = lambda w: G.transpose_conv2d(x, w, [2, 2], "SAME")
+    ref = from_dev(run(to_dev(w_np)))
+    w = to_dev(w_np)
+    declared(w, 3)
+    for _ in range(2):
+        assert np.array_equal(from_dev(run(w)), ref)
