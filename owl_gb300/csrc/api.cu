@@ -397,15 +397,18 @@ static int host_call(std::vector<Buf> bufs, int64_t batch, int chunks, F body,
       if (e != cudaSuccess) { rc = cuda_fail(e, "cudaMemcpyAsync(D2H)"); break; }
     }
   }
+  // the watchdog status words ride on the compute stream's synchronisation
+  const bool tc = take_tc_launched();
+  if (rc == kOk && tc) rc = tc_status_enqueue(hs->s);
   cudaError_t e1 = one ? cudaSuccess : cudaStreamSynchronize(hs->cin);
   cudaError_t e2 = cudaStreamSynchronize(hs->s);
   cudaError_t e3 = one ? cudaSuccess : cudaStreamSynchronize(hs->cout);
   for (auto &b : bufs) scratch_free(b.dev, hs->s);
   cudaError_t e = e1 != cudaSuccess ? e1 : e2 != cudaSuccess ? e2 : e3;
   if (rc == kOk && e != cudaSuccess) rc = cuda_fail(e, "cudaStreamSynchronize");
-  if (rc == kOk && take_tc_launched()) {
+  if (rc == kOk && tc) {
     int st = 0;
-    rc = tc_read_status(&st, hs->s);
+    rc = tc_status_take(&st, hs->s);
     if (rc == kOk && st) {
       set_error("a tensor-core kernel gave up waiting on one of its pipeline barriers");
       rc = kErrTimeout;

@@ -244,6 +244,11 @@ long long set_wait_limit(long long cycles);
 
 // Read (and clear) the tensor-core kernels' device error word on stream s.
 int tc_read_status(int *out, cudaStream_t s);
+// The same in two steps around a synchronisation the caller makes anyway:
+// enqueue the copies of the status words on s, then (after s has been
+// synchronised) take their value and clear the words that were set.
+int tc_status_enqueue(cudaStream_t s);
+int tc_status_take(int *out, cudaStream_t s);
 int *tc_wgrad_status_word();  // device address of the weight-gradient kernel's status word
 int *tc_gemm_status_word();   // device address of the tensor-core GEMM's status word
 // out[i] = sum over r = 0 .. R-1 of part[r * n + i], in that order.

@@ -1367,17 +1367,46 @@ int tc_conv_bwd_input(int prec, const ConvGeom &g, float *dx, const float *w, co
 
 // The tensor-core kernels' status words (convolution, weight gradient,
 // GEMM), read with one synchronisation and cleared when set.
-int tc_read_status(int *out, cudaStream_t s) {
+// The three status words are copied into page-locked host memory of the
+// calling thread, so the copies are asynchronous and a host drop-in call can
+// enqueue them before its final synchronisation instead of after it.
+int *status_host() {
+  static thread_local int *h = nullptr;
+  if (!h) {
+    void *q = nullptr;
+    if (cudaHostAlloc(&q, 4 * sizeof(int), cudaHostAllocDefault) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    h = static_cast<int *>(q);
+  }
+  return h;
+}
+
+int tc_status_enqueue(cudaStream_t s) {
   int *w[3] = {status_ptr(), tc_wgrad_status_word(), tc_gemm_status_word()};
-  if (!w[0] || !w[1] || !w[2]) return kErrCuda;
-  int v[3] = {0, 0, 0};
+  int *h = status_host();
+  if (!w[0] || !w[1] || !w[2] || !h) return kErrCuda;
   for (int i = 0; i < 3; ++i)
-    OWL_CUDA(cudaMemcpyAsync(&v[i], w[i], sizeof(int), cudaMemcpyDeviceToHost, s));
-  OWL_CUDA(cudaStreamSynchronize(s));
-  for (int i = 0; i < 3; ++i)
-    if (v[i]) OWL_CUDA(cudaMemsetAsync(w[i], 0, sizeof(int), s));
-  *out = v[0] | v[1] | v[2];
+    OWL_CUDA(cudaMemcpyAsync(&h[i], w[i], sizeof(int), cudaMemcpyDeviceToHost, s));
   return kOk;
+}
+
+int tc_status_take(int *out, cudaStream_t s) {
+  int *w[3] = {status_ptr(), tc_wgrad_status_word(), tc_gemm_status_word()};
+  const int *h = status_host();
+  if (!w[0] || !w[1] || !w[2] || !h) return kErrCuda;
+  for (int i = 0; i < 3; ++i)
+    if (h[i]) OWL_CUDA(cudaMemsetAsync(w[i], 0, sizeof(int), s));
+  *out = h[0] | h[1] | h[2];
+  return kOk;
+}
+
+int tc_read_status(int *out, cudaStream_t s) {
+  int rc = tc_status_enqueue(s);
+  if (rc) return rc;
+  OWL_CUDA(cudaStreamSynchronize(s));
+  return tc_status_take(out, s);
 }
 
 }  // namespace owlgpu
