@@ -333,6 +333,282 @@ __global__ void splitk_reduce_kernel(const T *__restrict__ part, T *__restrict__
   }
 }
 
+// ---- float32 vector path ----------------------------------------------------
+// The same GEMM views in float32 with 16-byte operand gathers: 128 x 128
+// tiles, 16-deep k slabs, 256 threads of 8 x 8 outputs (four 4 x 4
+// quadrants, rows ty*4 and 64 + ty*4, columns tx*4 and 64 + tx*4, so every
+// shared-memory fragment is one 16-byte load without bank conflicts).
+// Shared-memory wavefronts, not the FMA pipe, bound this kind of kernel:
+// four per warp and k against 64 FMAs.
+//   FWD : a slab is 16 consecutive input channels of one tap (Ci % 16 == 0);
+//         four threads read one pixel's 64 bytes, and each thread's two
+//         output pixels are decoded once per CTA.  A is stored k-major with
+//         its row index XOR-swizzled by the channel quad (k / 4) * 8, so the
+//         four threads of a pixel write four different bank groups.
+//   BWDK: a slab is 16 consecutive output pixels; a thread reads four
+//         consecutive (tap, ci) rows of one pixel (Ci % 4 == 0), a warp one
+//         pixel's 128 rows; the slab's pixels are decoded by 16 threads into
+//         shared memory one slab ahead.
+// The k order of every output's sum is the same as the scalar kernel's
+// (ascending, one fused multiply-add per k), so a float32 forward gives the
+// same bits on either path.
+constexpr int kVBM = 128, kVBN = 128, kVBK = 16, kVNT = 256;
+
+__device__ __forceinline__ float4 ldg4(const float *p) {
+  return __ldg(reinterpret_cast<const float4 *>(p));
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kVNT, 1)
+    conv_f32v_kernel(Dev g, const float *__restrict__ A0, const float *__restrict__ B0,
+                     float *__restrict__ C, int64_t k_per_split) {
+  __shared__ __align__(16) float As[2][kVBK][kVBM];
+  __shared__ __align__(16) float Bs[2][kVBK][kVBN];
+  __shared__ int64_t s_base[2][kVBK];  // BWDK: slab pixels (batch image offset, -1 past the end)
+  __shared__ int s_c[2][kVBK], s_r[2][kVBK], s_d[2][kVBK];
+
+  const int tid = threadIdx.x;
+  // a warp covers 8 row groups x 4 column groups: its 16-byte fragment loads
+  // touch 128 contiguous bytes of A and 64 of B (one shared-memory wavefront
+  // each) per k
+  const int lane = tid & 31, warp = tid >> 5;
+  const int ty = (warp >> 2) * 8 + (lane >> 2), tx = (warp & 3) * 4 + (lane & 3);
+  const int64_t m0 = (int64_t)blockIdx.x * kVBM, n0 = (int64_t)blockIdx.y * kVBN;
+  const int64_t k_begin = (int64_t)blockIdx.z * k_per_split;
+  const int64_t k_end = min(g.K, k_begin + k_per_split);
+  const int64_t img = g.IC * g.IR * g.ID;  // pixels per batch image of X
+
+  // ---- FWD: this thread's two output pixels and its channel quad ----------
+  const int aq = tid & 3;  // FWD: channel quad within the slab
+  int64_t abase[2] = {-1, -1};
+  int ac[2] = {0, 0}, ar[2] = {0, 0}, ad[2] = {0, 0};
+  // ---- BWDK: this thread's four (tap, ci) rows ----------------------------
+  const int mq = (tid & 31) * 4;  // BWDK: row quad within the tile
+  bool mval = false;
+  int t_dc = 0, t_dr = 0, t_dd = 0;
+  int64_t mci = 0;
+  if (MODE == FWD) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int64_t m = m0 + (tid >> 2) + 64 * h;
+      if (m < g.M) {
+        int64_t t = m;
+        const int64_t od = t % g.OD;
+        t /= g.OD;
+        const int64_t orr = t % g.OR;
+        t /= g.OR;
+        const int64_t oc = t % g.OC, b = t / g.OC;
+        abase[h] = b * img;
+        ac[h] = (int)(oc * g.sc) - g.pc;
+        ar[h] = (int)(orr * g.sr) - g.pr;
+        ad[h] = (int)(od * g.sd) - g.pd;
+      }
+    }
+  } else {
+    const int64_t m = m0 + mq;
+    if (m < g.M) {
+      mval = true;
+      int64_t tap = m / g.Ci;
+      mci = m - tap * g.Ci;
+      const int kd = (int)(tap % g.KD);
+      tap /= g.KD;
+      const int kr = (int)(tap % g.KR), kc = (int)(tap / g.KR);
+      t_dc = kc * g.dc;
+      t_dr = kr * g.dr;
+      t_dd = kd * g.dd;
+    }
+  }
+  // BWDK: decode pixel p into slot `slot` of buffer `buf` (-1 past k_end)
+  auto decode = [&](int64_t p, int slot, int buf) {
+    if (p < k_end) {
+      int64_t t = p;
+      const int64_t od = t % g.OD;
+      t /= g.OD;
+      const int64_t orr = t % g.OR;
+      t /= g.OR;
+      const int64_t oc = t % g.OC, b = t / g.OC;
+      s_base[buf][slot] = b * img;
+      s_c[buf][slot] = (int)(oc * g.sc) - g.pc;
+      s_r[buf][slot] = (int)(orr * g.sr) - g.pr;
+      s_d[buf][slot] = (int)(od * g.sd) - g.pd;
+    } else {
+      s_base[buf][slot] = -1;
+    }
+  };
+
+  // FWD slab position: tap (kc, kr, kd) and first channel ci0 of slab k0
+  int kc = 0, kr = 0, kd = 0;
+  int64_t ci0 = 0;
+  if (MODE == FWD) {
+    int64_t tap = k_begin / g.Ci;
+    ci0 = k_begin - tap * g.Ci;
+    kd = (int)(tap % g.KD);
+    tap /= g.KD;
+    kr = (int)(tap % g.KR);
+    kc = (int)(tap / g.KR);
+  }
+
+  float4 va[2], vb[2];
+  const int bcol = (tid & 31) * 4, bk = tid >> 5;
+  const bool bval = n0 + bcol < g.N;
+
+  // global -> registers for slab k0 (FWD: at tap kc/kr/kd, channels ci0..)
+  auto load = [&](int64_t k0, int buf) {
+    if (MODE == FWD) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int c = ac[h] + kc * g.dc, r = ar[h] + kr * g.dr, d = ad[h] + kd * g.dd;
+        va[h] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (abase[h] >= 0 && (unsigned)c < (unsigned)g.IC && (unsigned)r < (unsigned)g.IR &&
+            (unsigned)d < (unsigned)g.ID)
+          va[h] = ldg4(A0 + (abase[h] + ((int64_t)c * g.IR + r) * g.ID + d) * g.Ci + ci0 + aq * 4);
+      }
+    } else {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int kl = bk + 8 * h;
+        const int64_t base = s_base[buf][kl];
+        va[h] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (mval && base >= 0) {
+          const int c = s_c[buf][kl] + t_dc, r = s_r[buf][kl] + t_dr, d = s_d[buf][kl] + t_dd;
+          if ((unsigned)c < (unsigned)g.IC && (unsigned)r < (unsigned)g.IR &&
+              (unsigned)d < (unsigned)g.ID)
+            va[h] = ldg4(A0 + (base + ((int64_t)c * g.IR + r) * g.ID + d) * g.Ci + mci);
+        }
+      }
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int64_t kq = k0 + bk + 8 * h;
+      vb[h] = (bval && kq < k_end) ? ldg4(B0 + kq * g.N + n0 + bcol)
+                                   : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  };
+  auto store = [&](int buf) {
+    if (MODE == FWD) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int row = ((tid >> 2) + 64 * h) ^ (aq << 3);
+        As[buf][aq * 4 + 0][row] = va[h].x;
+        As[buf][aq * 4 + 1][row] = va[h].y;
+        As[buf][aq * 4 + 2][row] = va[h].z;
+        As[buf][aq * 4 + 3][row] = va[h].w;
+      }
+    } else {
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+        *reinterpret_cast<float4 *>(&As[buf][bk + 8 * h][mq]) = va[h];
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) *reinterpret_cast<float4 *>(&Bs[buf][bk + 8 * h][bcol]) = vb[h];
+  };
+  auto next_tap = [&]() {
+    ci0 += kVBK;
+    if (ci0 == g.Ci) {
+      ci0 = 0;
+      if (++kd == g.KD) {
+        kd = 0;
+        if (++kr == g.KR) {
+          kr = 0;
+          ++kc;
+        }
+      }
+    }
+  };
+
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+
+  if (k_begin < k_end) {
+    if (MODE == BWDK) {
+      if (tid < kVBK) decode(k_begin + tid, tid, 0);
+      if (tid >= kVBK && tid < 2 * kVBK) decode(k_begin + kVBK + tid - kVBK, tid - kVBK, 1);
+      __syncthreads();
+    }
+    load(k_begin, 0);
+    store(0);
+    if (MODE == FWD) next_tap();
+    __syncthreads();
+    int buf = 0;
+    for (int64_t k0 = k_begin; k0 < k_end; k0 += kVBK) {
+      const int64_t kn = k0 + kVBK;
+      const bool more = kn < k_end;
+      if (more) load(kn, buf ^ 1);  // BWDK: slab kn's pixels sit in buffer buf ^ 1
+      // BWDK: decode slab kn + 16 into this slab's (now unused) buffer
+      if (MODE == BWDK && tid < kVBK) decode(kn + kVBK + tid, tid, buf);
+#pragma unroll
+      for (int k = 0; k < kVBK; ++k) {
+        const int sw = MODE == FWD ? ((k >> 2) << 3) : 0;
+        const float4 a0 = *reinterpret_cast<const float4 *>(&As[buf][k][(ty * 4) ^ sw]);
+        const float4 a1 = *reinterpret_cast<const float4 *>(&As[buf][k][(64 + ty * 4) ^ sw]);
+        const float4 b0 = *reinterpret_cast<const float4 *>(&Bs[buf][k][tx * 4]);
+        const float4 b1 = *reinterpret_cast<const float4 *>(&Bs[buf][k][64 + tx * 4]);
+        const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+        const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+          for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+      }
+      if (more) {
+        store(buf ^ 1);
+        if (MODE == FWD) next_tap();
+      }
+      __syncthreads();
+      buf ^= 1;
+    }
+  }
+
+  float *Cz = C + (int64_t)blockIdx.z * g.M * g.N;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int64_t m = m0 + (i < 4 ? ty * 4 + i : 64 + ty * 4 + i - 4);
+    if (m >= g.M) continue;
+    int64_t row = m;
+    if (MODE == FWD && g.ystrided) {
+      int64_t t = m;
+      const int64_t od = t % g.OD;
+      t /= g.OD;
+      const int64_t orr = t % g.OR;
+      t /= g.OR;
+      const int64_t oc = t % g.OC, b = t / g.OC;
+      row = g.yoff + b * g.ysb + oc * g.ysc + orr * g.ysr + od * g.ysd;
+    }
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int64_t n = n0 + q * 64 + tx * 4;
+      if (n < g.N)
+        *reinterpret_cast<float4 *>(Cz + row * g.N + n) =
+            make_float4(acc[i][4 * q], acc[i][4 * q + 1], acc[i][4 * q + 2], acc[i][4 * q + 3]);
+    }
+  }
+}
+
+// Whether the float32 vector path takes a launch: 16-byte aligned operands,
+// N a multiple of 4 above 64 (the 128-wide tile), FWD slabs inside one tap
+// (Ci % 16, whole slabs per split), BWDK rows in quads of one tap (Ci % 4).
+bool f32v_ok(int mode, const Dev &d, const void *A, const void *B, const void *C,
+             int64_t kps) {
+  auto al = [](const void *p) { return ((uintptr_t)p & 15) == 0; };
+  if (!al(A) || !al(B) || !al(C) || d.N % 4 != 0 || d.N <= 64) return false;
+  if (d.IC >= (1 << 30) || d.IR >= (1 << 30) || d.ID >= (1 << 30)) return false;
+  if (mode == FWD) return d.Ci % kVBK == 0 && kps % kVBK == 0;
+  if (mode == BWDK) return d.Ci % 4 == 0;
+  return false;
+}
+
+template <int MODE>
+int launch_f32v(const Dev &d, const float *A, const float *B, float *C, int splits, int64_t kps,
+                cudaStream_t s) {
+  dim3 grid((unsigned)ceil_div(d.M, kVBM), (unsigned)ceil_div(d.N, kVBN), (unsigned)splits);
+  conv_f32v_kernel<MODE><<<grid, kVNT, 0, s>>>(d, A, B, C, kps);
+  OWL_CHECK_LAUNCH("conv_f32v_kernel");
+  return kOk;
+}
+
 Dev make_dev(const ConvGeom &g, int mode) {
   Dev d;
   d.B = g.B; d.IC = g.IC; d.IR = g.IR; d.ID = g.ID; d.Ci = g.Ci;
@@ -365,6 +641,10 @@ int launch_cfg(const Dev &d, const T *A, const T *B, T *C, int splits, int64_t k
 template <typename T, int MODE>
 int launch_any(const Dev &d, const T *A, const T *B, T *C, int splits, int64_t kps,
                cudaStream_t s) {
+  if constexpr (std::is_same_v<T, float>) {
+    if ((MODE == FWD || MODE == BWDK) && f32v_ok(MODE, d, A, B, C, kps))
+      return launch_f32v<MODE == BWDK ? BWDK : FWD>(d, A, B, C, splits, kps, s);
+  }
   if constexpr (sizeof(T) == 4) {
     if (d.N > 64) return launch_cfg<T, MODE, 128, 128, 8, 8, 8>(d, A, B, C, splits, kps, s);
     if (d.N > 32) return launch_cfg<T, MODE, 128, 64, 8, 8, 4>(d, A, B, C, splits, kps, s);
@@ -516,7 +796,7 @@ int splitk_t(const ConvGeom &g, const T *A, const T *B, T *C, cudaStream_t s) {
   int64_t want = ceil_div(4 * 152, tiles);
   int64_t max_by_k = ceil_div(d.K, 64);
   int splits = (int)std::max<int64_t>(1, std::min<int64_t>(want, std::min<int64_t>(max_by_k, 256)));
-  int64_t kps = ceil_div(ceil_div(d.K, splits), 8) * 8;
+  int64_t kps = ceil_div(ceil_div(d.K, splits), 16) * 16;
   splits = (int)ceil_div(d.K, kps);
   if (splits == 1) return launch_any<T, MODE>(d, A, B, C, 1, kps, s);
   void *ws = nullptr;
@@ -560,7 +840,7 @@ int bwdk_f32_into(const ConvGeom &g, const float *x, float *dw, const float *dy,
   int64_t max_by_ws = ws_elems / (d.M * d.N);
   int splits = (int)std::max<int64_t>(
       1, std::min<int64_t>(std::min<int64_t>(want, max_by_ws), std::min<int64_t>(max_by_k, 256)));
-  int64_t kps = ceil_div(ceil_div(d.K, splits), 8) * 8;
+  int64_t kps = ceil_div(ceil_div(d.K, splits), 16) * 16;
   splits = (int)ceil_div(d.K, kps);
   if (splits == 1) return launch_any<float, BWDK>(d, x, dy, dw, 1, kps, s);
   int rc = launch_any<float, BWDK>(d, x, dy, ws, splits, kps, s);
