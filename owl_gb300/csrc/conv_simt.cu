@@ -335,11 +335,10 @@ __global__ void splitk_reduce_kernel(const T *__restrict__ part, T *__restrict__
 
 // ---- float32 vector path ----------------------------------------------------
 // The same GEMM views in float32 with 16-byte operand gathers: 128 x 128
-// tiles, 16-deep k slabs, 256 threads of 8 x 8 outputs (four 4 x 4
-// quadrants, rows ty*4 and 64 + ty*4, columns tx*4 and 64 + tx*4, so every
-// shared-memory fragment is one 16-byte load without bank conflicts).
-// Shared-memory wavefronts, not the FMA pipe, bound this kind of kernel:
-// four per warp and k against 64 FMAs.
+// tiles (128 x 64 when N <= 64), 16-deep k slabs, 256 threads of 8 x 8
+// outputs (four 4 x 4 quadrants, rows ty*4 and 64 + ty*4, columns tx*4 and
+// 64 + tx*4, so every shared-memory fragment is one 16-byte load without
+// bank conflicts; 8 x 4 in the 64-wide tile).
 //   FWD : a slab is 16 consecutive input channels of one tap (Ci % 16 == 0);
 //         four threads read one pixel's 64 bytes, and each thread's two
 //         output pixels are decoded once per CTA.  A is stored k-major with
@@ -352,18 +351,21 @@ __global__ void splitk_reduce_kernel(const T *__restrict__ part, T *__restrict__
 // The k order of every output's sum is the same as the scalar kernel's
 // (ascending, one fused multiply-add per k), so a float32 forward gives the
 // same bits on either path.
-constexpr int kVBM = 128, kVBN = 128, kVBK = 16, kVNT = 256;
+constexpr int kVBM = 128, kVBK = 16, kVNT = 256;
 
 __device__ __forceinline__ float4 ldg4(const float *p) {
   return __ldg(reinterpret_cast<const float4 *>(p));
 }
 
-template <int MODE>
+// CN: 64-column blocks per tile (a thread holds 4 columns of each): 2 for
+// N > 64, 1 for 32 < N <= 64 (8 x 4 outputs per thread).
+template <int MODE, int CN>
 __global__ void __launch_bounds__(kVNT, 1)
     conv_f32v_kernel(Dev g, const float *__restrict__ A0, const float *__restrict__ B0,
                      float *__restrict__ C, int64_t k_per_split) {
+  constexpr int BN = 64 * CN;
   __shared__ __align__(16) float As[2][kVBK][kVBM];
-  __shared__ __align__(16) float Bs[2][kVBK][kVBN];
+  __shared__ __align__(16) float Bs[2][kVBK][BN];
   __shared__ int64_t s_base[2][kVBK];  // BWDK: slab pixels (batch image offset, -1 past the end)
   __shared__ int s_c[2][kVBK], s_r[2][kVBK], s_d[2][kVBK];
 
@@ -373,7 +375,7 @@ __global__ void __launch_bounds__(kVNT, 1)
   // each) per k
   const int lane = tid & 31, warp = tid >> 5;
   const int ty = (warp >> 2) * 8 + (lane >> 2), tx = (warp & 3) * 4 + (lane & 3);
-  const int64_t m0 = (int64_t)blockIdx.x * kVBM, n0 = (int64_t)blockIdx.y * kVBN;
+  const int64_t m0 = (int64_t)blockIdx.x * kVBM, n0 = (int64_t)blockIdx.y * BN;
   const int64_t k_begin = (int64_t)blockIdx.z * k_per_split;
   const int64_t k_end = min(g.K, k_begin + k_per_split);
   const int64_t img = g.IC * g.IR * g.ID;  // pixels per batch image of X
@@ -448,8 +450,11 @@ __global__ void __launch_bounds__(kVNT, 1)
     kc = (int)(tap / g.KR);
   }
 
-  float4 va[2], vb[2];
-  const int bcol = (tid & 31) * 4, bk = tid >> 5;
+  float4 va[2], vb[CN];
+  // B: float4 column bcol of k rows bk (+ 8); BWDK's A: pixels ak (+ 8)
+  const int bcol = CN == 2 ? (tid & 31) * 4 : (tid & 15) * 4;
+  const int bk = CN == 2 ? tid >> 5 : tid >> 4;
+  const int ak = tid >> 5;
   const bool bval = n0 + bcol < g.N;
 
   // global -> registers for slab k0 (FWD: at tap kc/kr/kd, channels ci0..)
@@ -466,7 +471,7 @@ __global__ void __launch_bounds__(kVNT, 1)
     } else {
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
-        const int kl = bk + 8 * h;
+        const int kl = ak + 8 * h;
         const int64_t base = s_base[buf][kl];
         va[h] = make_float4(0.f, 0.f, 0.f, 0.f);
         if (mval && base >= 0) {
@@ -478,7 +483,7 @@ __global__ void __launch_bounds__(kVNT, 1)
       }
     }
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
+    for (int h = 0; h < CN; ++h) {
       const int64_t kq = k0 + bk + 8 * h;
       vb[h] = (bval && kq < k_end) ? ldg4(B0 + kq * g.N + n0 + bcol)
                                    : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -497,10 +502,10 @@ __global__ void __launch_bounds__(kVNT, 1)
     } else {
 #pragma unroll
       for (int h = 0; h < 2; ++h)
-        *reinterpret_cast<float4 *>(&As[buf][bk + 8 * h][mq]) = va[h];
+        *reinterpret_cast<float4 *>(&As[buf][ak + 8 * h][mq]) = va[h];
     }
 #pragma unroll
-    for (int h = 0; h < 2; ++h) *reinterpret_cast<float4 *>(&Bs[buf][bk + 8 * h][bcol]) = vb[h];
+    for (int h = 0; h < CN; ++h) *reinterpret_cast<float4 *>(&Bs[buf][bk + 8 * h][bcol]) = vb[h];
   };
   auto next_tap = [&]() {
     ci0 += kVBK;
@@ -516,11 +521,11 @@ __global__ void __launch_bounds__(kVNT, 1)
     }
   };
 
-  float acc[8][8];
+  float acc[8][4 * CN];
 #pragma unroll
   for (int i = 0; i < 8; ++i)
 #pragma unroll
-    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+    for (int j = 0; j < 4 * CN; ++j) acc[i][j] = 0.f;
 
   if (k_begin < k_end) {
     if (MODE == BWDK) {
@@ -544,14 +549,20 @@ __global__ void __launch_bounds__(kVNT, 1)
         const int sw = MODE == FWD ? ((k >> 2) << 3) : 0;
         const float4 a0 = *reinterpret_cast<const float4 *>(&As[buf][k][(ty * 4) ^ sw]);
         const float4 a1 = *reinterpret_cast<const float4 *>(&As[buf][k][(64 + ty * 4) ^ sw]);
-        const float4 b0 = *reinterpret_cast<const float4 *>(&Bs[buf][k][tx * 4]);
-        const float4 b1 = *reinterpret_cast<const float4 *>(&Bs[buf][k][64 + tx * 4]);
         const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-        const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+        float b[4 * CN];
+#pragma unroll
+        for (int q = 0; q < CN; ++q) {
+          const float4 v = *reinterpret_cast<const float4 *>(&Bs[buf][k][64 * q + tx * 4]);
+          b[4 * q] = v.x;
+          b[4 * q + 1] = v.y;
+          b[4 * q + 2] = v.z;
+          b[4 * q + 3] = v.w;
+        }
 #pragma unroll
         for (int i = 0; i < 8; ++i)
 #pragma unroll
-          for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+          for (int j = 0; j < 4 * CN; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
       }
       if (more) {
         store(buf ^ 1);
@@ -578,7 +589,7 @@ __global__ void __launch_bounds__(kVNT, 1)
       row = g.yoff + b * g.ysb + oc * g.ysc + orr * g.ysr + od * g.ysd;
     }
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
+    for (int q = 0; q < CN; ++q) {
       const int64_t n = n0 + q * 64 + tx * 4;
       if (n < g.N)
         *reinterpret_cast<float4 *>(Cz + row * g.N + n) =
@@ -588,12 +599,13 @@ __global__ void __launch_bounds__(kVNT, 1)
 }
 
 // Whether the float32 vector path takes a launch: 16-byte aligned operands,
-// N a multiple of 4 above 64 (the 128-wide tile), FWD slabs inside one tap
-// (Ci % 16, whole slabs per split), BWDK rows in quads of one tap (Ci % 4).
+// N a multiple of 4 above 32 (64- or 128-wide tiles), FWD slabs inside one
+// tap (Ci % 16, whole slabs per split), BWDK rows in quads of one tap
+// (Ci % 4).
 bool f32v_ok(int mode, const Dev &d, const void *A, const void *B, const void *C,
              int64_t kps) {
   auto al = [](const void *p) { return ((uintptr_t)p & 15) == 0; };
-  if (!al(A) || !al(B) || !al(C) || d.N % 4 != 0 || d.N <= 64) return false;
+  if (!al(A) || !al(B) || !al(C) || d.N % 4 != 0 || d.N <= 32) return false;
   if (d.IC >= (1 << 30) || d.IR >= (1 << 30) || d.ID >= (1 << 30)) return false;
   if (mode == FWD) return d.Ci % kVBK == 0 && kps % kVBK == 0;
   if (mode == BWDK) return d.Ci % 4 == 0;
@@ -603,8 +615,12 @@ bool f32v_ok(int mode, const Dev &d, const void *A, const void *B, const void *C
 template <int MODE>
 int launch_f32v(const Dev &d, const float *A, const float *B, float *C, int splits, int64_t kps,
                 cudaStream_t s) {
-  dim3 grid((unsigned)ceil_div(d.M, kVBM), (unsigned)ceil_div(d.N, kVBN), (unsigned)splits);
-  conv_f32v_kernel<MODE><<<grid, kVNT, 0, s>>>(d, A, B, C, kps);
+  const int bn = d.N > 64 ? 128 : 64;
+  dim3 grid((unsigned)ceil_div(d.M, kVBM), (unsigned)ceil_div(d.N, bn), (unsigned)splits);
+  if (bn == 128)
+    conv_f32v_kernel<MODE, 2><<<grid, kVNT, 0, s>>>(d, A, B, C, kps);
+  else
+    conv_f32v_kernel<MODE, 1><<<grid, kVNT, 0, s>>>(d, A, B, C, kps);
   OWL_CHECK_LAUNCH("conv_f32v_kernel");
   return kOk;
 }
