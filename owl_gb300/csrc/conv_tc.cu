@@ -3,12 +3,13 @@
 // stride 1, any dilation, 2-D and 3-D.
 //
 // Design: persistent, warp-specialised "halo" implicit GEMM.
-//   * An output tile is 16*MH positions along one spatial axis (u) by 8 along
-//     another (v): N = 128*MH pixels, each group of 8 v-positions one 8-row
-//     core-matrix band of the MMA's N dimension.  The kernel tile (128 output
-//     channels) is the M = 128 operand.  tcgen05.mma costs the same number of
-//     cycles for N = 64..256 at M = 128, so the pixel dimension goes on N and
-//     uses the full N = 256 whenever the output is at least 17 rows tall.
+//   * An output tile is TU positions along one spatial axis (u) by 8 along
+//     another (v): N = 8*TU pixels (TU even, up to 32), each group of 8
+//     v-positions one 8-row core-matrix band of the MMA's N dimension.  The
+//     kernel tile (128 output channels) is the M = 128 operand.  tcgen05.mma
+//     costs the same number of cycles for any N at M = 128, so the pixel
+//     dimension goes on N, the tile is as tall as the fewest tiles along u
+//     allow, and no taller (less halo).
 //   * Producer warps load the input halo the tile needs for one block of
 //     channels -- once -- from the float32 activation, convert it (bf16 RN,
 //     tf32 RNA, or bf16 hi + lo) and store it in shared memory as
@@ -19,7 +20,7 @@
 //   * The kernel tensor is re-laid out once per call (prep_weights) into the
 //     exact shared-memory image of each (channel block, tap) B tile, which one
 //     thread streams with cp.async.bulk (TMA engine) into a ring of stages.
-//   * One thread issues tcgen05.mma (M=128 channels, N=128*MH pixels, K=16/8
+//   * One thread issues tcgen05.mma (M=128 channels, N=8*TU pixels, K=16/8
 //     per instruction) into a double-buffered TMEM accumulator; four epilogue
 //     warps drain the other buffer (tcgen05.ld, one TMEM lane per output
 //     channel) and write float32 results to HBM, 32 consecutive channels of a
@@ -95,7 +96,11 @@ struct TcParams {
   int B, IW, IU, IV;  // input extents (output extents, taps and pads per segment)
   long long xsb, xsw, xsu, xsv, ysb, ysw, ysu, ysv;  // pixel strides
   int Cin, Cout;
-  int BN, CB, NCH, CPB, NCB, MH;
+  int BN, CB, NCH, CPB, NCB;
+  // Output tile: TU positions along u (even, <= 32) by 8 along v, TN = 8*TU
+  // pixels = the MMA's N; TNA = TN rounded up to 32 TMEM columns (the
+  // column stride of the accumulators of a tile's co tiles and buffers).
+  int TU, TN, TNA;
   int T;  // plan: taps of the longest segment
   int sw, su, sv;          // strides along w, u, v
   int HW, HU, HV, HVR, HP, PS;  // halo rows along w, u; pixels per u-row (= sv * HVR)
@@ -167,7 +172,7 @@ __device__ __forceinline__ Tile decode_tile(const TcParams &p, long long t, int 
   t /= p.n_groups;
   r.v0 = (int)(t % sg.v_tiles) * 8;
   t /= sg.v_tiles;
-  r.u0 = (int)(t % sg.u_tiles) * 16 * p.MH;
+  r.u0 = (int)(t % sg.u_tiles) * p.TU;
   t /= sg.u_tiles;
   r.ow = (int)(t % sg.OW);
   r.b = (int)(t / sg.OW);
@@ -258,10 +263,13 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
     // ===================== halo producers =====================
     // Each warp stages whole halo rows: a row is one (w, u, residue) line of
     // HVR pixels whose global addresses advance by a fixed step, so the row
-    // bounds are checked once and each lane only adds offsets.  Two rows per
-    // pass give every lane up to 2*kSlots chunk loads in flight.
+    // bounds are checked once and each lane only adds offsets.  A pass takes
+    // one or two rows and deals their chunk slots flat over the lanes, up to
+    // six loads in flight per lane.
     const int nrows = p.HW * p.HU * p.sv;
     const int S = p.HVR * p.NCH;  // chunk slots per row
+    // rows per producer pass: two when both rows' slots fit 6 per lane
+    const int rpp = 2 * S <= 32 * 6 ? 2 : 1;
     const int nsh = (p.NCH & (p.NCH - 1)) == 0 ? __ffs(p.NCH) - 1 : -1;
     const long long vstep = (long long)p.sv * p.xsv * p.Cin;  // floats between row pixels
     long long k = 0;  // halo stage counter
@@ -276,75 +284,81 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
         if (!wait_bar(smem_u32(&halo_empty[hs]), ph ^ 1, abort_flag, p.status, p.spin_limit)) goto done;
         uint8_t *dst = halo + (size_t)hs * PARTS * p.halo_bytes;
         const int cbase = cb * p.CPB;
-        for (int r0 = pidx * 2; r0 < nrows; r0 += 2 * kProducerWarps) {
-          constexpr int kSlots = 3;  // slots per lane per row per pass
-          float v[2][kSlots][EPC];
-          int off[2][kSlots];
-#pragma unroll
-          for (int rr = 0; rr < 2; ++rr) {
+        for (int r0 = pidx * rpp; r0 < nrows; r0 += rpp * kProducerWarps) {
+          // the pass's rpp rows: bounds checked and base addresses formed once
+          // (two named rows, not an array: a slot picks its row by a select)
+          const float *rowp0, *rowp1;
+          bool ok0, ok1;
+          int ivs0, ivs1;
+          auto row_setup = [&](int rr, const float *&rp, bool &ok, int &ivs) {
             const int r = r0 + rr;
             // row -> (w row, u row, residue class)
             const int hr = r % p.sv, t3 = r / p.sv;
             const int hu = t3 % p.HU, hw = t3 / p.HU;
             const int iw = tl.ow * p.sw - pw + hw, iu = tl.u0 * p.su - pu + hu;
-            const int ivs = tl.v0 * p.sv - pv + hr;  // global v of the row's pixel 0
-            const bool row_ok = r < nrows && iw >= 0 && iw < p.IW && iu >= 0 && iu < p.IU;
-            const float *rowp =
-                p.x + ((long long)tl.b * p.xsb + (long long)iw * p.xsw + (long long)iu * p.xsu +
-                       (long long)ivs * p.xsv) * p.Cin + cbase;
+            ivs = tl.v0 * p.sv - pv + hr;  // global v of the row's pixel 0
+            ok = rr < rpp && r < nrows && iw >= 0 && iw < p.IW && iu >= 0 && iu < p.IU;
+            rp = p.x + ((long long)tl.b * p.xsb + (long long)iw * p.xsw + (long long)iu * p.xsu +
+                        (long long)ivs * p.xsv) * p.Cin + cbase;
+          };
+          row_setup(0, rowp0, ok0, ivs0);
+          row_setup(1, rowp1, ok1, ivs1);
+          // the pass's rpp*S chunk slots dealt over the lanes, up to kSlots each
+          constexpr int kSlots = 6;
+          float v[kSlots][EPC];
+          int off[kSlots];
 #pragma unroll
-            for (int q = 0; q < kSlots; ++q) {
-              const int sl = lane + 32 * q;
+          for (int q = 0; q < kSlots; ++q) {
+            const int sl = lane + 32 * q;
 #pragma unroll
-              for (int e = 0; e < EPC; ++e) v[rr][q][e] = 0.f;
-              off[rr][q] = -1;
-              if (r < nrows && sl < S) {
-                const int hc = nsh >= 0 ? (sl >> nsh) : sl / p.NCH;
-                const int j = sl - hc * p.NCH;
-                off[rr][q] = j * p.PS * 16 + (r * p.HVR + hc) * 16;
-                const int iv = ivs + hc * p.sv;
-                const int c = cbase + j * EPC;
-                if (row_ok && iv >= 0 && iv < p.IV && c < p.Cin) {
-                  const float *src = rowp + hc * vstep + j * EPC;
-                  if (p.vec_in && c + EPC <= p.Cin) {
-                    stage::load_vec<EPC>(src, p.vec_in, v[rr][q]);
-                  } else {
+            for (int e = 0; e < EPC; ++e) v[q][e] = 0.f;
+            off[q] = -1;
+            const int rr = sl >= S ? 1 : 0;
+            const int s2 = sl - rr * S;
+            const int r = r0 + rr;
+            if (sl < rpp * S && s2 < S && r < nrows) {
+              const int hc = nsh >= 0 ? (s2 >> nsh) : s2 / p.NCH;
+              const int j = s2 - hc * p.NCH;
+              off[q] = j * p.PS * 16 + (r * p.HVR + hc) * 16;
+              const int iv = (rr ? ivs1 : ivs0) + hc * p.sv;
+              const int c = cbase + j * EPC;
+              if ((rr ? ok1 : ok0) && iv >= 0 && iv < p.IV && c < p.Cin) {
+                const float *src = (rr ? rowp1 : rowp0) + hc * vstep + j * EPC;
+                if (p.vec_in && c + EPC <= p.Cin) {
+                  stage::load_vec<EPC>(src, p.vec_in, v[q]);
+                } else {
 #pragma unroll
-                    for (int e = 0; e < EPC; ++e)
-                      if (c + e < p.Cin) v[rr][q][e] = __ldg(src + e);
-                  }
+                  for (int e = 0; e < EPC; ++e)
+                    if (c + e < p.Cin) v[q][e] = __ldg(src + e);
                 }
               }
             }
           }
 #pragma unroll
-          for (int rr = 0; rr < 2; ++rr)
-#pragma unroll
-            for (int q = 0; q < kSlots; ++q) {
-              if (off[rr][q] < 0) continue;
-              uint4 hi;
-              if (KIND == K_TF32) {
-                hi = make_uint4(to_tf32(v[rr][q][0]), to_tf32(v[rr][q][1]),
-                                to_tf32(v[rr][q][2]), to_tf32(v[rr][q][3]));
-              } else {
-                hi = make_uint4(pack_bf16(v[rr][q][0], v[rr][q][1]),
-                                pack_bf16(v[rr][q][2], v[rr][q][3]),
-                                pack_bf16(v[rr][q][4], v[rr][q][5]),
-                                pack_bf16(v[rr][q][6], v[rr][q][7]));
-              }
-              *reinterpret_cast<uint4 *>(dst + off[rr][q]) = hi;
-              if (KIND == K_BF16X3) {
-                float rs[8];
-#pragma unroll
-                for (int e = 0; e < 8; ++e) rs[e] = v[rr][q][e] - bf16_round(v[rr][q][e]);
-                uint4 lo = make_uint4(pack_bf16(rs[0], rs[1]), pack_bf16(rs[2], rs[3]),
-                                      pack_bf16(rs[4], rs[5]), pack_bf16(rs[6], rs[7]));
-                *reinterpret_cast<uint4 *>(dst + p.halo_bytes + off[rr][q]) = lo;
-              }
+          for (int q = 0; q < kSlots; ++q) {
+            if (off[q] < 0) continue;
+            uint4 hi;
+            if (KIND == K_TF32) {
+              hi = make_uint4(to_tf32(v[q][0]), to_tf32(v[q][1]), to_tf32(v[q][2]),
+                              to_tf32(v[q][3]));
+            } else {
+              hi = make_uint4(pack_bf16(v[q][0], v[q][1]), pack_bf16(v[q][2], v[q][3]),
+                              pack_bf16(v[q][4], v[q][5]), pack_bf16(v[q][6], v[q][7]));
             }
-          // rows wider than 32*kSlots chunk slots: stage the remainder one
-          // slot at a time (large dilations / long kernel rows only)
-          for (int rr = 0; rr < 2; ++rr) {
+            *reinterpret_cast<uint4 *>(dst + off[q]) = hi;
+            if (KIND == K_BF16X3) {
+              float rs[8];
+#pragma unroll
+              for (int e = 0; e < 8; ++e) rs[e] = v[q][e] - bf16_round(v[q][e]);
+              uint4 lo = make_uint4(pack_bf16(rs[0], rs[1]), pack_bf16(rs[2], rs[3]),
+                                    pack_bf16(rs[4], rs[5]), pack_bf16(rs[6], rs[7]));
+              *reinterpret_cast<uint4 *>(dst + p.halo_bytes + off[q]) = lo;
+            }
+          }
+          // rows wider than 32*kSlots chunk slots (one row per pass then):
+          // stage the remainder one slot at a time (large dilations / long
+          // kernel rows only)
+          for (int rr = 0; rr < rpp; ++rr) {
             const int r = r0 + rr;
             if (r >= nrows) break;
             for (int sl = lane + 32 * kSlots; sl < S; sl += 32) {
@@ -445,7 +459,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
 #pragma unroll 4
                 for (int s = 0; s < ksteps; ++s) {
                   const uint64_t wd = wd0 + (uint64_t)(s * wstep16);  // A: 128 output channels
-                  const uint64_t xd = xd0 + (uint64_t)(s * xstep16);  // B: 16*MH pixel groups
+                  const uint64_t xd = xd0 + (uint64_t)(s * xstep16);  // B: TU pixel groups
                   if (KIND == K_TF32) {
                     mma_tf32(d0, wd, xd, p.idesc, acc);
                   } else {
@@ -460,7 +474,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
               } else {
                 // two co tiles share the pixel operand; alternating between
                 // their accumulators keeps N = 128 MMAs at full rate
-                const uint32_t d1 = d0 + (uint32_t)(p.MH * 128);
+                const uint32_t d1 = d0 + (uint32_t)p.TNA;
                 const uint64_t wd1 = wd0 + (uint64_t)(p.TPS * tile16);
 #pragma unroll 2
                 for (int s = 0; s < ksteps; ++s) {
@@ -572,7 +586,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
         const int co = (tl.nt * p.NCT + ct) * 128 + q * 32 + lane;
         const bool co_ok = co < p.Cout;
         const uint32_t tcol = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)abuf * p.acc_cols +
-                              (uint32_t)(ct * p.MH * 128);
+                              (uint32_t)(ct * p.TNA);
         // Few instructions per store: this warp (quadrant 0) shares a
         // scheduler with the MMA issuer.  Element (u, v) of the tile is at
         // ytile + (u - u0) * du + (v - v0) * dv.  Streaming stores: the
@@ -591,18 +605,22 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
                        ((long long)tl.b * p.ysb + (long long)tl.ow * p.ysw +
                         (long long)tl.u0 * p.ysu + (long long)tl.v0 * p.ysv) * p.ych + cy;
         const long long du = p.ysu * (long long)p.ych, dv = p.ysv * (long long)p.ych;
-        const int urows = min(p.MH * 16, sg.OU - tl.u0), vcols = min(8, sg.OV - tl.v0);
+        const int urows = min(p.TU, sg.OU - tl.u0), vcols = min(8, sg.OV - tl.v0);
         // four 16-column loads per wait; BF16X3 loads two of the hi*hi sums
         // and the two matching cross-term sums, and adds them
         constexpr int LD = SEP ? 2 : 4;
-        for (int c0 = 0; c0 < p.MH * 128; c0 += 16 * LD) {
+        // (TN is a multiple of 16 columns: a load group may end early, the
+        // same for every lane, so the warp-collective loads stay uniform)
+        for (int c0 = 0; c0 < p.TN; c0 += 16 * LD) {
           uint32_t r[LD][16];
 #pragma unroll
-          for (int k = 0; k < LD; ++k) tmem_ld16(tcol + (uint32_t)(c0 + 16 * k), r[k]);
+          for (int k = 0; k < LD; ++k)
+            if (c0 + 16 * k < p.TN) tmem_ld16(tcol + (uint32_t)(c0 + 16 * k), r[k]);
           if (SEP) {
             uint32_t r2[LD][16];
 #pragma unroll
-            for (int k = 0; k < LD; ++k) tmem_ld16(tcol + p.small_off + (uint32_t)(c0 + 16 * k), r2[k]);
+            for (int k = 0; k < LD; ++k)
+              if (c0 + 16 * k < p.TN) tmem_ld16(tcol + p.small_off + (uint32_t)(c0 + 16 * k), r2[k]);
             tmem_ld_wait();
 #pragma unroll
             for (int k = 0; k < LD; ++k)
@@ -629,7 +647,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_const
 #pragma unroll
               for (int h = 0; h < 2; ++h) {
                 const int ur = (c0 + 16 * k + 8 * h) >> 3;  // u row within the tile
-                if (ur < urows) {
+                if (ur < urows && c0 + 16 * k < p.TN) {
                   float *row = ytile + ur * du;
                   if (vcols == 8) {
 #pragma unroll
@@ -822,9 +840,14 @@ int *status_ptr() {
 }
 
 // Choose tile and pipeline sizes; false if no configuration fits.
-// Priorities: two 128-pixel halves (N = 256) first; then the widest channel
-// block (fewer, fuller halo stages for the producers); then the most taps per
-// weight slot (fewer barrier polls between MMAs).
+// Priorities: the fewest halo stagings, tiles along u times co-tile groups
+// (an MMA costs the same whatever its N, so a tile's MMA count does not
+// depend on its height, and a tile of up to 128 pixels stages its halo once
+// for two co tiles); then the widest
+// channel block (fewer, fuller halo stages for the producers: a whole
+// 128-channel pixel per stage when two stages fit); then the most taps per
+// weight slot (fewer barrier polls between MMAs); then the lowest tile (the
+// least halo).  Tile heights are even (N = 8*TU a multiple of 16) up to 32.
 // `v` holds the largest halo extents of the launch's segments; t_slot is the
 // most taps of one segment (weight slots), t_table the taps of all segments
 // (the shared-memory tap table).
@@ -834,22 +857,27 @@ bool plan(TcParams &p, const View &v, int kind, int t_slot, int t_table) {
   p.BN = 128;  // output channels per tile = the MMA's M
   p.n_tiles = (v.Cout + p.BN - 1) / p.BN;
   p.T = t_slot;
-  const int cb0 = std::min(128, (int)((v.Cin * EB + 31) / 32 * 32));
+  const int cb0 = std::min(256, (int)((v.Cin * EB + 31) / 32 * 32));
   bool found = false;
   TcParams best = p;
-  long long best_score = -1;
+  long long best_score = 0;
   // two halo stages (staging overlaps the MMAs); one only when two do not
   // fit shared memory (wide strided halos in split-BF16)
   for (int nh = 2; nh >= 1 && !found; --nh)
-  for (int mh = (v.OU > 16 ? 2 : 1); mh >= 1 && !found; --mh) {
+  for (int tu = 32; tu >= 2; tu -= 2) {
+    const long long u_tiles = (v.OU + tu - 1) / tu;
     for (int cb = cb0; cb >= 32; cb -= 32) {
-      if (cb != cb0 && cb % 64 != 0 && cb != 32) continue;  // try cb0, then 64, 32
+      // cb0 (all channels, up to 256 bytes), then 128, 64, 32: blocks that
+      // divide the channels evenly (a ragged last block costs full MMAs)
+      if (cb != cb0 && cb != 128 && cb != 64 && cb != 32) continue;
       TcParams q = p;
       q.NH = nh;
-      q.MH = mh;
-      // 128-pixel tiles take two co tiles when there are two: the halo is
-      // staged once for both and their MMAs alternate accumulators
-      q.NCT = (mh == 1 && p.n_tiles >= 2) ? 2 : 1;
+      q.TU = tu;
+      q.TN = 8 * tu;
+      q.TNA = (q.TN + 31) / 32 * 32;
+      // tiles of up to 128 pixels take two co tiles when there are two: the
+      // halo is staged once for both and their MMAs alternate accumulators
+      q.NCT = (q.TN <= 128 && p.n_tiles >= 2) ? 2 : 1;
       q.n_groups = (p.n_tiles + q.NCT - 1) / q.NCT;
       q.CB = cb;
       q.CPB = q.CB / EB;
@@ -857,7 +885,7 @@ bool plan(TcParams &p, const View &v, int kind, int t_slot, int t_table) {
       q.NCB = (v.Cin + q.CPB - 1) / q.CPB;
       q.tile_bytes = (unsigned)(q.BN * q.CB);
       q.HW = (v.KW - 1) * v.dw + 1;
-      q.HU = (16 * mh - 1) * v.su + (v.KU - 1) * v.du + 1;
+      q.HU = (tu - 1) * v.su + (v.KU - 1) * v.du + 1;
       q.HVR = 8 + ((v.KV - 1) * v.dv) / v.sv;
       q.HV = v.sv * q.HVR;
       q.HP = q.HW * q.HU * q.HV;
@@ -879,19 +907,22 @@ bool plan(TcParams &p, const View &v, int kind, int t_slot, int t_table) {
       if (q.NB < 2) continue;
       // accumulator sets: double-buffered when they fit TMEM (the epilogue
       // of one tile overlaps the next tile's MMAs), else one set
-      q.small_off = (unsigned)(q.NCT * q.MH * 128);
+      q.small_off = (unsigned)(q.NCT * q.TNA);
       q.acc_cols = q.small_off * (unsigned)parts;
       q.nbuf = q.acc_cols * 2 <= 512 ? 2 : 1;
       if (q.acc_cols > 512) continue;
       q.tmem_cols = 32;
       while (q.tmem_cols < q.acc_cols * (unsigned)q.nbuf) q.tmem_cols <<= 1;
-      const long long score = (long long)q.CB * 1000 + (long long)q.TPS * (q.NCH / 2);
-      if (score > best_score) {
+      // halo stagings per output: tiles along u times co-tile groups
+      const long long stagings = u_tiles * q.n_groups;
+      const long long score = -stagings * 1000000000000LL + (long long)q.CB * 1000000LL +
+                              (long long)q.TPS * (q.NCH / 2) * 1000LL - tu;
+      if (!found || score > best_score) {
         best_score = score;
         best = q;
+        found = true;
       }
     }
-    if (best_score >= 0) found = true;
   }
   if (!found) return false;
   p = best;
@@ -1065,7 +1096,7 @@ int run_segs(int prec, int nseg_in, const SegSpec *sp, bool bwd_input, int Ci, i
     g.yoff = fuse_n ? 0 : sp[idx[k]].yoff;
     g.woff = (long long)woff;
     g.OW = v.OW; g.OU = v.OU; g.OV = v.OV;
-    g.u_tiles = (v.OU + 16 * p.MH - 1) / (16 * p.MH);
+    g.u_tiles = (v.OU + p.TU - 1) / p.TU;
     g.v_tiles = (v.OV + 7) / 8;
     g.KW = v.KW; g.KU = v.KU; g.KV = v.KV;
     g.dw = v.dw; g.du = v.du; g.dv = v.dv;
@@ -1078,7 +1109,7 @@ int run_segs(int prec, int nseg_in, const SegSpec *sp, bool bwd_input, int Ci, i
     woff += (size_t)p.n_tiles * p.NCB * g.T * p.tile_bytes;
   }
   p.total_tiles = tiles;
-  p.idesc = instr_desc(kind == K_TF32 ? 2u : 1u, (uint32_t)(128 * p.MH));
+  p.idesc = instr_desc(kind == K_TF32 ? 2u : 1u, (uint32_t)p.TN);
   // 1: 16-byte vector loads; 2: 32-byte aligned chunks (one load per chunk)
   p.vec_in = ((uintptr_t)x % 32 == 0 && pv.Cin % 8 == 0)
                  ? 2
