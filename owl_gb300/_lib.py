@@ -94,9 +94,15 @@ def last_error() -> str:
     return lib().owlgpu_last_error().decode()
 
 
+_entry: dict = {}  # name -> bound entry point (lib() and getattr once per name)
+
+
 def call(name: str, *args) -> None:
     """Call an `int`-returning entry point and raise on a negative status."""
-    rc = getattr(lib(), name)(*args)
+    f = _entry.get(name)
+    if f is None:
+        f = _entry[name] = getattr(lib(), name)
+    rc = f(*args)
     if rc != 0:
         raise OwlGpuError(name, rc, last_error())
 

@@ -34,9 +34,12 @@ class InvalidArgument(ValueError):
     """Mirror of Owl_exception.INVALID_ARGUMENT (raised before any stub call)."""
 
 
-def _verify(cond: bool, msg: str) -> None:
+def _verify(cond: bool, msg) -> None:
+    """Raise InvalidArgument(msg) unless cond; msg may be a function that
+    builds the message (formatted only on failure: these checks run on
+    every call)."""
     if not cond:
-        raise InvalidArgument(msg)
+        raise InvalidArgument(msg() if callable(msg) else msg)
 
 
 # ---- IS: shape and padding math (owl_utils_infer_shape.ml) ----------------
@@ -96,25 +99,29 @@ def calc_conv2d_padding(input_cols, input_rows, kernel_cols, kernel_rows, output
 
 
 def _pad_typ(padding) -> int:
-    _verify(padding in (SAME, VALID), f"padding must be SAME or VALID, got {padding!r}")
+    _verify(padding in (SAME, VALID), lambda: f"padding must be SAME or VALID, got {padding!r}")
     return 0 if padding == SAME else 1
 
 
 # ---- stub name mapping -------------------------------------------------------
 
+_KIND_OF: dict = {}  # element type -> kind name, filled as types are met
+
+
 def _kind(a) -> str:
     """Owl's kind name of an array's element type: float32 / float64 (S, D)
     and complex32 / complex64 (C, Z), the latter numpy's / torch's complex64
     and complex128."""
-    dt = str(getattr(a, "dtype", ""))
-    if "float32" in dt:
-        return "float32"
-    if "float64" in dt:
-        return "float64"
-    if "complex64" in dt:
-        return "complex32"
-    if "complex128" in dt:
-        return "complex64"
+    dtype = getattr(a, "dtype", None)
+    k = _KIND_OF.get(dtype)
+    if k is not None:
+        return k
+    dt = str(dtype if dtype is not None else "")
+    for name, kind in (("float32", "float32"), ("float64", "float64"),
+                       ("complex64", "complex32"), ("complex128", "complex64")):
+        if name in dt:
+            _KIND_OF[dtype] = kind
+            return kind
     raise InvalidArgument(f"unsupported element kind {dt} (float32, float64, complex64 and "
                           "complex128 only)")
 
@@ -164,9 +171,8 @@ class GpuBackend(Backend):
         return np.empty(tuple(shape), dtype=dtype or like.dtype)
 
     def stub(self, kind, op, *args):
-        arrays = [a for a in args if not isinstance(a, (int, np.integer))]
-        dev = any(self._is_torch(a) for a in arrays)
         conv = []
+        dev = host = False
         for a in args:
             if isinstance(a, (int, np.integer)):
                 conv.append(int(a))
@@ -174,10 +180,14 @@ class GpuBackend(Backend):
                 if not a.is_cuda or not a.is_contiguous():
                     raise InvalidArgument("device arrays must be contiguous CUDA tensors")
                 conv.append(a.data_ptr())
+                dev = True
             else:
                 if not (isinstance(a, np.ndarray) and a.flags.c_contiguous):
                     raise InvalidArgument("host arrays must be C-contiguous numpy arrays")
                 conv.append(a.ctypes.data)
+                host = True
+        if dev and host:
+            raise InvalidArgument("a call takes either CUDA tensors or numpy arrays, not both")
         if dev:
             import torch
 
@@ -188,7 +198,8 @@ class GpuBackend(Backend):
             try:
                 self._lib.call(f"owl_{kind}_ndarray_{op}", *conv)
             finally:
-                self._lib.set_precision(prev)
+                if prev != self.precision:
+                    self._lib.set_precision(prev)
 
 
 # ---- the NN function set (G) -------------------------------------------------
@@ -213,7 +224,7 @@ class NN:
         if out is None:
             return self.b.empty(like, shape, dtype)
         _verify(tuple(self._shape(out)) == tuple(shape),
-                f"out: shape {list(self._shape(out))} should be {list(shape)}")
+                lambda: f"out: shape {list(self._shape(out))} should be {list(shape)}")
         return out
 
     def _ob(self, out):
@@ -232,14 +243,14 @@ class NN:
     def conv2d(self, input, kernel, stride: Sequence[int], padding=SAME, out=None):
         """G:2324 conv2d."""
         _verify(self._dims(input) == 4 and self._dims(kernel) == 4 and len(stride) == 2,
-                f"conv2d: input dimension = {self._dims(input)} (should be 4); kernel dimension "
-                f"= {self._dims(kernel)} (should be 4); stride dimension = {len(stride)} "
-                f"(should be 2).")
+                lambda: f"conv2d: input dimension = {self._dims(input)} (should be 4); kernel "
+                f"dimension = {self._dims(kernel)} (should be 4); stride dimension = "
+                f"{len(stride)} (should be 2).")
         B, IC, IR, Ci = self._shape(input)
         KC, KR, kci, Co = self._shape(kernel)
-        _verify(Ci == kci, f"conv2d: input shape is {list(self._shape(input))}, kernel shape is "
-                f"{list(self._shape(kernel))}, the 4th dimension of input shape should be equal "
-                f"to the 3rd dimension of kernel shape.")
+        _verify(Ci == kci, lambda: f"conv2d: input shape is {list(self._shape(input))}, kernel "
+                f"shape is {list(self._shape(kernel))}, the 4th dimension of input shape should "
+                f"be equal to the 3rd dimension of kernel shape.")
         cs, rs = stride
         OC, OR = calc_conv2d_output_shape(padding, IC, IR, KC, KR, rs, cs)
         output = self._out(out, input, (B, OC, OR, Co))
@@ -249,14 +260,15 @@ class NN:
 
     def _conv2d_bwd_check(self, name, input, kernel, stride, output_):
         _verify(self._dims(input) == 4 and self._dims(kernel) == 4 and
-                self._dims(output_) == 4 and len(stride) == 2, f"{name}: bad dimensions")
+                self._dims(output_) == 4 and len(stride) == 2, lambda: f"{name}: bad dimensions")
         B, IC, IR, Ci = self._shape(input)
         KC, KR, kci, Co = self._shape(kernel)
-        _verify(Ci == kci, f"{name}: the 4th dimension of input shape should be equal to the "
-                f"3rd dimension of kernel shape")
+        _verify(Ci == kci, lambda: f"{name}: the 4th dimension of input shape should be equal to "
+                f"the 3rd dimension of kernel shape")
         ob, OC, OR, oco = self._shape(output_)
-        _verify(B == ob and Co == oco, f"{name}: output' shape {list(self._shape(output_))} "
-                f"does not match input/kernel")
+        _verify(B == ob and Co == oco,
+                lambda: f"{name}: output' shape {list(self._shape(output_))} does not match "
+                f"input/kernel")
         return B, IC, IR, Ci, KC, KR, Co, OC, OR
 
     def conv2d_backward_input(self, input, kernel, stride, output_, out=None):
@@ -332,12 +344,12 @@ class NN:
 
     def _conv3d_bwd_check(self, name, input, kernel, stride, output_):
         _verify(self._dims(input) == 5 and self._dims(kernel) == 5 and
-                self._dims(output_) == 5 and len(stride) == 3, f"{name}: bad dimensions")
+                self._dims(output_) == 5 and len(stride) == 3, lambda: f"{name}: bad dimensions")
         B, IC, IR, ID, Ci = self._shape(input)
         KC, KR, KD, kci, Co = self._shape(kernel)
-        _verify(Ci == kci, f"{name}: channel mismatch")
+        _verify(Ci == kci, lambda: f"{name}: channel mismatch")
         ob, OC, OR, OD, oco = self._shape(output_)
-        _verify(B == ob and Co == oco, f"{name}: output' shape mismatch")
+        _verify(B == ob and Co == oco, lambda: f"{name}: output' shape mismatch")
         return B, IC, IR, ID, Ci, KC, KR, KD, Co, OC, OR, OD
 
     def conv3d_backward_input(self, input, kernel, stride, output_, out=None):
@@ -579,7 +591,7 @@ class NN:
 
     def _pool2d(self, which, padding, input, kernel, stride, out=None):
         _verify(self._dims(input) == 4 and len(kernel) == 2 and len(stride) == 2,
-                f"{which}_pool2d: bad dimensions")
+                lambda: f"{which}_pool2d: bad dimensions")
         B, IC, IR, C = self._shape(input)
         KC, KR = kernel
         cs, rs = stride
@@ -614,7 +626,7 @@ class NN:
 
     def _pool2d_backward(self, which, padding, input, kernel, stride, output_, out=None):
         _verify(self._dims(input) == 4 and len(kernel) == 2 and len(stride) == 2,
-                f"{which}_pool2d_backward: bad dimensions")
+                lambda: f"{which}_pool2d_backward: bad dimensions")
         B, IC, IR, C = self._shape(input)
         KC, KR = kernel
         cs, rs = stride
@@ -638,7 +650,7 @@ class NN:
 
     def _pool3d(self, which, padding, input, kernel, stride, out=None):
         _verify(self._dims(input) == 5 and len(kernel) == 3 and len(stride) == 3,
-                f"{which}_pool3d: bad dimensions")
+                lambda: f"{which}_pool3d: bad dimensions")
         B, IC, IR, ID, C = self._shape(input)
         KC, KR, KD = kernel
         cs, rs, ds = stride
@@ -658,7 +670,7 @@ class NN:
 
     def _pool3d_backward(self, which, padding, input, kernel, stride, output_, out=None):
         _verify(self._dims(input) == 5 and len(kernel) == 3 and len(stride) == 3,
-                f"{which}_pool3d_backward: bad dimensions")
+                lambda: f"{which}_pool3d_backward: bad dimensions")
         B, IC, IR, ID, C = self._shape(input)
         KC, KR, KD = kernel
         cs, rs, ds = stride
@@ -692,7 +704,7 @@ class NN:
 
     def _pool1d_backward(self, which, padding, input, kernel, stride, output_, out=None):
         _verify(self._dims(input) == 3 and len(kernel) == 1 and len(stride) == 1,
-                f"{which}_pool1d_backward: bad dimensions")
+                lambda: f"{which}_pool1d_backward: bad dimensions")
         B, IC, C = self._shape(input)
         ob, OC, oc = self._shape(output_)
         dx = self._pool2d_backward(which, padding, self.b.reshape(input, (B, 1, IC, C)),
@@ -713,7 +725,7 @@ class NN:
     def upsampling2d(self, input, size, out=None):
         """G:8223 upsampling2d: `repeat input [|1; size0; size1; 1|]`."""
         _verify(self._dims(input) == 4 and len(size) == 2,
-                f"upsampling2d: input dimension = {self._dims(input)} (should be 4); "
+                lambda: f"upsampling2d: input dimension = {self._dims(input)} (should be 4); "
                 f"size dimension = {len(size)} (should be 2).")
         B, IC, IR, C = self._shape(input)
         cs, rs = size
@@ -726,15 +738,15 @@ class NN:
         """G:8249 upsampling2d_backward input size output: the gradient for
         `input` from the output gradient `output`."""
         _verify(self._dims(input) == 4 and len(size) == 2,
-                f"upsampling2d_backward: input dimension = {self._dims(input)} (should be 4); "
-                f"size dimension = {len(size)} (should be 2).")
+                lambda: f"upsampling2d_backward: input dimension = {self._dims(input)} (should be "
+                f"4); size dimension = {len(size)} (should be 2).")
         B, IC, IR, C = self._shape(input)
         cs, rs = size
         osh = self._shape(output)
         OC, OR = IC * cs, IR * rs
         _verify(len(osh) == 4 and OC == osh[1] and OR == osh[2],
-                f"upsampling2d_backward: output shape is {list(osh)}; scaled output cols is "
-                f"{OC}, should be equal to the 2nd dimension of output shape; scaled output "
+                lambda: f"upsampling2d_backward: output shape is {list(osh)}; scaled output cols "
+                f"is {OC}, should be equal to the 2nd dimension of output shape; scaled output "
                 f"rows is {OR}, should be equal to the 3rd dimension of output shape.")
         input_ = self._out(out, input, (B, IC, IR, C))
         self.b.stub(_kind(input), "upsampling_spatial_backward", input_, output, B, IC, IR, C,
