@@ -348,28 +348,28 @@ def cpu_baseline(budget_s: float = 12.0, batch: int = 2, runs: int = 5):
 
 def accuracy(nn, precision, batch=2):
     """max|gpu - f64| / max|f64| per layer and pass, on a batch-2 sample of
-    each layer: the GPU runs at `precision` on float32 data, the oracle in
-    float64 (Owl's D path restated) on the same values."""
+    each layer: the GPU runs at `precision` on float32 data, the reference
+    is the library's float64 path (the D-module kernels, which the tests pin
+    to the float64 oracle within 1e-11) on the same values."""
     import torch
 
-    import oracle
-    from owl_gb300.dense import NN
+    from owl_gb300.dense import NN, GpuBackend
 
-    O = NN(oracle.OracleBackend(threads=os.cpu_count() or 1))
+    D = NN(GpuBackend("fp32"))  # float64 arrays run the float64 kernels
     out = {}
     worst = 0.0
     for i, (name, xs, ks, st, r, p) in enumerate(LAYERS):
         x, w, dy = make_inputs(xs, ks, st, r, p, seed=500 + i, batch=batch)
         dev = [torch.from_numpy(a).cuda() for a in (x, w, dy)]
         g = [t.cpu().numpy() for t in run_layer(nn, *dev, st, r, p)]
-        ref = run_layer(O, x.astype(np.float64), w.astype(np.float64), dy.astype(np.float64),
-                        st, r, p)
+        dev64 = [torch.from_numpy(a.astype(np.float64)).cuda() for a in (x, w, dy)]
+        ref = [t.cpu().numpy() for t in run_layer(D, *dev64, st, r, p)]
         for op, a, b in zip(("fwd", "bwd_input", "bwd_kernel"), g, ref):
             e = float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
             out[f"{name}.{op}"] = e
             worst = max(worst, e)
     out["max"] = worst
-    out["sample"] = f"batch {batch} of each layer; oracle float64"
+    out["sample"] = f"batch {batch} of each layer; reference: the float64 kernels"
     return out
 
 
@@ -508,10 +508,10 @@ def bench_conv3d(precision: str):
     [4;32;32;32;64] -> [4;64;64;64;32] with its two backward passes
     (12.88 GFLOP); float32 at `precision` and plain FP32, float64 on the D
     path.  Inputs uniform[-1,1], seeded.  Error: max|y - y64| / max|y64|
-    against the float64 oracle on batch 1."""
+    against the library's float64 path (pinned to the float64 oracle by the
+    tests) on batch 1."""
     import torch
 
-    import oracle
     from owl_gb300.dense import NN, GpuBackend
 
     rng = np.random.default_rng(31)
@@ -521,17 +521,25 @@ def bench_conv3d(precision: str):
     f_conv = 2.0 * 4 * 32 ** 3 * 64 * 27 * 32
     f_tconv = 2.0 * 4 * 32 ** 3 * 64 * 8 * 32
     out = {"gflop": {"conv3d_step": 3 * f_conv / 1e9, "transpose_conv3d_step": 3 * f_tconv / 1e9}}
-    O = NN(oracle.OracleBackend(threads=os.cpu_count() or 1))
+    D = NN(GpuBackend("fp32"))  # float64 arrays run the float64 kernels
+
+    def d64(a):
+        return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()
+
+    def host(*ts):
+        return tuple(t.cpu().numpy() for t in ts)
+
     ref = {}
-    x1, w64, wt64 = x[:1].astype(np.float64), w.astype(np.float64), wt.astype(np.float64)
-    y64 = O.conv3d(x1, w64, [1, 1, 1], "SAME")
+    x1, w64, wt64 = d64(x[:1]), d64(w), d64(wt)
+    y64 = D.conv3d(x1, w64, [1, 1, 1], "SAME").cpu().numpy()
     dy1 = rng.standard_normal(y64.shape)
-    ref["conv3d"] = (y64, O.conv3d_backward_input(x1, w64, [1, 1, 1], dy1),
-                     O.conv3d_backward_kernel(x1, w64, [1, 1, 1], dy1))
-    t64 = O.transpose_conv3d(y64, wt64, [2, 2, 2], "SAME")
+    ref["conv3d"] = (y64,) + host(D.conv3d_backward_input(x1, w64, [1, 1, 1], d64(dy1)),
+                                  D.conv3d_backward_kernel(x1, w64, [1, 1, 1], d64(dy1)))
+    t64 = D.transpose_conv3d(d64(y64), wt64, [2, 2, 2], "SAME").cpu().numpy()
     dt1 = rng.standard_normal(t64.shape)
-    ref["transpose_conv3d"] = (t64, O.transpose_conv3d_backward_input(y64, wt64, [2, 2, 2], dt1),
-                               O.transpose_conv3d_backward_kernel(y64, wt64, [2, 2, 2], dt1))
+    ref["transpose_conv3d"] = (t64,) + host(
+        D.transpose_conv3d_backward_input(d64(y64), wt64, [2, 2, 2], d64(dt1)),
+        D.transpose_conv3d_backward_kernel(d64(y64), wt64, [2, 2, 2], d64(dt1)))
     for prec, dt in ((precision, torch.float32), ("fp32", torch.float32), ("fp64", torch.float64)):
         if prec in out:
             continue
@@ -555,7 +563,7 @@ def bench_conv3d(precision: str):
             nn.transpose_conv3d_backward_kernel(Y, WT, [2, 2, 2], DT)
 
         ms3, mst = graph_ms(step3, 3), graph_ms(stept, 3)
-        # accuracy on batch 1, same values as the oracle
+        # accuracy on batch 1, same values as the float64 reference
         X1 = torch.from_numpy(x[:1]).to("cuda", dt)
         D1 = torch.from_numpy(dy1).to("cuda", dt)
         Y1 = torch.from_numpy(y64).to("cuda", dt)
@@ -576,7 +584,8 @@ def bench_conv3d(precision: str):
                      "transpose_conv3d_tflops": 3 * f_tconv / (mst / 1e3) / 1e12,
                      "error_vs_f64": err}
     out["note"] = ("fwd + backward_input + backward_kernel per step; device time of the calls "
-                   "replayed from a CUDA graph; error on batch 1 against the float64 oracle")
+                   "replayed from a CUDA graph; error on batch 1 against the float64 kernels "
+                   "(the fp64 entry is that reference itself)")
     return out
 
 
@@ -997,7 +1006,7 @@ def main():
 
     # ---- the precision ladder on the same step: the plain FP32 CUDA-core
     # kernel and split-BF16 (FP32-level accuracy on the tensor cores), each
-    # timed like the main step and checked against the float64 oracle ----
+    # timed like the main step and checked against the float64 kernels ----
     if not args.no_extras and rank == 0:
         def ladder_step(prec, reps=3):
             nnp = NN(GpuBackend(prec))
@@ -1023,12 +1032,14 @@ def main():
             err = accuracy(nnp, prec)
             return {"value": flops_step / (msp / 1e3) / 1e12, "unit": "TFLOP/s",
                     "ms_per_step": msp, "error_vs_f64_max": err["max"],
-                    "tolerance": {"fp32": 1e-4, "bf16x3": 1e-5}[prec],
+                    "tolerance": {"fp32": 1e-4, "tf32": 5e-3, "bf16x3": 1e-5}[prec],
                     "speedup_of_headline": (flops_step / (ms_per_step / 1e3)) /
                                            (flops_step / (msp / 1e3))}
         result["error_vs_f64"] = accuracy(nn, args.precision)
         if args.precision != "fp32":
             result["fp32_plain"] = ladder_step("fp32")
+        if args.precision != "tf32":
+            result["tf32"] = ladder_step("tf32")
         if args.precision != "bf16x3":
             result["split_bf16"] = ladder_step("bf16x3")
         result["pool"] = bench_pool()
