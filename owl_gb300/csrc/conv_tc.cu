@@ -763,6 +763,77 @@ __global__ void prep_weights(const float *__restrict__ w, uint8_t *__restrict__ 
   }
 }
 
+// The same re-layout, BF16 kinds, when the kernel tensor's channel axes are
+// multiples of 4 and 16-byte aligned and no classes are fused: a thread
+// takes four consecutive output channels n of one (tile, block, tap, chunk)
+// and reads the 32 floats with eight 16-byte loads (along n for the forward,
+// along k for backward_input), then writes the four 16-byte chunks.
+template <int KIND>
+__global__ void prep_weights_v4(const float *__restrict__ w, uint8_t *__restrict__ hi_base,
+                                uint8_t *__restrict__ lo_base, int Ci, int Co, int K, int N,
+                                int BN, int CPB, int NCB, int n_tiles, int bwd_input,
+                                const __grid_constant__ PrepSegs ps) {
+  asm volatile("griddepcontrol.launch_dependents;");
+  static_assert(KIND != K_TF32, "8-channel chunks");
+  const int T = ps.T[blockIdx.y];
+  uint8_t *hi = hi_base + ps.off[blockIdx.y];
+  uint8_t *lo = lo_base ? lo_base + ps.off[blockIdx.y] : nullptr;
+  const int NCH = CPB / 8, BN4 = BN / 4;
+  const TapMap &tm = ps.tm[blockIdx.y];
+  const long long total = (long long)n_tiles * NCB * T * NCH * BN4;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    long long r = i;
+    const int n0 = (int)(r % BN4) * 4; r /= BN4;
+    const int j = (int)(r % NCH); r /= NCH;
+    const int tap = (int)(r % T); r /= T;
+    const int cb = (int)(r % NCB);
+    const int nt = (int)(r / NCB);
+    const int nf0 = nt * BN + n0;
+    const int ta = tap / (tm.K[1] * tm.K[2]), tb = tap / tm.K[2] % tm.K[1], tc = tap % tm.K[2];
+    const long long orig =
+        ((long long)(tm.base[0] + tm.mul[0] * ta) * tm.KO[1] + (tm.base[1] + tm.mul[1] * tb)) *
+            tm.KO[2] + (tm.base[2] + tm.mul[2] * tc);
+    const int k0 = cb * CPB + j * 8;
+    float v[4][8];
+    if (!bwd_input) {  // W[tap][k][n]: 16 bytes along n
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (k0 + e < K && nf0 < N)
+          f = __ldg(reinterpret_cast<const float4 *>(w + (orig * Ci + k0 + e) * Co + nf0));
+        v[0][e] = f.x; v[1][e] = f.y; v[2][e] = f.z; v[3][e] = f.w;
+      }
+    } else {  // channel-exchanged W[tap][n][k]: 16 bytes along k
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int e = 0; e < 8; e += 4) {
+          float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (k0 + e < K && nf0 + q < N)
+            f = __ldg(reinterpret_cast<const float4 *>(w + (orig * Ci + nf0 + q) * Co + k0 + e));
+          v[q][e] = f.x; v[q][e + 1] = f.y; v[q][e + 2] = f.z; v[q][e + 3] = f.w;
+        }
+    }
+    const long long tile = ((long long)nt * NCB + cb) * T + tap;
+    const long long off = tile * (long long)NCH * BN * 16 + ((long long)j * BN + n0) * 16;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      *reinterpret_cast<uint4 *>(hi + off + q * 16) =
+          make_uint4(pack_bf16(v[q][0], v[q][1]), pack_bf16(v[q][2], v[q][3]),
+                     pack_bf16(v[q][4], v[q][5]), pack_bf16(v[q][6], v[q][7]));
+      if (KIND == K_BF16X3) {
+        float rr[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) rr[e] = v[q][e] - bf16_round(v[q][e]);
+        *reinterpret_cast<uint4 *>(lo + off + q * 16) =
+            make_uint4(pack_bf16(rr[0], rr[1]), pack_bf16(rr[2], rr[3]), pack_bf16(rr[4], rr[5]),
+                       pack_bf16(rr[6], rr[7]));
+      }
+    }
+  }
+}
+
 // A convolution seen as (w, u, v) spatial axes plus channels.
 struct View {
   int B, IW, IU, IV, OW, OU, OV, KW, KU, KV, dw, du, dv, pw, pu, pv, sw, su, sv;
@@ -1186,7 +1257,19 @@ int run_segs(int prec, int nseg_in, const SegSpec *sp, bool bwd_input, int Ci, i
     const long long n = (long long)p.n_tiles * p.NCB * t_slot * p.NCH * p.BN;
     const dim3 grid((unsigned)std::min<long long>((n + 255) / 256, 4096), (unsigned)nseg);
     const int K = pv.Cin, N = pv.Cout;
-    if (kind == K_TF32)
+    // the vector re-layout: 16-byte loads along the kernel tensor's Co axis
+    // (n for the forward, k for backward_input) and whole 4-channel groups
+    const bool v4 = kind != K_TF32 && !fuse_n && (uintptr_t)w % 16 == 0 && Co % 4 == 0 &&
+                    K % 4 == 0 && N % 4 == 0 && p.BN % 4 == 0;
+    if (v4) {
+      const dim3 g4((unsigned)std::min<long long>((n / 4 + 255) / 256, 4096), (unsigned)nseg);
+      if (kind == K_BF16X3)
+        prep_weights_v4<K_BF16X3><<<g4, 256, 0, s>>>(w, hi, lo, Ci, Co, K, N, p.BN, p.CPB,
+                                                     p.NCB, p.n_tiles, bwd_input, ps);
+      else
+        prep_weights_v4<K_BF16><<<g4, 256, 0, s>>>(w, hi, nullptr, Ci, Co, K, N, p.BN, p.CPB,
+                                                   p.NCB, p.n_tiles, bwd_input, ps);
+    } else if (kind == K_TF32)
       prep_weights<K_TF32><<<grid, 256, 0, s>>>(w, hi, nullptr, Ci, Co, K, N, p.BN, p.CPB, p.NCB,
                                                 p.n_tiles, bwd_input, ps);
     else if (kind == K_BF16X3)
