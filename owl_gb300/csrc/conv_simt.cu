@@ -335,10 +335,10 @@ __global__ void splitk_reduce_kernel(const T *__restrict__ part, T *__restrict__
 
 // ---- float32 vector path ----------------------------------------------------
 // The same GEMM views in float32 with 16-byte operand gathers: 128 x 128
-// tiles (128 x 64 when N <= 64), 16-deep k slabs, 256 threads of 8 x 8
-// outputs (four 4 x 4 quadrants, rows ty*4 and 64 + ty*4, columns tx*4 and
-// 64 + tx*4, so every shared-memory fragment is one 16-byte load without
-// bank conflicts; 8 x 4 in the 64-wide tile).
+// tiles (128 x 64 when N <= 64, 256 x 32 when N <= 32), 16-deep k slabs,
+// 256 threads of 8 x 8 outputs (four 4 x 4 quadrants, rows ty*4 and
+// 64 + ty*4, columns tx*4 and 64 + tx*4, so every shared-memory fragment is
+// one 16-byte load without bank conflicts; 8 x 4 in the narrower tiles).
 //   FWD : a slab is 16 consecutive input channels of one tap (Ci % 16 == 0);
 //         four threads read one pixel's 64 bytes, and each thread's two
 //         output pixels are decoded once per CTA.  A is stored k-major with
@@ -351,48 +351,67 @@ __global__ void splitk_reduce_kernel(const T *__restrict__ part, T *__restrict__
 // The k order of every output's sum is the same as the scalar kernel's
 // (ascending, one fused multiply-add per k), so a float32 forward gives the
 // same bits on either path.
-constexpr int kVBM = 128, kVBK = 16, kVNT = 256;
+constexpr int kVBK = 16, kVNT = 256;
 
 __device__ __forceinline__ float4 ldg4(const float *p) {
   return __ldg(reinterpret_cast<const float4 *>(p));
 }
 
-// CN: 64-column blocks per tile (a thread holds 4 columns of each): 2 for
-// N > 64, 1 for 32 < N <= 64 (8 x 4 outputs per thread).
+// Tile shapes, by the GEMM's N:
+//   CN = 2: 128 x 128, a thread 8 x 8 (rows ty*4 + {0, 64}, columns tx*4 + {0, 64})
+//   CN = 1: 128 x 64,  a thread 8 x 4 (columns tx*4)
+//   CN = 0: 256 x 32,  a thread 8 x 4 (rows ty*4 + {0, 128}, columns tx*4)
+template <int CN>
+struct F32vShape {
+  static constexpr int BM = CN == 0 ? 256 : 128;
+  static constexpr int BN = CN == 0 ? 32 : 64 * CN;
+  static constexpr int RQ = BM / 64;    // FWD: A rows per thread (a 4-channel quad each)
+  static constexpr int NJ = CN == 0 ? 1 : CN;  // column quads per thread
+  static constexpr int RSTEP = BM / 2;  // a thread's second row quad
+  static constexpr int BH = CN == 2 ? 2 : 1;  // B float4 loads per thread
+};
+
 template <int MODE, int CN>
 __global__ void __launch_bounds__(kVNT, 1)
     conv_f32v_kernel(Dev g, const float *__restrict__ A0, const float *__restrict__ B0,
                      float *__restrict__ C, int64_t k_per_split) {
-  constexpr int BN = 64 * CN;
-  __shared__ __align__(16) float As[2][kVBK][kVBM];
+  using S = F32vShape<CN>;
+  constexpr int BM = S::BM, BN = S::BN, RQ = S::RQ, NJ = S::NJ;
+  __shared__ __align__(16) float As[2][kVBK][BM];
   __shared__ __align__(16) float Bs[2][kVBK][BN];
   __shared__ int64_t s_base[2][kVBK];  // BWDK: slab pixels (batch image offset, -1 past the end)
   __shared__ int s_c[2][kVBK], s_r[2][kVBK], s_d[2][kVBK];
 
   const int tid = threadIdx.x;
-  // a warp covers 8 row groups x 4 column groups: its 16-byte fragment loads
-  // touch 128 contiguous bytes of A and 64 of B (one shared-memory wavefront
-  // each) per k
+  // A warp's 16-byte fragment loads touch one contiguous run of A and one of
+  // B per k (one shared-memory wavefront each): 8 row groups x 4 column
+  // groups in the 128-row tiles, 4 x 8 in the 256-row one.
   const int lane = tid & 31, warp = tid >> 5;
-  const int ty = (warp >> 2) * 8 + (lane >> 2), tx = (warp & 3) * 4 + (lane & 3);
-  const int64_t m0 = (int64_t)blockIdx.x * kVBM, n0 = (int64_t)blockIdx.y * BN;
+  const int ty = CN == 0 ? warp * 4 + (lane >> 3) : (warp >> 2) * 8 + (lane >> 2);
+  const int tx = CN == 0 ? (lane & 7) : (warp & 3) * 4 + (lane & 3);
+  const int64_t m0 = (int64_t)blockIdx.x * BM, n0 = (int64_t)blockIdx.y * BN;
   const int64_t k_begin = (int64_t)blockIdx.z * k_per_split;
   const int64_t k_end = min(g.K, k_begin + k_per_split);
   const int64_t img = g.IC * g.IR * g.ID;  // pixels per batch image of X
 
-  // ---- FWD: this thread's two output pixels and its channel quad ----------
+  // ---- FWD: this thread's RQ output pixels and its channel quad -----------
   const int aq = tid & 3;  // FWD: channel quad within the slab
-  int64_t abase[2] = {-1, -1};
-  int ac[2] = {0, 0}, ar[2] = {0, 0}, ad[2] = {0, 0};
-  // ---- BWDK: this thread's four (tap, ci) rows ----------------------------
-  const int mq = (tid & 31) * 4;  // BWDK: row quad within the tile
+  int64_t abase[RQ];
+  int ac[RQ], ar[RQ], ad[RQ];
+  // ---- BWDK: this thread's four (tap, ci) rows, its pixels ak + k*(256/(BM/4))
+  constexpr int MQ = BM / 4;       // row quads per k row
+  constexpr int AKS = kVNT / MQ;   // k rows per pass
+  const int mq = (tid % MQ) * 4;
+  const int ak = tid / MQ;
   bool mval = false;
   int t_dc = 0, t_dr = 0, t_dd = 0;
   int64_t mci = 0;
   if (MODE == FWD) {
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
+    for (int h = 0; h < RQ; ++h) {
       const int64_t m = m0 + (tid >> 2) + 64 * h;
+      abase[h] = -1;
+      ac[h] = ar[h] = ad[h] = 0;
       if (m < g.M) {
         int64_t t = m;
         const int64_t od = t % g.OD;
@@ -450,18 +469,20 @@ __global__ void __launch_bounds__(kVNT, 1)
     kc = (int)(tap / g.KR);
   }
 
-  float4 va[2], vb[CN];
-  // B: float4 column bcol of k rows bk (+ 8); BWDK's A: pixels ak (+ 8)
-  const int bcol = CN == 2 ? (tid & 31) * 4 : (tid & 15) * 4;
-  const int bk = CN == 2 ? tid >> 5 : tid >> 4;
-  const int ak = tid >> 5;
-  const bool bval = n0 + bcol < g.N;
+  // A: FWD RQ float4 (pixels), BWDK 16/AKS float4 (k rows); B: BH float4
+  constexpr int AH = MODE == FWD ? RQ : kVBK / AKS;
+  float4 va[AH], vb[S::BH];
+  // B: float4 column bcol of k rows bk (+ 8)
+  constexpr int BQ = BN / 4;  // float4 per k row of B
+  const int bcol = (tid % BQ) * 4;
+  const int bk = tid / BQ;
+  const bool bval = bk < kVBK && n0 + bcol < g.N;  // (256x32: threads past 128 load no B)
 
   // global -> registers for slab k0 (FWD: at tap kc/kr/kd, channels ci0..)
   auto load = [&](int64_t k0, int buf) {
     if (MODE == FWD) {
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
+      for (int h = 0; h < AH; ++h) {
         const int c = ac[h] + kc * g.dc, r = ar[h] + kr * g.dr, d = ad[h] + kd * g.dd;
         va[h] = make_float4(0.f, 0.f, 0.f, 0.f);
         if (abase[h] >= 0 && (unsigned)c < (unsigned)g.IC && (unsigned)r < (unsigned)g.IR &&
@@ -470,8 +491,8 @@ __global__ void __launch_bounds__(kVNT, 1)
       }
     } else {
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int kl = ak + 8 * h;
+      for (int h = 0; h < AH; ++h) {
+        const int kl = ak + AKS * h;
         const int64_t base = s_base[buf][kl];
         va[h] = make_float4(0.f, 0.f, 0.f, 0.f);
         if (mval && base >= 0) {
@@ -483,7 +504,7 @@ __global__ void __launch_bounds__(kVNT, 1)
       }
     }
 #pragma unroll
-    for (int h = 0; h < CN; ++h) {
+    for (int h = 0; h < S::BH; ++h) {
       const int64_t kq = k0 + bk + 8 * h;
       vb[h] = (bval && kq < k_end) ? ldg4(B0 + kq * g.N + n0 + bcol)
                                    : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -492,7 +513,7 @@ __global__ void __launch_bounds__(kVNT, 1)
   auto store = [&](int buf) {
     if (MODE == FWD) {
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
+      for (int h = 0; h < AH; ++h) {
         const int row = ((tid >> 2) + 64 * h) ^ (aq << 3);
         As[buf][aq * 4 + 0][row] = va[h].x;
         As[buf][aq * 4 + 1][row] = va[h].y;
@@ -501,11 +522,14 @@ __global__ void __launch_bounds__(kVNT, 1)
       }
     } else {
 #pragma unroll
-      for (int h = 0; h < 2; ++h)
-        *reinterpret_cast<float4 *>(&As[buf][ak + 8 * h][mq]) = va[h];
+      for (int h = 0; h < AH; ++h)
+        *reinterpret_cast<float4 *>(&As[buf][ak + AKS * h][mq]) = va[h];
     }
+    if (bk < kVBK) {
 #pragma unroll
-    for (int h = 0; h < CN; ++h) *reinterpret_cast<float4 *>(&Bs[buf][bk + 8 * h][bcol]) = vb[h];
+      for (int h = 0; h < S::BH; ++h)
+        *reinterpret_cast<float4 *>(&Bs[buf][bk + 8 * h][bcol]) = vb[h];
+    }
   };
   auto next_tap = [&]() {
     ci0 += kVBK;
@@ -521,11 +545,11 @@ __global__ void __launch_bounds__(kVNT, 1)
     }
   };
 
-  float acc[8][4 * CN];
+  float acc[8][4 * NJ];
 #pragma unroll
   for (int i = 0; i < 8; ++i)
 #pragma unroll
-    for (int j = 0; j < 4 * CN; ++j) acc[i][j] = 0.f;
+    for (int j = 0; j < 4 * NJ; ++j) acc[i][j] = 0.f;
 
   if (k_begin < k_end) {
     if (MODE == BWDK) {
@@ -547,22 +571,23 @@ __global__ void __launch_bounds__(kVNT, 1)
 #pragma unroll
       for (int k = 0; k < kVBK; ++k) {
         const int sw = MODE == FWD ? ((k >> 2) << 3) : 0;
-        const float4 a0 = *reinterpret_cast<const float4 *>(&As[buf][k][(ty * 4) ^ sw]);
-        const float4 a1 = *reinterpret_cast<const float4 *>(&As[buf][k][(64 + ty * 4) ^ sw]);
-        const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-        float b[4 * CN];
+        float a[8];
 #pragma unroll
-        for (int q = 0; q < CN; ++q) {
-          const float4 v = *reinterpret_cast<const float4 *>(&Bs[buf][k][64 * q + tx * 4]);
-          b[4 * q] = v.x;
-          b[4 * q + 1] = v.y;
-          b[4 * q + 2] = v.z;
-          b[4 * q + 3] = v.w;
+        for (int q = 0; q < 2; ++q) {
+          const float4 f =
+              *reinterpret_cast<const float4 *>(&As[buf][k][(S::RSTEP * q + ty * 4) ^ sw]);
+          a[4 * q] = f.x; a[4 * q + 1] = f.y; a[4 * q + 2] = f.z; a[4 * q + 3] = f.w;
+        }
+        float b[4 * NJ];
+#pragma unroll
+        for (int q = 0; q < NJ; ++q) {
+          const float4 f = *reinterpret_cast<const float4 *>(&Bs[buf][k][64 * q + tx * 4]);
+          b[4 * q] = f.x; b[4 * q + 1] = f.y; b[4 * q + 2] = f.z; b[4 * q + 3] = f.w;
         }
 #pragma unroll
         for (int i = 0; i < 8; ++i)
 #pragma unroll
-          for (int j = 0; j < 4 * CN; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+          for (int j = 0; j < 4 * NJ; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
       }
       if (more) {
         store(buf ^ 1);
@@ -576,7 +601,7 @@ __global__ void __launch_bounds__(kVNT, 1)
   float *Cz = C + (int64_t)blockIdx.z * g.M * g.N;
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
-    const int64_t m = m0 + (i < 4 ? ty * 4 + i : 64 + ty * 4 + i - 4);
+    const int64_t m = m0 + S::RSTEP * (i >> 2) + ty * 4 + (i & 3);
     if (m >= g.M) continue;
     int64_t row = m;
     if (MODE == FWD && g.ystrided) {
@@ -589,7 +614,7 @@ __global__ void __launch_bounds__(kVNT, 1)
       row = g.yoff + b * g.ysb + oc * g.ysc + orr * g.ysr + od * g.ysd;
     }
 #pragma unroll
-    for (int q = 0; q < CN; ++q) {
+    for (int q = 0; q < NJ; ++q) {
       const int64_t n = n0 + q * 64 + tx * 4;
       if (n < g.N)
         *reinterpret_cast<float4 *>(Cz + row * g.N + n) =
@@ -599,13 +624,12 @@ __global__ void __launch_bounds__(kVNT, 1)
 }
 
 // Whether the float32 vector path takes a launch: 16-byte aligned operands,
-// N a multiple of 4 above 32 (64- or 128-wide tiles), FWD slabs inside one
-// tap (Ci % 16, whole slabs per split), BWDK rows in quads of one tap
-// (Ci % 4).
+// N a multiple of 4 (128-, 64- or 32-wide tiles), FWD slabs inside one tap
+// (Ci % 16, whole slabs per split), BWDK rows in quads of one tap (Ci % 4).
 bool f32v_ok(int mode, const Dev &d, const void *A, const void *B, const void *C,
              int64_t kps) {
   auto al = [](const void *p) { return ((uintptr_t)p & 15) == 0; };
-  if (!al(A) || !al(B) || !al(C) || d.N % 4 != 0 || d.N <= 32) return false;
+  if (!al(A) || !al(B) || !al(C) || d.N % 4 != 0 || d.N == 0) return false;
   if (d.IC >= (1 << 30) || d.IR >= (1 << 30) || d.ID >= (1 << 30)) return false;
   if (mode == FWD) return d.Ci % kVBK == 0 && kps % kVBK == 0;
   if (mode == BWDK) return d.Ci % 4 == 0;
@@ -615,12 +639,15 @@ bool f32v_ok(int mode, const Dev &d, const void *A, const void *B, const void *C
 template <int MODE>
 int launch_f32v(const Dev &d, const float *A, const float *B, float *C, int splits, int64_t kps,
                 cudaStream_t s) {
-  const int bn = d.N > 64 ? 128 : 64;
-  dim3 grid((unsigned)ceil_div(d.M, kVBM), (unsigned)ceil_div(d.N, bn), (unsigned)splits);
-  if (bn == 128)
+  const int cn = d.N > 64 ? 2 : (d.N > 32 ? 1 : 0);
+  const int bm = cn == 0 ? 256 : 128, bn = cn == 0 ? 32 : 64 * cn;
+  dim3 grid((unsigned)ceil_div(d.M, bm), (unsigned)ceil_div(d.N, bn), (unsigned)splits);
+  if (cn == 2)
     conv_f32v_kernel<MODE, 2><<<grid, kVNT, 0, s>>>(d, A, B, C, kps);
-  else
+  else if (cn == 1)
     conv_f32v_kernel<MODE, 1><<<grid, kVNT, 0, s>>>(d, A, B, C, kps);
+  else
+    conv_f32v_kernel<MODE, 0><<<grid, kVNT, 0, s>>>(d, A, B, C, kps);
   OWL_CHECK_LAUNCH("conv_f32v_kernel");
   return kOk;
 }
@@ -672,7 +699,7 @@ int launch_any(const Dev &d, const T *A, const T *B, T *C, int splits, int64_t k
 }
 
 template <typename T>
-int tile_m(const Dev &d) { return sizeof(T) == 4 ? 128 : 64; }
+int tile_m(const Dev &d) { return sizeof(T) == 4 ? (d.N <= 32 ? 256 : 128) : 64; }
 template <typename T>
 int tile_n(const Dev &d) {
   if (sizeof(T) == 4) return d.N > 64 ? 128 : (d.N > 32 ? 64 : 32);
