@@ -32,6 +32,13 @@ struct Dev {
   // residue class of a backward_input); otherwise the output is dense.
   int ystrided;
   int64_t yoff, ysb, ysc, ysr, ysd;
+  // FWD, float32 vector kernel only, ystrided == 2 (window scatter): column
+  // n = t*s2d_ci + ci of row m goes to output pixel (row pixel of m) +
+  // tc*s2d_tc + tr*s2d_tr + td, channel ci, for tap t = (tc*s2d_kr + tr)*s2d_kd
+  // + td (a backward_input whose kernel equals its stride: every input pixel
+  // receives exactly one tap)
+  int64_t s2d_ci, s2d_tc, s2d_tr;
+  int s2d_kr, s2d_kd;
 };
 
 template <typename T, int MODE, int BM, int BN, int BK, int TM, int TN>
@@ -616,9 +623,18 @@ __global__ void __launch_bounds__(kVNT, 1)
 #pragma unroll
     for (int q = 0; q < NJ; ++q) {
       const int64_t n = n0 + q * 64 + tx * 4;
-      if (n < g.N)
-        *reinterpret_cast<float4 *>(Cz + row * g.N + n) =
-            make_float4(acc[i][4 * q], acc[i][4 * q + 1], acc[i][4 * q + 2], acc[i][4 * q + 3]);
+      if (n >= g.N) continue;
+      const float4 v =
+          make_float4(acc[i][4 * q], acc[i][4 * q + 1], acc[i][4 * q + 2], acc[i][4 * q + 3]);
+      if (MODE == FWD && g.ystrided == 2) {
+        const int64_t t = n / g.s2d_ci, ci = n - t * g.s2d_ci;
+        const int64_t tc = t / (g.s2d_kr * g.s2d_kd), tr = (t / g.s2d_kd) % g.s2d_kr,
+                      td = t % g.s2d_kd;
+        *reinterpret_cast<float4 *>(
+            Cz + (row + tc * g.s2d_tc + tr * g.s2d_tr + td) * g.s2d_ci + ci) = v;
+      } else {
+        *reinterpret_cast<float4 *>(Cz + row * g.N + n) = v;
+      }
     }
   }
 }
@@ -653,7 +669,7 @@ int launch_f32v(const Dev &d, const float *A, const float *B, float *C, int spli
 }
 
 Dev make_dev(const ConvGeom &g, int mode) {
-  Dev d;
+  Dev d{};
   d.B = g.B; d.IC = g.IC; d.IR = g.IR; d.ID = g.ID; d.Ci = g.Ci;
   d.KC = g.KC; d.KR = g.KR; d.KD = g.KD;
   d.OC = g.OC; d.OR = g.OR; d.OD = g.OD; d.Co = g.Co;
@@ -739,6 +755,68 @@ __global__ void bwdi_class_weights(const T *__restrict__ w, T *__restrict__ w2, 
   }
 }
 
+// The kernel of a kernel = stride backward_input as one GEMM operand:
+// w2[co][t*Ci + ci] = w[t][ci][co].
+__global__ void window_weights(const float *__restrict__ w, float *__restrict__ w2, int64_t T,
+                               int64_t Ci, int64_t Co) {
+  const int64_t total = T * Ci * Co;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ci = i % Ci;
+    const int64_t r = i / Ci;
+    const int64_t t = r % T, co = r / T;
+    w2[i] = w[(t * Ci + ci) * Co + co];
+  }
+}
+
+// float32 backward_input of a convolution whose kernel equals its stride
+// (no dilation, no padding, the windows tiling the input exactly): every
+// input pixel takes exactly one tap of one output pixel, so dX is one GEMM,
+// dY [pixels][Co] x w2 [Co][taps*Ci], scattered window by window
+// (depth-to-space) in its epilogue.  One launch reads dY once, where the
+// residue classes (one tap each) read it once per class.  Returns 1 when the
+// geometry or the operands do not qualify.
+int bwdi_window_f32(const ConvGeom &g, float *dx, const float *w, const float *dy,
+                    cudaStream_t s) {
+  const bool win = g.KC == g.sc && g.KR == g.sr && g.KD == g.sd && g.dc == 1 && g.dr == 1 &&
+                   g.dd == 1 && g.pc == 0 && g.pr == 0 && g.pd == 0 &&
+                   g.IC == g.OC * g.sc && g.IR == g.OR * g.sr && g.ID == g.OD * g.sd &&
+                   g.taps() > 1;
+  if (!win) return 1;
+  ConvGeom gc{};
+  gc.B = g.B;
+  gc.IC = g.OC; gc.IR = g.OR; gc.ID = g.OD; gc.Ci = g.Co;
+  gc.KC = gc.KR = gc.KD = 1;
+  gc.OC = g.OC; gc.OR = g.OR; gc.OD = g.OD; gc.Co = g.taps() * g.Ci;
+  gc.sc = gc.sr = gc.sd = 1;
+  gc.dc = gc.dr = gc.dd = 1;
+  Dev d = make_dev(gc, FWD);
+  d.ystrided = 2;
+  d.yoff = 0;
+  d.ysb = g.IC * g.IR * g.ID;
+  d.ysc = (int64_t)g.sc * g.IR * g.ID;
+  d.ysr = (int64_t)g.sr * g.ID;
+  d.ysd = g.sd;
+  d.s2d_ci = g.Ci;
+  d.s2d_tc = g.IR * g.ID;
+  d.s2d_tr = g.ID;
+  d.s2d_kr = (int)g.KR;
+  d.s2d_kd = (int)g.KD;
+  if (g.Ci % 4 != 0 || !f32v_ok(FWD, d, dy, dy, dx, d.K)) return 1;  // w2 is fresh scratch
+  float *w2 = nullptr;
+  int rc = scratch_alloc((void **)&w2, sizeof(float) * (size_t)g.w_elems(), s);
+  if (rc) return rc;
+  const int64_t nw = g.w_elems();
+  window_weights<<<(unsigned)std::min<int64_t>(ceil_div(nw, 256), 1024), 256, 0, s>>>(
+      w, w2, g.taps(), g.Ci, g.Co);
+  cudaError_t e = cudaGetLastError();
+  note_launch();
+  if (e != cudaSuccess) rc = cuda_fail(e, "window_weights");
+  if (rc == kOk) rc = launch_f32v<FWD>(d, dy, w2, dx, 1, d.K, s);
+  scratch_free(w2, s);
+  return rc;
+}
+
 // backward_input as forward convolutions over the residue classes of dX.
 // With forward index s*o - p + t*d, element i = s*a + r of dX receives
 // dY[o] W[t] for the taps with (r + p - t*d) divisible by s, at
@@ -752,6 +830,12 @@ __global__ void bwdi_class_weights(const T *__restrict__ w, T *__restrict__ w2, 
 template <typename T>
 int bwdi_t(const ConvGeom &g, T *dx, const T *w, const T *dy, cudaStream_t s) {
   if (g.in_pixels() == 0 || g.Ci == 0) return kOk;
+  if constexpr (std::is_same_v<T, float>) {
+    if (g.Co > 0 && g.out_pixels() > 0) {
+      const int rc = bwdi_window_f32(g, dx, w, dy, s);
+      if (rc != 1) return rc;
+    }
+  }
   const int S[3] = {g.sc, g.sr, g.sd}, D[3] = {g.dc, g.dr, g.dd}, P[3] = {g.pc, g.pr, g.pd};
   const int64_t K[3] = {g.KC, g.KR, g.KD}, I[3] = {g.IC, g.IR, g.ID};
   struct Axis {
