@@ -1,10 +1,11 @@
 """The float32 CUDA-core vector kernels (conv_f32v_kernel: 16-byte operand
-gathers, 128x128 or 128x64 tiles, 16-deep k slabs) at the edges of where
-they apply, against the float32 oracle (Owl's S path restated) at 1e-4:
-output channels that fill neither tile width (partial column tiles), reduction
-lengths that end inside a k slab, several split-K partials, strides,
-dilation and 3-D windows, and operands that are not 16-byte aligned (which
-take the scalar kernel instead, with the same results)."""
+gathers, 128x128, 128x64 or 256x32 tiles, 16-deep k slabs) at the edges of
+where they apply, against the float32 oracle (Owl's S path restated) at
+1e-4: output channels that fill no tile width (partial column tiles),
+reduction lengths that end inside a k slab, several split-K partials,
+strides, dilation and 3-D windows, kernel = stride backward_input as one
+window-scatter GEMM, and operands that are not 16-byte aligned (which take
+the scalar kernel instead, with the same results)."""
 
 import numpy as np
 import pytest
@@ -118,3 +119,30 @@ def test_unaligned_operands_give_the_same_results(gpu_lib):
     torch.cuda.synchronize()
     assert np.array_equal(yv.cpu().numpy().reshape(ys), aligned)
     del xb, wb, yb
+
+
+@pytest.mark.parametrize("dims", [2, 3])
+def test_window_backward_input(gpu_lib, oracle_nn, dims):
+    """A backward_input whose kernel equals its stride (and the transpose
+    convolution forward that is one) runs as one GEMM with a window-scatter
+    epilogue; every dX element written once, against the float32 oracle."""
+    rng = np.random.default_rng(75)
+    G, O = _nn(), oracle_nn
+    if dims == 2:
+        xs, ks, st = (3, 12, 10, 36), (2, 2, 36, 48), [2, 2]
+        bwd, conv = G.conv2d_backward_input, O.conv2d_backward_input
+        tconv_g, tconv_o = G.transpose_conv2d, O.transpose_conv2d
+    else:
+        xs, ks, st = (2, 6, 8, 4, 20), (2, 2, 2, 20, 32), [2, 2, 2]
+        bwd, conv = G.conv3d_backward_input, O.conv3d_backward_input
+        tconv_g, tconv_o = G.transpose_conv3d, O.transpose_conv3d
+    x = rng.uniform(-1, 1, xs).astype(np.float32)
+    w = (rng.standard_normal(ks) * 0.2).astype(np.float32)
+    oshape = (xs[0],) + tuple(d // s for d, s in zip(xs[1:-1], st)) + (ks[-1],)
+    dy = rng.standard_normal(oshape).astype(np.float32)
+    dx = from_dev(bwd(to_dev(x), to_dev(w), st, to_dev(dy)))
+    assert rel(dx, conv(x, w, st, dy)) <= TOL
+    # transpose convolution forward: kernel [.., in=Co, out=Ci]
+    wt = np.ascontiguousarray(np.swapaxes(w, -1, -2))
+    y = from_dev(tconv_g(to_dev(dy), to_dev(wt), st, "SAME"))
+    assert rel(y, tconv_o(dy, wt, st, "SAME")) <= TOL
