@@ -322,3 +322,25 @@ def test_kernel_equals_stride_with_channels_off_the_chunk_runs_the_conv_kernel(g
     assert _path() == 1
     assert rel(y, f64_nn.conv2d(x.astype(np.float64), w.astype(np.float64), [2, 2],
                                 VALID)) <= TOL["bf16"]
+
+
+@pytest.mark.parametrize("rows", [1, 3, 5, 7, 9, 15, 17, 29, 33, 56])
+def test_tile_heights(gpu_lib, f64_nn, rows):
+    """Output heights that select every kind of tile the planner may choose
+    (one tile of the output's even height, the fewest tiles of up to 32
+    rows, partial last tiles, two co tiles under 128 pixels), forward and
+    backward_input, BF16, against the float64 oracle."""
+    rng = np.random.default_rng(77)
+    x = rng.uniform(-1, 1, (2, rows, 11, 64)).astype(np.float32)
+    w = (rng.standard_normal((3, 3, 64, 160)) * 0.06).astype(np.float32)
+    G = _nn("bf16")
+    y = from_dev(G.conv2d(to_dev(x), to_dev(w), [1, 1], SAME))
+    assert _path() == 1
+    y64 = f64_nn.conv2d(x.astype(np.float64), w.astype(np.float64), [1, 1], SAME)
+    assert rel(y, y64) <= TOL["bf16"]
+    dy = rng.standard_normal(y64.shape).astype(np.float32)
+    dx = from_dev(G.conv2d_backward_input(to_dev(x), to_dev(w), [1, 1], to_dev(dy)))
+    assert _path() == 1
+    ref = f64_nn.conv2d_backward_input(x.astype(np.float64), w.astype(np.float64), [1, 1],
+                                       dy.astype(np.float64))
+    assert rel(dx, ref) <= TOL["bf16"]
