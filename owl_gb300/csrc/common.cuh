@@ -141,6 +141,26 @@ int cuda_fail(cudaError_t e, const char *where);
 extern std::atomic<uint64_t> g_launches;
 inline void note_launch(int n = 1) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
 
+// Launch kernel k as a programmatic dependent of the work before it on s: it
+// may be scheduled while that work drains, so the launch gap overlaps the
+// previous kernel's tail.  Every such kernel executes griddepcontrol.wait
+// before it touches global memory, and so sees all earlier work complete.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                       Args &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, static_cast<Args &&>(args)...);
+}
+
 #define OWL_CHECK_LAUNCH(where)                                   \
   do {                                                            \
     owlgpu::note_launch();                                        \

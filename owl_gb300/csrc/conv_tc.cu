@@ -703,8 +703,11 @@ __global__ void prep_weights(const float *__restrict__ w, uint8_t *__restrict__ 
                              uint8_t *__restrict__ lo_base, int Ci, int Co, int K, int N,
                              int BN, int CPB, int NCB, int n_tiles, int bwd_input,
                              const __grid_constant__ PrepSegs ps) {
-  // the convolution launched next may start its prologue and halo staging
-  // now; its weight loader waits for this grid (griddepcontrol.wait)
+  // Launched as a programmatic dependent of whatever ran before it: wait
+  // for that work (the kernel tensor may be its output), then let the
+  // convolution launched next start its prologue and halo staging; its
+  // weight loader waits for this grid (griddepcontrol.wait).
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   asm volatile("griddepcontrol.launch_dependents;");
   const int T = ps.T[blockIdx.y];
   uint8_t *hi = hi_base + ps.off[blockIdx.y];
@@ -773,6 +776,7 @@ __global__ void prep_weights_v4(const float *__restrict__ w, uint8_t *__restrict
                                 uint8_t *__restrict__ lo_base, int Ci, int Co, int K, int N,
                                 int BN, int CPB, int NCB, int n_tiles, int bwd_input,
                                 const __grid_constant__ PrepSegs ps) {
+  asm volatile("griddepcontrol.wait;" ::: "memory");  // as prep_weights
   asm volatile("griddepcontrol.launch_dependents;");
   static_assert(KIND != K_TF32, "8-channel chunks");
   const int T = ps.T[blockIdx.y];
@@ -1261,24 +1265,25 @@ int run_segs(int prec, int nseg_in, const SegSpec *sp, bool bwd_input, int Ci, i
     // (n for the forward, k for backward_input) and whole 4-channel groups
     const bool v4 = kind != K_TF32 && !fuse_n && (uintptr_t)w % 16 == 0 && Co % 4 == 0 &&
                     K % 4 == 0 && N % 4 == 0 && p.BN % 4 == 0;
+    cudaError_t e;
     if (v4) {
       const dim3 g4((unsigned)std::min<long long>((n / 4 + 255) / 256, 4096), (unsigned)nseg);
       if (kind == K_BF16X3)
-        prep_weights_v4<K_BF16X3><<<g4, 256, 0, s>>>(w, hi, lo, Ci, Co, K, N, p.BN, p.CPB,
-                                                     p.NCB, p.n_tiles, bwd_input, ps);
+        e = launch_pdl(prep_weights_v4<K_BF16X3>, g4, dim3(256), 0, s, w, hi, lo, Ci, Co, K, N,
+                       p.BN, p.CPB, p.NCB, p.n_tiles, (int)bwd_input, ps);
       else
-        prep_weights_v4<K_BF16><<<g4, 256, 0, s>>>(w, hi, nullptr, Ci, Co, K, N, p.BN, p.CPB,
-                                                   p.NCB, p.n_tiles, bwd_input, ps);
+        e = launch_pdl(prep_weights_v4<K_BF16>, g4, dim3(256), 0, s, w, hi, (uint8_t *)nullptr,
+                       Ci, Co, K, N, p.BN, p.CPB, p.NCB, p.n_tiles, (int)bwd_input, ps);
     } else if (kind == K_TF32)
-      prep_weights<K_TF32><<<grid, 256, 0, s>>>(w, hi, nullptr, Ci, Co, K, N, p.BN, p.CPB, p.NCB,
-                                                p.n_tiles, bwd_input, ps);
+      e = launch_pdl(prep_weights<K_TF32>, grid, dim3(256), 0, s, w, hi, (uint8_t *)nullptr, Ci,
+                     Co, K, N, p.BN, p.CPB, p.NCB, p.n_tiles, (int)bwd_input, ps);
     else if (kind == K_BF16X3)
-      prep_weights<K_BF16X3><<<grid, 256, 0, s>>>(w, hi, lo, Ci, Co, K, N, p.BN, p.CPB, p.NCB,
-                                                  p.n_tiles, bwd_input, ps);
+      e = launch_pdl(prep_weights<K_BF16X3>, grid, dim3(256), 0, s, w, hi, lo, Ci, Co, K, N,
+                     p.BN, p.CPB, p.NCB, p.n_tiles, (int)bwd_input, ps);
     else
-      prep_weights<K_BF16><<<grid, 256, 0, s>>>(w, hi, nullptr, Ci, Co, K, N, p.BN, p.CPB, p.NCB,
-                                                p.n_tiles, bwd_input, ps);
-    cudaError_t e = cudaGetLastError();
+      e = launch_pdl(prep_weights<K_BF16>, grid, dim3(256), 0, s, w, hi, (uint8_t *)nullptr, Ci,
+                     Co, K, N, p.BN, p.CPB, p.NCB, p.n_tiles, (int)bwd_input, ps);
+    if (e == cudaSuccess) e = cudaGetLastError();
     note_launch();
     if (e != cudaSuccess) {
       if (!cached) scratch_free(wt, s);

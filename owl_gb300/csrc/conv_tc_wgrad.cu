@@ -114,6 +114,9 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const __grid_cons
   // in one accumulator that rounding is three times that of the hi*hi sums.
   constexpr bool SEP = (KIND == K_BF16X3);
   extern __shared__ __align__(1024) uint8_t smem[];
+  // a programmatic dependent of the work before it: wait for that work (X
+  // and dY may be its output) before any global access
+  asm volatile("griddepcontrol.wait;" ::: "memory");
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int YPL = p.BN * EB / 16;
@@ -388,6 +391,8 @@ __global__ void __launch_bounds__(kThreads, 1) wgrad_tc_kernel(const __grid_cons
 // 16 loads are in flight.
 __global__ void wgrad_reduce(const float *__restrict__ part, float *__restrict__ out, long long n,
                              int R, int vec) {
+  // a programmatic dependent of the kernel that wrote the partials
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   // vec: n % 4 == 0 and `out` 16-byte aligned (the partials always are)
   const long long n4 = vec ? n / 4 : 0;
   const float4 *p4 = reinterpret_cast<const float4 *>(part);
@@ -448,9 +453,11 @@ int launch(const WgParams &p, size_t smem, int grid, cudaStream_t s) {
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemMax));
     attr[dev] = true;
   }
-  wgrad_tc_kernel<KIND><<<grid, kThreads, smem, s>>>(p);
+  cudaError_t e = launch_pdl(wgrad_tc_kernel<KIND>, dim3(grid), dim3(kThreads), smem, s, p);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  note_launch();
   note_tc_launch();
-  OWL_CHECK_LAUNCH("wgrad_tc_kernel");
+  if (e != cudaSuccess) return cuda_fail(e, "wgrad_tc_kernel");
   return kOk;
 }
 
@@ -464,8 +471,11 @@ int sum_partials_f32(const float *part, float *out, long long n, int R, cudaStre
   const bool v4 = n % 4 == 0 && (uintptr_t)out % 16 == 0 && (uintptr_t)part % 16 == 0;
   const long long work = v4 ? n / 4 : n;
   const int blocks = (int)std::max<long long>(1, std::min<long long>((work + 127) / 128, 8 * 152));
-  wgrad_reduce<<<blocks, 128, 0, s>>>(part, out, n, R, v4 ? 1 : 0);
-  OWL_CHECK_LAUNCH("wgrad_reduce");
+  cudaError_t e = launch_pdl(wgrad_reduce, dim3(blocks), dim3(128), 0, s, part, out, n, R,
+                             v4 ? 1 : 0);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  note_launch();
+  if (e != cudaSuccess) return cuda_fail(e, "wgrad_reduce");
   return kOk;
 }
 
@@ -674,8 +684,9 @@ int tc_conv_bwd_kernel(int prec, const ConvGeom &g, const float *x, float *dw, c
     const bool v4 = welems % 4 == 0 && (uintptr_t)dw % 16 == 0;
     const long long work = v4 ? welems / 4 : welems;
     const int blocks = (int)std::max<long long>(1, std::min<long long>((work + 127) / 128, 8 * 152));
-    wgrad_reduce<<<blocks, 128, 0, s>>>(part, dw, welems, p.R, v4 ? 1 : 0);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = launch_pdl(wgrad_reduce, dim3(blocks), dim3(128), 0, s, (const float *)part,
+                               dw, welems, p.R, v4 ? 1 : 0);
+    if (e == cudaSuccess) e = cudaGetLastError();
     note_launch();
     if (e != cudaSuccess) rc = cuda_fail(e, "wgrad_reduce");
   }
