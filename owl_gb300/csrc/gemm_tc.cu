@@ -285,6 +285,8 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(const __grid_const
   constexpr int PARTS = (KIND == stage::K_BF16X3) ? 2 : 1;
   constexpr bool SEP = (KIND == stage::K_BF16X3);
   extern __shared__ __align__(1024) uint8_t smem[];
+  // launched with launch_pdl: the operands may be the previous kernel's output
+  asm volatile("griddepcontrol.wait;" ::: "memory");
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long m0 = (long long)blockIdx.x * kBM, n0 = (long long)blockIdx.y * p.BN;
@@ -468,6 +470,7 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(const __grid_const
 __global__ void gemm_reduce(const float *__restrict__ part, float *__restrict__ out,
                             const float *__restrict__ bias, int act, long long M, long long N,
                             int splits) {
+  asm volatile("griddepcontrol.wait;" ::: "memory");  // launched with launch_pdl
   const long long n_all = M * N;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n_all;
        i += (long long)gridDim.x * blockDim.x) {
@@ -508,10 +511,11 @@ int launch(const GemmParams &p, size_t smem, dim3 grid, cudaStream_t s) {
                                   kSmemMax));
     attr[dev] = true;
   }
-  gemm_tc_kernel<KIND><<<grid, kThreads, smem, s>>>(p);
+  cudaError_t e = launch_pdl(gemm_tc_kernel<KIND>, grid, dim3(kThreads), smem, s, p);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  note_launch();
   note_tc_launch();
-  OWL_CHECK_LAUNCH("gemm_tc_kernel");
-  return kOk;
+  return e == cudaSuccess ? kOk : cuda_fail(e, "gemm_tc_kernel");
 }
 
 }  // namespace
@@ -572,8 +576,9 @@ int gemm_run(int prec, GemmParams p, float *c, cudaStream_t s) {
   if (rc == kOk && p.splits > 1) {
     const long long n_all = M * N;
     const int blocks = (int)std::max<long long>(1, std::min<long long>((n_all + 255) / 256, 4 * 152));
-    gemm_reduce<<<blocks, 256, 0, s>>>(part, c, bias, act, M, N, p.splits);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = launch_pdl(gemm_reduce, dim3(blocks), dim3(256), 0, s, (const float *)part,
+                               c, bias, act, M, N, p.splits);
+    if (e == cudaSuccess) e = cudaGetLastError();
     note_launch();
     if (e != cudaSuccess) rc = cuda_fail(e, "gemm_reduce");
   }

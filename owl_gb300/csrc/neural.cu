@@ -33,6 +33,7 @@ __device__ __forceinline__ T act_fn(T v, int act) {
 template <typename T>
 __global__ void bias_act_kernel(T *__restrict__ y, const T *__restrict__ bias, long long n,
                                 long long C, int act) {
+  asm volatile("griddepcontrol.wait;" ::: "memory");  // launched with launch_pdl
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     T v = y[i];
@@ -50,6 +51,7 @@ template <typename T>
 __global__ void bias_act_bwd_kernel(const T *__restrict__ y, const T *__restrict__ dy,
                                     T *__restrict__ dz, T *__restrict__ partial, long long P,
                                     long long C, long long rows_per_chunk, int act) {
+  asm volatile("griddepcontrol.wait;" ::: "memory");  // launched with launch_pdl
   __shared__ T red[kBiasRows][33];
   const long long c = (long long)blockIdx.x * 32 + threadIdx.x;
   const long long p0 = (long long)blockIdx.y * rows_per_chunk;
@@ -81,6 +83,7 @@ __global__ void bias_act_bwd_kernel(const T *__restrict__ y, const T *__restrict
 template <typename T>
 __global__ void sum_chunks_kernel(const T *__restrict__ partial, T *__restrict__ out, long long C,
                                   int chunks) {
+  asm volatile("griddepcontrol.wait;" ::: "memory");  // launched with launch_pdl
   __shared__ T red[32][33];
   const long long c = (long long)blockIdx.x * 32 + threadIdx.x;
   T s = T(0);
@@ -119,6 +122,7 @@ template <typename T>
 __global__ void softmax_ce_rows(const T *__restrict__ logits, const T *__restrict__ labels,
                                 T *__restrict__ row_loss, T *__restrict__ dlogits,
                                 const T *__restrict__ dloss, long long R, long long C) {
+  asm volatile("griddepcontrol.wait;" ::: "memory");  // launched with launch_pdl
   const long long r = (long long)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   const int lane = threadIdx.x & 31;
   if (r >= R) return;
@@ -145,6 +149,7 @@ __global__ void softmax_ce_rows(const T *__restrict__ logits, const T *__restric
 // loss = (sum over rows of row_loss, in a fixed order) / R, one block of 256.
 template <typename T>
 __global__ void softmax_ce_total(const T *__restrict__ row_loss, T *__restrict__ loss, long long R) {
+  asm volatile("griddepcontrol.wait;" ::: "memory");  // launched with launch_pdl
   __shared__ T part[256];
   T s = T(0);
   const long long per = (R + 255) / 256;
@@ -166,6 +171,7 @@ __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(
 // multiply-add), as the composition rate * g, then w - that, rounds.
 template <typename T>
 __global__ void sgd_kernel(T *__restrict__ w, const T *__restrict__ g, long long n, T lr) {
+  asm volatile("griddepcontrol.wait;" ::: "memory");  // launched with launch_pdl
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
     w[i] = w[i] - mul_rn(lr, g[i]);
@@ -183,9 +189,11 @@ int bad(const char *fn, const char *what) {
 template <typename T>
 int bias_act(T *y, const T *bias, long long n, long long C, int act, cudaStream_t s) {
   if (n == 0 || (!bias && act == OWLGPU_ACT_NONE)) return kOk;
-  bias_act_kernel<T><<<grid_for(n, 256), 256, 0, s>>>(y, bias, n, C, act);
-  OWL_CHECK_LAUNCH("bias_act_kernel");
-  return kOk;
+  cudaError_t e = launch_pdl(bias_act_kernel<T>, dim3(grid_for(n, 256)), dim3(256), 0, s, y,
+                             bias, n, C, act);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  note_launch();
+  return e == cudaSuccess ? kOk : cuda_fail(e, "bias_act_kernel");
 }
 
 // C = op(A) op(B) on the CUDA cores, as a 1x1 convolution with its
@@ -260,14 +268,15 @@ int bias_act_bwd_t(const char *fn, const T *y, const T *dy, T *dz, T *db, long P
     int rc = scratch_alloc((void **)&part, sizeof(T) * (size_t)(chunks * C), s);
     if (rc) return rc;
   }
-  bias_act_bwd_kernel<T><<<dim3((unsigned)ctiles, (unsigned)chunks), dim3(32, kBiasRows), 0, s>>>(
-      y, dy, dz, part, P, C, rows, act);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = launch_pdl(bias_act_bwd_kernel<T>, dim3((unsigned)ctiles, (unsigned)chunks),
+                             dim3(32, kBiasRows), 0, s, y, dy, dz, part, P, C, rows, act);
+  if (e == cudaSuccess) e = cudaGetLastError();
   note_launch();
   int rc = e == cudaSuccess ? kOk : cuda_fail(e, "bias_act_bwd_kernel");
   if (rc == kOk && db) {
-    sum_chunks_kernel<T><<<(unsigned)ctiles, dim3(32, 32), 0, s>>>(part, db, C, (int)chunks);
-    e = cudaGetLastError();
+    e = launch_pdl(sum_chunks_kernel<T>, dim3((unsigned)ctiles), dim3(32, 32), 0, s,
+                   (const T *)part, db, C, (int)chunks);
+    if (e == cudaSuccess) e = cudaGetLastError();
     note_launch();
     if (e != cudaSuccess) rc = cuda_fail(e, "sum_chunks_kernel");
   }
@@ -285,14 +294,17 @@ int softmax_ce_t(const char *fn, const T *logits, const T *labels, T *loss, T *d
   int rc = scratch_alloc((void **)&row_loss, sizeof(T) * (size_t)R, s);
   if (rc) return rc;
   const int rows_per_block = 8;
-  softmax_ce_rows<T><<<(unsigned)((R + rows_per_block - 1) / rows_per_block), 32 * rows_per_block,
-                       0, s>>>(logits, labels, row_loss, dlogits, dloss, R, C);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = launch_pdl(softmax_ce_rows<T>,
+                             dim3((unsigned)((R + rows_per_block - 1) / rows_per_block)),
+                             dim3(32 * rows_per_block), 0, s, logits, labels, row_loss, dlogits,
+                             dloss, R, C);
+  if (e == cudaSuccess) e = cudaGetLastError();
   note_launch();
   rc = e == cudaSuccess ? kOk : cuda_fail(e, "softmax_ce_rows");
   if (rc == kOk && loss) {
-    softmax_ce_total<T><<<1, 256, 0, s>>>(row_loss, loss, R);
-    e = cudaGetLastError();
+    e = launch_pdl(softmax_ce_total<T>, dim3(1), dim3(256), 0, s, (const T *)row_loss, loss,
+                   (long long)R);
+    if (e == cudaSuccess) e = cudaGetLastError();
     note_launch();
     if (e != cudaSuccess) rc = cuda_fail(e, "softmax_ce_total");
   }
@@ -304,9 +316,11 @@ template <typename T>
 int sgd_t(const char *fn, T *w, const T *g, long n, T lr, cudaStream_t s) {
   if (n < 0) return bad(fn, "negative size");
   if (n == 0) return kOk;
-  sgd_kernel<T><<<grid_for(n, 256), 256, 0, s>>>(w, g, n, lr);
-  OWL_CHECK_LAUNCH("sgd_kernel");
-  return kOk;
+  cudaError_t e = launch_pdl(sgd_kernel<T>, dim3(grid_for(n, 256)), dim3(256), 0, s, w, g,
+                             (long long)n, lr);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  note_launch();
+  return e == cudaSuccess ? kOk : cuda_fail(e, "sgd_kernel");
 }
 
 }  // namespace
