@@ -1,7 +1,8 @@
 // conv_simt.cu -- CUDA-core implicit-GEMM convolutions (float32 "plain",
 // float64, complex32 and complex64), forward / backward-input /
-// backward-kernel, 2-D, 3-D, strided, dilated.  No im2col matrix is ever materialised: every GEMM operand element
-// is gathered from the NHWC-style Owl array while the tile is staged into
+// backward-kernel, 2-D, 3-D, strided, dilated.  No im2col matrix is ever
+// materialised: every GEMM operand element is gathered from the NHWC-style
+// Owl array while the tile is staged into
 // shared memory.
 //
 // GEMM views (k = ((kc*KR + kr)*KD + kd)*Ci + ci, Owl's im2col column order,
@@ -45,6 +46,7 @@ template <typename T, int MODE, int BM, int BN, int BK, int TM, int TN>
 __global__ void __launch_bounds__((BM / TM) * (BN / TN))
     conv_simt_kernel(Dev g, const T *__restrict__ A0, const T *__restrict__ B0,
                      T *__restrict__ C, int64_t k_per_split) {
+  asm volatile("griddepcontrol.wait;" ::: "memory");  // launched with launch_pdl
   constexpr int NT = (BM / TM) * (BN / TN);
   constexpr int A_PER = BM * BK / NT;
   constexpr int B_PER = BN * BK / NT;
@@ -331,6 +333,7 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
 template <typename T>
 __global__ void splitk_reduce_kernel(const T *__restrict__ part, T *__restrict__ out,
                                      int64_t n, int splits) {
+  asm volatile("griddepcontrol.wait;" ::: "memory");  // launched with launch_pdl
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (; i < n; i += stride) {
@@ -382,6 +385,7 @@ template <int MODE, int CN>
 __global__ void __launch_bounds__(kVNT, 1)
     conv_f32v_kernel(Dev g, const float *__restrict__ A0, const float *__restrict__ B0,
                      float *__restrict__ C, int64_t k_per_split) {
+  asm volatile("griddepcontrol.wait;" ::: "memory");  // launched with launch_pdl
   using S = F32vShape<CN>;
   constexpr int BM = S::BM, BN = S::BN, RQ = S::RQ, NJ = S::NJ;
   __shared__ __align__(16) float As[2][kVBK][BM];
@@ -658,14 +662,16 @@ int launch_f32v(const Dev &d, const float *A, const float *B, float *C, int spli
   const int cn = d.N > 64 ? 2 : (d.N > 32 ? 1 : 0);
   const int bm = cn == 0 ? 256 : 128, bn = cn == 0 ? 32 : 64 * cn;
   dim3 grid((unsigned)ceil_div(d.M, bm), (unsigned)ceil_div(d.N, bn), (unsigned)splits);
+  cudaError_t e;
   if (cn == 2)
-    conv_f32v_kernel<MODE, 2><<<grid, kVNT, 0, s>>>(d, A, B, C, kps);
+    e = launch_pdl(conv_f32v_kernel<MODE, 2>, grid, dim3(kVNT), 0, s, d, A, B, C, kps);
   else if (cn == 1)
-    conv_f32v_kernel<MODE, 1><<<grid, kVNT, 0, s>>>(d, A, B, C, kps);
+    e = launch_pdl(conv_f32v_kernel<MODE, 1>, grid, dim3(kVNT), 0, s, d, A, B, C, kps);
   else
-    conv_f32v_kernel<MODE, 0><<<grid, kVNT, 0, s>>>(d, A, B, C, kps);
-  OWL_CHECK_LAUNCH("conv_f32v_kernel");
-  return kOk;
+    e = launch_pdl(conv_f32v_kernel<MODE, 0>, grid, dim3(kVNT), 0, s, d, A, B, C, kps);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  note_launch();
+  return e == cudaSuccess ? kOk : cuda_fail(e, "conv_f32v_kernel");
 }
 
 Dev make_dev(const ConvGeom &g, int mode) {
@@ -690,9 +696,11 @@ int launch_cfg(const Dev &d, const T *A, const T *B, T *C, int splits, int64_t k
                cudaStream_t s) {
   constexpr int NT = (BM / TM) * (BN / TN);
   dim3 grid((unsigned)ceil_div(d.M, BM), (unsigned)ceil_div(d.N, BN), (unsigned)splits);
-  conv_simt_kernel<T, MODE, BM, BN, BK, TM, TN><<<grid, NT, 0, s>>>(d, A, B, C, kps);
-  OWL_CHECK_LAUNCH("conv_simt_kernel");
-  return kOk;
+  cudaError_t e = launch_pdl(conv_simt_kernel<T, MODE, BM, BN, BK, TM, TN>, grid, dim3(NT), 0, s,
+                             d, A, B, C, kps);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  note_launch();
+  return e == cudaSuccess ? kOk : cuda_fail(e, "conv_simt_kernel");
 }
 
 // Tile choice by the GEMM's N (output channels for FWD, input channels for
@@ -741,6 +749,7 @@ __global__ void bwdi_class_weights(const T *__restrict__ w, T *__restrict__ w2, 
                                    int Kc, int base_a, int base_b, int base_c, int mul_a,
                                    int mul_b, int mul_c, int KR, int KD, int64_t Ci,
                                    int64_t Co) {
+  asm volatile("griddepcontrol.wait;" ::: "memory");  // launched with launch_pdl
   const int64_t total = (int64_t)Ka * Kb * Kc * Co * Ci;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -759,6 +768,7 @@ __global__ void bwdi_class_weights(const T *__restrict__ w, T *__restrict__ w2, 
 // w2[co][t*Ci + ci] = w[t][ci][co].
 __global__ void window_weights(const float *__restrict__ w, float *__restrict__ w2, int64_t T,
                                int64_t Ci, int64_t Co) {
+  asm volatile("griddepcontrol.wait;" ::: "memory");  // launched with launch_pdl
   const int64_t total = T * Ci * Co;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -807,9 +817,10 @@ int bwdi_window_f32(const ConvGeom &g, float *dx, const float *w, const float *d
   int rc = scratch_alloc((void **)&w2, sizeof(float) * (size_t)g.w_elems(), s);
   if (rc) return rc;
   const int64_t nw = g.w_elems();
-  window_weights<<<(unsigned)std::min<int64_t>(ceil_div(nw, 256), 1024), 256, 0, s>>>(
-      w, w2, g.taps(), g.Ci, g.Co);
-  cudaError_t e = cudaGetLastError();
+  const dim3 wgrid((unsigned)std::min<int64_t>(ceil_div(nw, 256), 1024));
+  cudaError_t e = launch_pdl(window_weights, wgrid, dim3(256), 0, s, w, w2, (int64_t)g.taps(),
+                             (int64_t)g.Ci, (int64_t)g.Co);
+  if (e == cudaSuccess) e = cudaGetLastError();
   note_launch();
   if (e != cudaSuccess) rc = cuda_fail(e, "window_weights");
   if (rc == kOk) rc = launch_f32v<FWD>(d, dy, w2, dx, 1, d.K, s);
@@ -876,10 +887,11 @@ int bwdi_t(const ConvGeom &g, T *dx, const T *w, const T *dy, cudaStream_t s) {
         const Axis a = axis_class(0, r0), b = axis_class(1, r1), c = axis_class(2, r2);
         if (a.n == 0 || b.n == 0 || c.n == 0 || a.out * b.out * c.out == 0) continue;
         const int64_t nw = (int64_t)a.n * b.n * c.n * g.Co * g.Ci;
-        bwdi_class_weights<T><<<(unsigned)std::min<int64_t>(ceil_div(nw, 256), 1024), 256, 0, s>>>(
-            w, w2, a.n, b.n, c.n, a.base, b.base, c.base, a.mul, b.mul, c.mul, (int)g.KR,
-            (int)g.KD, g.Ci, g.Co);
-        cudaError_t e = cudaGetLastError();
+        cudaError_t e = launch_pdl(
+            bwdi_class_weights<T>, dim3((unsigned)std::min<int64_t>(ceil_div(nw, 256), 1024)),
+            dim3(256), 0, s, w, w2, a.n, b.n, c.n, a.base, b.base, c.base, a.mul, b.mul, c.mul,
+            (int)g.KR, (int)g.KD, (int64_t)g.Ci, (int64_t)g.Co);
+        if (e == cudaSuccess) e = cudaGetLastError();
         note_launch();
         if (e != cudaSuccess) {
           rc = cuda_fail(e, "bwdi_class_weights");
@@ -934,8 +946,9 @@ int splitk_t(const ConvGeom &g, const T *A, const T *B, T *C, cudaStream_t s) {
   if (rc == kOk) {
     int64_t n = d.M * d.N;
     int blocks = (int)std::min<int64_t>(ceil_div(n, 256), 4 * 152);
-    splitk_reduce_kernel<T><<<blocks, 256, 0, s>>>((const T *)ws, C, n, splits);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = launch_pdl(splitk_reduce_kernel<T>, dim3(blocks), dim3(256), 0, s,
+                               (const T *)ws, C, (int64_t)n, splits);
+    if (e == cudaSuccess) e = cudaGetLastError();
     note_launch();
     if (e != cudaSuccess) rc = cuda_fail(e, "splitk_reduce_kernel");
   }
@@ -974,9 +987,11 @@ int bwdk_f32_into(const ConvGeom &g, const float *x, float *dw, const float *dy,
   if (rc != kOk) return rc;
   int64_t n = d.M * d.N;
   int blocks = (int)std::min<int64_t>(ceil_div(n, 256), 4 * 152);
-  splitk_reduce_kernel<float><<<blocks, 256, 0, s>>>(ws, dw, n, splits);
-  OWL_CHECK_LAUNCH("splitk_reduce_kernel");
-  return kOk;
+  cudaError_t e = launch_pdl(splitk_reduce_kernel<float>, dim3(blocks), dim3(256), 0, s,
+                             (const float *)ws, dw, (int64_t)n, splits);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  note_launch();
+  return e == cudaSuccess ? kOk : cuda_fail(e, "splitk_reduce_kernel");
 }
 
 }  // namespace
