@@ -132,6 +132,11 @@ struct TcParams {
   const float *bias;
   int act;
   long long spin_limit;  // cycles a pipeline wait polls before the CTA gives up
+  // 1: launched as a programmatic dependent of arbitrary earlier work (a
+  // cached weight image, no prep_weights before it): every thread waits for
+  // that work before any global access.  0: the dependent of prep_weights,
+  // which itself waited for the earlier work; only the weight loader waits.
+  int wait_all;
 };
 
 __device__ int g_tc_status;
@@ -196,6 +201,7 @@ __device__ __forceinline__ uint32_t to_tf32(float a) {
 // constant offset of the parameters).
 template <int KIND, bool MULTI>
 __global__ void __launch_bounds__(kThreads, 1) conv_tc_kernel(const __grid_constant__ TcParams p) {
+  if (p.wait_all) asm volatile("griddepcontrol.wait;" ::: "memory");
   constexpr int EPC = (KIND == K_TF32) ? 4 : 8;  // channels per 16-byte chunk
   constexpr int PARTS = (KIND == K_BF16X3) ? 2 : 1;
   // BF16X3 keeps the cross terms in an accumulator of their own: the tensor
@@ -1076,7 +1082,7 @@ int launch(const TcParams &p, size_t smem, cudaStream_t s, bool after_prep) {
     attr_set[dev] = true;
   }
   int grid = (int)std::min<long long>(p.total_tiles, num_sms());
-  // programmatic dependent launch on prep_weights (launched just before)
+  // programmatic dependent launch (on prep_weights when it ran just before)
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(kThreads);
@@ -1086,10 +1092,12 @@ int launch(const TcParams &p, size_t smem, cudaStream_t s, bool after_prep) {
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
+  cfg.numAttrs = 1;
   // a cached weight image has no prep_weights launch before the kernel:
-  // then it is an ordinary launch, ordered after everything on the stream
-  cfg.numAttrs = after_prep ? 1 : 0;
-  cudaError_t e = cudaLaunchKernelEx(&cfg, conv_tc_kernel<KIND, MULTI>, p);
+  // then every thread waits for the earlier work (wait_all)
+  TcParams q = p;
+  q.wait_all = after_prep ? 0 : 1;
+  cudaError_t e = cudaLaunchKernelEx(&cfg, conv_tc_kernel<KIND, MULTI>, q);
   note_launch();
   note_tc_launch();
   if (e != cudaSuccess) return cuda_fail(e, "conv_tc_kernel");
