@@ -468,6 +468,40 @@ __global__ void __launch_bounds__(kVNT, 1)
     }
   };
 
+  // BWDK: in the loop, decode thread tid (< 16) decodes pixel dp = (slab j +
+  // 2)'s pixel tid, one slab further each step: (b, oc, orr*OD + od) advance
+  // by adding 16 to the last with carries, no division per slab
+  int64_t dp = 0, db = 0, doc = 0, dq = 0;
+  const int64_t ORD = g.OR * g.OD;
+  if (MODE == BWDK && tid < kVBK) {
+    dp = k_begin + 2 * kVBK + tid;
+    int64_t t = dp;
+    dq = t % ORD;
+    t /= ORD;
+    doc = t % g.OC;
+    db = t / g.OC;
+  }
+  auto decode_next = [&](int slot, int buf) {
+    if (dp < k_end) {
+      const int64_t orr = g.OD == 1 ? dq : dq / g.OD, od = dq - orr * g.OD;
+      s_base[buf][slot] = db * img;
+      s_c[buf][slot] = (int)(doc * g.sc) - g.pc;
+      s_r[buf][slot] = (int)(orr * g.sr) - g.pr;
+      s_d[buf][slot] = (int)(od * g.sd) - g.pd;
+    } else {
+      s_base[buf][slot] = -1;
+    }
+    dp += kVBK;
+    dq += kVBK;
+    while (dq >= ORD) {
+      dq -= ORD;
+      if (++doc == g.OC) {
+        doc = 0;
+        ++db;
+      }
+    }
+  };
+
   // FWD slab position: tap (kc, kr, kd) and first channel ci0 of slab k0
   int kc = 0, kr = 0, kd = 0;
   int64_t ci0 = 0;
@@ -578,7 +612,7 @@ __global__ void __launch_bounds__(kVNT, 1)
       const bool more = kn < k_end;
       if (more) load(kn, buf ^ 1);  // BWDK: slab kn's pixels sit in buffer buf ^ 1
       // BWDK: decode slab kn + 16 into this slab's (now unused) buffer
-      if (MODE == BWDK && tid < kVBK) decode(kn + kVBK + tid, tid, buf);
+      if (MODE == BWDK && tid < kVBK) decode_next(tid, buf);  // pixel kn + 16 + tid
 #pragma unroll
       for (int k = 0; k < kVBK; ++k) {
         const int sw = MODE == FWD ? ((k >> 2) << 3) : 0;
