@@ -1,6 +1,7 @@
 // conv_tc.cu -- tcgen05 tensor-core convolutions for float32 data
-// (precisions BF16, TF32 and split BF16 "BF16X3"), forward and backward-input,
-// stride 1, any dilation, 2-D and 3-D.
+// (precisions BF16, TF32 and split BF16 "BF16X3"): forward at any stride and
+// dilation, backward-input (stride 1 directly, larger strides as residue
+// classes), 2-D and 3-D.
 //
 // Design: persistent, warp-specialised "halo" implicit GEMM.
 //   * An output tile is TU positions along one spatial axis (u) by 8 along
@@ -21,8 +22,9 @@
 //     exact shared-memory image of each (channel block, tap) B tile, which one
 //     thread streams with cp.async.bulk (TMA engine) into a ring of stages.
 //   * One thread issues tcgen05.mma (M=128 channels, N=8*TU pixels, K=16/8
-//     per instruction) into a double-buffered TMEM accumulator; four epilogue
-//     warps drain the other buffer (tcgen05.ld, one TMEM lane per output
+//     per instruction) into a TMEM accumulator, double-buffered when two fit
+//     TMEM's 512 columns; four epilogue warps drain the finished buffer
+//     (tcgen05.ld, one TMEM lane per output
 //     channel) and write float32 results to HBM, 32 consecutive channels of a
 //     pixel per warp store.
 //   * Every wait is bounded: a stuck barrier sets an error word and the CTA

@@ -1,6 +1,6 @@
 // conv_tc_wgrad.cu -- tcgen05 backward-kernel (weight gradient) for float32
-// data in BF16, TF32 or split-BF16 precision, strides up to 8, any dilation,
-// 2-D/3-D.
+// data in BF16 or split-BF16 precision (a TF32 request runs split-BF16),
+// strides up to 8, any dilation, 2-D/3-D.
 //
 //   dW[t][ci][co] = sum over output pixels p of X[p + off(t)][ci] * dY[p][co]
 //
