@@ -66,9 +66,10 @@ static bool tc_requested(Dtype dt, int prec) { return dt == F32 && prec != OWLGP
 static thread_local int t_last_path = -1;
 
 // A float32 request for tensor-core precision runs on tcgen05 when the
-// geometry is one the tensor-core kernels implement (stride 1 today);
-// otherwise it runs on the FP32 CUDA-core kernels, which are at least as
-// accurate.  The path taken is visible through owlgpu_last_conv_path().
+// geometry is one the tensor-core kernels implement (strides up to 8, a halo
+// that fits shared memory, no empty extents); otherwise it runs on the FP32
+// CUDA-core kernels, which are at least as accurate.  The path taken is
+// visible through owlgpu_last_conv_path().
 int conv_fwd(Dtype dt, int prec, const ConvGeom &g, const void *x, const void *w, void *y,
              cudaStream_t s, const void *bias, int act) {
   if (tc_requested(dt, prec) && prec != OWLGPU_PREC_TF32) {
