@@ -13,7 +13,7 @@ accuracy bar the served results are reported at)."""
 import numpy as np
 import pytest
 
-from gpu_util import from_dev, rel, to_dev
+from gpu_util import from_dev, rel
 
 pytestmark = pytest.mark.gpu
 

@@ -6,7 +6,6 @@ import os
 import socket
 
 import numpy as np
-import pytest
 
 from owl_gb300.replicas import shard
 

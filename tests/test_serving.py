@@ -5,8 +5,8 @@ batching), and the residual stack on the oracle (batch independence)."""
 import numpy as np
 import pytest
 
-from owl_gb300.serving import (BUCKETS, Request, ResidualStack, Scheduler, bucket_for,
-                               init_stack, poisson_stream, stack_flops, stack_layers)
+from owl_gb300.serving import (Request, ResidualStack, Scheduler, bucket_for, init_stack,
+                               poisson_stream, stack_flops, stack_layers)
 
 
 class FakeClock:
