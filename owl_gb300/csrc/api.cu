@@ -371,15 +371,19 @@ static int host_call(std::vector<Buf> bufs, int64_t batch, int chunks, F body,
       if (e != cudaSuccess) { rc = cuda_fail(e, "cudaMemcpyAsync(H2D)"); break; }
     }
     if (rc) break;
+    // errors leave the loop (not the function): the scratch buffers are
+    // freed and the streams synchronised below on every path
     if (!one) {
-      OWL_CUDA(cudaEventRecord(ein, hs->cin));
-      OWL_CUDA(cudaStreamWaitEvent(hs->s, ein, 0));
+      cudaError_t e = cudaEventRecord(ein, hs->cin);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(hs->s, ein, 0);
+      if (e != cudaSuccess) { rc = cuda_fail(e, "cudaStreamWaitEvent(copy-in)"); break; }
     }
     rc = body(ptrs, b0, b1 - b0, hs->s);
     if (rc) break;
     if (!one) {
-      OWL_CUDA(cudaEventRecord(ecomp, hs->s));
-      OWL_CUDA(cudaStreamWaitEvent(hs->cout, ecomp, 0));
+      cudaError_t e = cudaEventRecord(ecomp, hs->s);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(hs->cout, ecomp, 0);
+      if (e != cudaSuccess) { rc = cuda_fail(e, "cudaStreamWaitEvent(compute)"); break; }
     }
     for (auto &b : bufs) {
       if (!b.out || !b.batched || b.bytes == 0) continue;
